@@ -1,0 +1,214 @@
+"""Seeded generators for the CU-BENs benchmark models, written as model_def.txt text.
+
+Every generator returns the text of a ``model_def.txt`` in the positional,
+comma-separated layout that the reference reads:
+
+* header and element counts          main.c:340-433
+* incidences and constraints        model.c:95-264 (``struc``)
+* joint coordinates                  main.c:1395-1397
+* truss / shell properties           truss.c:66, shell.c:61
+* joint loads                        model.c:1313-1335 (``load``)
+* MSAL control block                 arc.c:48, main.c:2240-2245
+
+The generators are deterministic. The only random input (the panel imperfection)
+comes from ``numpy.random.default_rng(seed)``, and the seed is part of the
+returned ``ModelSpec``.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class MsalControls:
+    """MSAL parameters in the order main.c:2240-2245 reads them."""
+
+    joint: int            # joint of the initially prescribed displacement (1-based)
+    direction: int        # 1..6
+    dk: float             # initially prescribed displacement
+    alpha: float = 1.0
+    psi_thresh: float = 0.1
+    iteopt: int = 6
+    lpfmax: float = 1e9
+    dkimax: float = 1e9
+    itemax: int = 20
+    submax: int = 10
+    imagmax: int = 10
+    negmax: int = 10
+    toldisp: float = 1e-6
+    tolforc: float = 1.0
+    tolener: float = 1e-6
+
+    def lines(self) -> list[str]:
+        return [
+            f"{self.joint},{self.direction},{self.dk!r}",
+            f"{self.alpha!r}",
+            f"{self.psi_thresh!r}",
+            f"{self.iteopt}",
+            f"{self.lpfmax!r},{self.dkimax!r}",
+            f"{self.itemax},{self.submax},{self.imagmax},{self.negmax}",
+            f"{self.toldisp!r},{self.tolforc!r},{self.tolener!r}",
+        ]
+
+
+@dataclass
+class ModelSpec:
+    name: str
+    text: str
+    nj: int
+    ne_tr: int = 0
+    ne_fr: int = 0
+    ne_sh: int = 0
+    seed: int | None = None
+    params: dict = field(default_factory=dict)
+
+
+def _fmt(v: float) -> str:
+    # repr() round-trips a double exactly through the reference's "%lf" fscanf.
+    return repr(float(v))
+
+
+def space_truss(bays: int = 10, bay: float = 3.0, depth: float = 1.5,
+                emod: float = 200e9, area: float = 1.0e-3, load: float = -10e3,
+                controls: MsalControls | None = None) -> ModelSpec:
+    """Double-layer square space truss (10x10 bays of 3.0 m, depth 1.5 m).
+
+    The top grid has (bays+1)^2 joints and the bottom grid bays^2 joints offset
+    by half a bay. Top and bottom chords run along both axes; every bottom joint
+    has four diagonals to the top corners of its bay. Perimeter top joints are
+    pinned (translations fixed); every interior top joint carries ``load`` in
+    direction 3. Truss joints expose DOF 1-3 only (model.c:267-285).
+    """
+    nb = bays
+    nodes: list[tuple[float, float, float]] = []
+    top: dict[tuple[int, int], int] = {}
+    bot: dict[tuple[int, int], int] = {}
+    for i in range(nb + 1):
+        for j in range(nb + 1):
+            nodes.append((bay * i, bay * j, depth))
+            top[(i, j)] = len(nodes)
+    for i in range(nb):
+        for j in range(nb):
+            nodes.append((bay * i + bay / 2, bay * j + bay / 2, 0.0))
+            bot[(i, j)] = len(nodes)
+    el: list[tuple[int, int]] = []
+    for i in range(nb + 1):
+        for j in range(nb):
+            el.append((top[(i, j)], top[(i, j + 1)]))
+            el.append((top[(j, i)], top[(j + 1, i)]))
+    for i in range(nb):
+        for j in range(nb - 1):
+            el.append((bot[(i, j)], bot[(i, j + 1)]))
+            el.append((bot[(j, i)], bot[(j + 1, i)]))
+    for i in range(nb):
+        for j in range(nb):
+            for di in (0, 1):
+                for dj in (0, 1):
+                    el.append((bot[(i, j)], top[(i + di, j + dj)]))
+    cons: list[str] = []
+    loads: list[str] = []
+    for (i, j), k in sorted(top.items(), key=lambda kv: kv[1]):
+        if i in (0, nb) or j in (0, nb):
+            cons += [f"{k},{d}" for d in (1, 2, 3)]
+        else:
+            loads.append(f"{k},3,{_fmt(load)}")
+    centre = top[(nb // 2, nb // 2)]
+    if controls is None:
+        controls = MsalControls(joint=centre, direction=3, dk=-0.005,
+                                toldisp=1e-10, tolforc=1.0, tolener=1e-10,
+                                itemax=20)
+    out = ["2", "3", "0", "1", str(len(nodes)), f"{len(el)},0,0,0,0"]
+    out += [f"{a},{b}" for a, b in el]
+    out += cons + ["0,0"]
+    out += [f"{_fmt(x)},{_fmt(y)},{_fmt(z)}" for x, y, z in nodes]
+    out += [f"{_fmt(emod)},{_fmt(area)},7850.0,1e30"] * len(el)
+    out += loads + ["0,0,0"]
+    out += controls.lines()
+    return ModelSpec("space_truss", "\n".join(out) + "\n", nj=len(nodes),
+                     ne_tr=len(el), params={"bays": nb, "centre": centre})
+
+
+PANEL_R = 2540.0
+PANEL_L = 508.0
+PANEL_THETA = 0.2
+PANEL_T = 12.7
+PANEL_E = 3102.75
+PANEL_NU = 0.3
+
+
+def imperfection_amplitudes(seed: int, scale: float) -> np.ndarray:
+    """Four sine-mode amplitudes ~ U(-scale, scale) * thickness, seeded."""
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-scale, scale, size=4) * PANEL_T
+
+
+# (m, p) sine modes of the imperfection, axial x angular; the builder's choice.
+IMPERFECTION_MODES = ((1, 1), (1, 2), (2, 1), (2, 2))
+
+
+def cylindrical_panel(n: int = 64, seed: int | None = None, imperfection: float = 0.0,
+                      load: float = -1.0, controls: MsalControls | None = None,
+                      radius: float = PANEL_R, length: float = PANEL_L,
+                      theta: float = PANEL_THETA, thick: float = PANEL_T,
+                      emod: float = PANEL_E, nu: float = PANEL_NU) -> ModelSpec:
+    """Hinged cylindrical DKT shell panel on an n x n quad grid (2 n^2 triangles).
+
+    Joints are (x_i, R sin a_j, R cos a_j - R) with x_i = L i/n along the axis and
+    a_j = -theta/2 + theta j/n; joint (i, j) is number i*(n+1)+j+1. Each quad
+    (a,b,c,d) splits into (a,b,c) and (a,c,d). Both straight (axial) edges
+    j=0 and j=n have translations 1-3 fixed; the curved edges are free. The
+    centre joint carries ``load`` in direction 3. With ``seed`` given, a radial
+    imperfection sum_k A_k sin(m_k pi x/L) sin(p_k pi (a+theta/2)/theta) is
+    added, A_k ~ U(-imperfection, imperfection) * thickness.
+    """
+    amps = np.zeros(4)
+    if seed is not None and imperfection > 0:
+        amps = imperfection_amplitudes(seed, imperfection)
+    nodes = []
+    for i in range(n + 1):
+        x = length * i / n
+        for j in range(n + 1):
+            a = -theta / 2 + theta * j / n
+            w = 0.0
+            for (m, p), amp in zip(IMPERFECTION_MODES, amps):
+                w += amp * math.sin(m * math.pi * x / length) * math.sin(p * math.pi * (a + theta / 2) / theta)
+            r = radius + w
+            nodes.append((x, r * math.sin(a), r * math.cos(a) - radius))
+
+    def idx(i: int, j: int) -> int:
+        return i * (n + 1) + j + 1
+
+    tris = []
+    for i in range(n):
+        for j in range(n):
+            a, b, c, d = idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)
+            tris.append((a, b, c))
+            tris.append((a, c, d))
+    cons = []
+    for i in range(n + 1):
+        for j in (0, n):
+            for dr in (1, 2, 3):
+                cons.append(f"{idx(i, j)},{dr}")
+    centre = idx(n // 2, n // 2)
+    if controls is None:
+        controls = MsalControls(joint=centre, direction=3, dk=-0.5)
+    out = ["2", "3", "0", "1", str(len(nodes)), f"0,0,{len(tris)},0,0"]
+    out += [f"{a},{b},{c}" for a, b, c in tris]
+    out += cons + ["0,0"]
+    out += [f"{_fmt(x)},{_fmt(y)},{_fmt(z)}" for x, y, z in nodes]
+    out += [f"{_fmt(emod)},{_fmt(nu)},{_fmt(thick)},1.0,1e30"] * len(tris)
+    out += [f"{centre},3,{_fmt(load)}", "0,0,0"]
+    out += controls.lines()
+    return ModelSpec(f"panel{n}", "\n".join(out) + "\n", nj=len(nodes), ne_sh=len(tris),
+                     seed=seed, params={"n": n, "centre": centre,
+                                        "imperfection_amplitudes": amps.tolist()})
+
+
+def batch_sizes(count: int = 512, seed: int = 2024,
+                choices: tuple[int, ...] = tuple(range(16, 97, 8))) -> list[int]:
+    """Mesh sizes drawn uniformly from {16, 24, ..., 96}, seeded."""
+    rng = np.random.default_rng(seed)
+    return [int(v) for v in rng.choice(np.array(choices), size=count)]
