@@ -1,0 +1,184 @@
+// Internal declarations shared by the host driver and the kernel files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "cubens_gb300.h"
+
+namespace cb {
+
+// ---------------------------------------------------------------------------
+// Host-side model: what main() builds during setup (main.c:330-1648)
+// ---------------------------------------------------------------------------
+struct HostModel {
+    long nj = 0, ne_tr = 0, ne_fr = 0, ne_sh = 0, neq = 0, lss = 0, bw = 0;
+    std::vector<long> jcode;   // NJ*7, 1-based equation numbers, 0 = fixed
+    std::vector<long> maxa;    // NEQ+1, 1-based skyline diagonal addresses
+    std::vector<double> x0;    // NJ*3
+    std::vector<double> q;     // NEQ
+    std::vector<int> tr_conn;  // NE_TR*2 (0-based joints)
+    std::vector<double> tr_e, tr_a;
+    std::vector<int> sh_conn;  // NE_SH*3
+    std::vector<double> sh_e, sh_nu, sh_t;
+    // MSAL controls (arc.c:48, main.c:2240-2245)
+    long dkdof = -1;
+    double dk = 0, alpha = 1, psi_thresh = 0.1, lpfmax = 0, dkimax = 0;
+    double toldisp = 1, tolforc = 1, tolener = 1;
+    int iteopt = 6, itemax = 20, submax = 10, imagmax = 10, negmax = 10;
+};
+
+// Parse a model_def text; returns an empty string on success, else the reason.
+std::string parse_model_def(const char *text, size_t len, HostModel &m, int &status);
+
+// Gather lists: out[i] = sum_{k in ptr[i]..ptr[i+1]} src[idx[k]] in list order.
+struct GatherMap {
+    std::vector<int> ptr;   // n+1
+    std::vector<int> src;   // contributions, in the reference's accumulation order
+    std::vector<int64_t> dst;  // destination slot per row (band map only)
+};
+
+// Force assembly: eq -> contributions into the per-element force buffer.
+// Tangent assembly: band slot -> contributions into the per-element matrix buffer.
+void build_force_map(const HostModel &m, GatherMap &g);
+void build_tangent_map(const HostModel &m, long ld, GatherMap &g);
+
+// ---------------------------------------------------------------------------
+// Device buffers
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+};
+
+// Shell element data, structure-of-arrays (index k*E + e).
+struct DevShell {
+    int *conn = nullptr;       // 3*E
+    int *eq = nullptr;         // 18*E, 0-based equation or -1
+    double *prop = nullptr;    // 3*E: E, nu, t
+    double *xl = nullptr;      // 3*E initial local x2, x3, y3
+    double *kem = nullptr;     // 36*E membrane stiffness
+    double *keb = nullptr;     // 81*E bending stiffness
+    double *c_c = nullptr, *c_ip = nullptr, *c_i = nullptr;     // 9*E triads
+    double *a_c = nullptr, *a_i = nullptr;                      // E areas
+    double *ef_c = nullptr, *ef_ip = nullptr, *ef_i = nullptr;  // 18*E element forces
+};
+
+struct DevTruss {
+    int *conn = nullptr;     // 2*T
+    int *eq = nullptr;       // 6*T
+    double *ea = nullptr;    // T: E*A
+    double *len0 = nullptr;  // T
+    double *len_c = nullptr, *len_i = nullptr;  // T
+    double *dir_c = nullptr, *dir_i = nullptr;  // 3*T
+    double *n_c = nullptr, *n_i = nullptr;      // T: axial force ef[0]
+};
+
+// The band LDL^T factor in precision T and its block-bidiagonal inverse form.
+struct BandFactor {
+    long n = 0, bw = 0, ld = 0;  // lower band L[j*ld + (i-j)], 0 <= i-j <= bw
+    long s = 0, nblk = 0;        // block size (>= bw, multiple of 32) and block count
+    void *band = nullptr;        // ld * npad elements
+    void *dinv = nullptr;        // npad: 1/d
+    void *linv = nullptr;        // nblk * s*s: inverse of the unit-lower diagonal block
+    void *pmat = nullptr;        // nblk * s*s: P_i = Linv_i L_{i,i-1}   (row-major)
+    void *rmat = nullptr;        // nblk * s*s: R_i = L_{i+1,i} Linv_i (stored transposed)
+    void *work = nullptr;        // 2 * npad solve work vectors
+    double *ssd = nullptr;       // n pivots (FP64 copy)
+    int *flags = nullptr;        // [0] det (any pivot <= 0), [1] zero pivot seen
+    bool fp32 = false;
+    int inv_width = 32;          // columns per CTA of the block inversion
+    cudaGraphExec_t factor_graph = nullptr;
+    long factor_launches = 0;
+    struct SolveGraph {
+        const double *in = nullptr;  // pointers baked into the graph
+        double *out = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        long launches = 0;
+    } solve_graphs[4];
+};
+
+void band_alloc(BandFactor &f, long n, long bw, bool fp32);
+void band_free(BandFactor &f);
+// Factor the band in place: pivots to f.ssd, det/zero flags to f.flags.
+void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches);
+// Solve K x = rhs with the factor (rhs, x: FP64 device vectors of length n).
+void band_solve(BandFactor &f, const double *rhs, double *x, cudaStream_t st, bool use_graph,
+                long *launches);
+
+// ---------------------------------------------------------------------------
+// Kernel entry points (host wrappers)
+// ---------------------------------------------------------------------------
+void launch_shell_setup(const DevShell &s, const double *x0, long ne, cudaStream_t st);
+void launch_shell_forces(const DevShell &s, const double *x_t, const double *dd, double *fe,
+                         long ne, cudaStream_t st);
+void launch_truss_forces(const DevTruss &t, const double *x_t, double *fe, long nt,
+                         cudaStream_t st);
+template <typename T>
+void launch_shell_tangent(const DevShell &s, const double *x_c, T *kel, long ne, cudaStream_t st);
+template <typename T>
+void launch_truss_tangent(const DevTruss &t, T *kel, long nt, cudaStream_t st);
+void launch_gather_f64(const int *ptr, const int *src, const double *in, double *out, long n,
+                       cudaStream_t st);
+template <typename T>
+void launch_gather_band(const int *ptr, const int *src, const int64_t *dst, const T *in, T *band,
+                        long nslots, cudaStream_t st);
+void launch_update_coords(const int *eq_x, const double *dd, double *x_t, long neq,
+                          cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Arc-length vector algebra (vecops.cu)
+// ---------------------------------------------------------------------------
+// Scalars the device-side steps of one iteration exchange. The host reads
+// the block back once per iteration.
+struct MsalScalars {
+    double dots[16];     // latest fused reductions (see the kernels for the slots)
+    double lam_t;        // lpf_temp
+    double lam_old;      // lpf_temp when the residual was formed (qtot = lam_old q)
+    double root;         // dlpf chosen by quad
+    double a, arc, lamp, qq;  // inputs of quad (set by the host)
+    int psi_ge;          // psi >= psi_thresh
+    int quad_status;     // 0 ok, 2 imaginary roots, 3 both gammas <= 0 (arc.c:70-157)
+    int convchk;         // misc.c:187-250
+    int test_err;        // 1 when a denominator of the test is zero
+    double toldisp, tolforc, tolener, intener1;
+};
+
+constexpr int kRedBlocks = 148;  // fixed partial-sum grid: bit-reproducible reductions
+
+// r = lam_t q - f; records lam_old = lam_t
+void launch_residual(const double *q, const double *f, double *r, MsalScalars *sc, long n,
+                     cudaStream_t st);
+// dots for b, c and the quad gammas over (d_temp, dp, ddr, ddq) -> sc->dots[0..11]
+void launch_quad_dots(const double *dt, const double *dp, const double *ddr, const double *ddq,
+                      double *partial, MsalScalars *sc, long n, cudaStream_t st);
+// quad (arc.c:70-157) on the device: root, status, lam_t += root
+void launch_quad(const double *partial, MsalScalars *sc, cudaStream_t st);
+// dd = ddr + root ddq; d_temp = (d_temp - dp + dd) + dp; x_t += dd (translations)
+void launch_quad_update(const double *ddr, const double *ddq, const double *dp, double *dt,
+                        double *dd, const int *eq_x, double *x_t, const MsalScalars *sc, long n,
+                        cudaStream_t st);
+// test dots (misc.c:187-250) -> sc->dots[0..6] and convchk
+void launch_test(const double *dd, const double *dt, const double *dp, const double *q,
+                 const double *f, const double *fp, const double *fip, double *partial,
+                 MsalScalars *sc, long n, cudaStream_t st);
+// generic: sc->dots[slot] = a . b (b == nullptr: a . a; diff: (a-b).(a-b))
+void launch_dot(const double *a, const double *b, double *partial, MsalScalars *sc, int slot,
+                long n, cudaStream_t st, bool diff = false);
+// first increment corrector (main.c:2355-2370): dl = -ddr[k]/ddq[k]; lam_t += dl;
+// dd = ddr + dl ddq; d += dd; x_t += dd
+void launch_first_update(const double *ddr, const double *ddq, long kdof, double *d, double *dd,
+                         const int *eq_x, double *x_t, MsalScalars *sc, long n, cudaStream_t st);
+// psi = min(1, min_i |ssd_i / ssd_o_i|) -> sc->dots[slot]
+void launch_psi(const double *ssd, const double *ssd_o, double *partial, MsalScalars *sc, int slot,
+                long n, cudaStream_t st);
+// y = alpha * x
+void launch_scale(const double *x, double alpha, double *y, long n, cudaStream_t st);
+// y += alpha * x
+void launch_axpy(const double *x, double alpha, double *y, long n, cudaStream_t st);
+
+}  // namespace cb

@@ -1,0 +1,899 @@
+// Resident model and the GPU-resident modified spherical arc-length driver.
+//
+// The host keeps the scalar control flow of main.c:2158-3141 (step-size
+// control, subdivision counters, acceptance); every vector and element
+// operation runs on the GPU, and the host reads one small scalar block back
+// per Newton iteration. State that the reference keeps as "converged" (x,
+// c, ef, deffarea, defllen) and "current/previous iteration" (x_temp, c_i,
+// c_ip, ef_i, ef_ip) arrays is kept in the same three roles on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "cubens_gb300.h"
+#include "internal.hpp"
+
+#define CB_CUDA(x)                                                                         \
+    do {                                                                                   \
+        cudaError_t e_ = (x);                                                              \
+        if (e_ != cudaSuccess)                                                             \
+            throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + \
+                                     " at " __FILE__ ":" + std::to_string(__LINE__));      \
+    } while (0)
+
+struct cb_status_error : std::runtime_error {
+    int code;
+    cb_status_error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+struct cb_model {
+    cb::HostModel h;
+    cb_options opt{};
+    std::string err;
+    cudaStream_t st = nullptr;
+    size_t bytes = 0;
+    std::vector<void *> allocs;
+
+    // nodes and equations
+    double *x0 = nullptr, *x_c = nullptr, *x_t = nullptr;
+    int *eq_x = nullptr;
+    // global vectors (NEQ)
+    double *q = nullptr, *d = nullptr, *dp = nullptr, *dpp = nullptr, *ddq = nullptr, *ddr = nullptr,
+           *dd = nullptr, *dt = nullptr, *r = nullptr, *f = nullptr, *zero = nullptr, *ssd_o = nullptr;
+    double *fcur = nullptr, *fprev = nullptr;  // f_temp and f_ip
+    // elements
+    cb::DevShell sh;
+    cb::DevTruss tr;
+    double *fe = nullptr;   // element force contributions
+    void *kel = nullptr;    // element tangents
+    int *fmap_ptr = nullptr, *fmap_src = nullptr;
+    int *tmap_ptr = nullptr, *tmap_src = nullptr;
+    int64_t *tmap_dst = nullptr;
+    long tmap_n = 0;
+    cb::BandFactor bf;
+    cb::MsalScalars *sc = nullptr, *sc_h = nullptr;
+    double *partial = nullptr;
+
+    // host control state (main.c:2205-2230)
+    int phase = 0;  // 0 created, 1 first increment done
+    double lpf = 0, lpfp = 0, lpfpp = 0, beta = 0, psi = 1, dnormallow = 0, dnorm = 0, arc = 0, qq = 0;
+    double dkc = 0, lpfc = 0;
+    int errchk2 = 0, subcnt = 0, imagcnt = 0, negcnt = 0, itecnt = 0;
+
+    // timing
+    bool timing = false;
+    cb_timers tm{};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+
+    template <typename T>
+    T *alloc(size_t n)
+    {
+        void *p = nullptr;
+        size_t b = std::max<size_t>(1, n) * sizeof(T);
+        CB_CUDA(cudaMalloc(&p, b));
+        CB_CUDA(cudaMemsetAsync(p, 0, b, st));
+        allocs.push_back(p);
+        bytes += b;
+        return (T *)p;
+    }
+};
+
+namespace {
+
+using cb::HostModel;
+
+template <typename T>
+void h2d(T *dst, const T *src, size_t n, cudaStream_t st)
+{
+    if (n) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+template <typename T>
+void d2h(T *dst, const T *src, size_t n, cudaStream_t st)
+{
+    if (n) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, st));
+}
+template <typename T>
+void d2d(T *dst, const T *src, size_t n, cudaStream_t st)
+{
+    if (n && dst != src) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+}
+
+// AoS (element-major, k fastest) <-> SoA (k-major) for per-element arrays
+std::vector<double> to_soa(const double *aos, long ne, int k)
+{
+    std::vector<double> s((size_t)ne * k);
+    for (long e = 0; e < ne; ++e)
+        for (int j = 0; j < k; ++j) s[(size_t)j * ne + e] = aos[(size_t)e * k + j];
+    return s;
+}
+void from_soa(const std::vector<double> &s, long ne, int k, double *aos)
+{
+    for (long e = 0; e < ne; ++e)
+        for (int j = 0; j < k; ++j) aos[(size_t)e * k + j] = s[(size_t)j * ne + e];
+}
+
+struct PhaseTimer {
+    cb_model *m;
+    double *acc;
+    PhaseTimer(cb_model *m_, double *acc_) : m(m_), acc(acc_)
+    {
+        if (m->timing) CB_CUDA(cudaEventRecord(m->ev[0], m->st));
+    }
+    ~PhaseTimer()
+    {
+        if (!m->timing) return;
+        cudaEventRecord(m->ev[1], m->st);
+        cudaEventSynchronize(m->ev[1]);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, m->ev[0], m->ev[1]);
+        *acc += ms;
+    }
+};
+
+void upload_model(cb_model *m)
+{
+    HostModel &h = m->h;
+    cudaStream_t st = m->st;
+    const long NJ = h.nj, N = h.neq, E = h.ne_sh, T = h.ne_tr;
+    m->x0 = m->alloc<double>(NJ * 3);
+    m->x_c = m->alloc<double>(NJ * 3);
+    m->x_t = m->alloc<double>(NJ * 3);
+    h2d(m->x0, h.x0.data(), NJ * 3, st);
+    d2d(m->x_c, m->x0, NJ * 3, st);
+    std::vector<int> eqx(N, -1);
+    for (long i = 0; i < NJ; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (h.jcode[i * 7 + j]) eqx[h.jcode[i * 7 + j] - 1] = (int)(i * 3 + j);
+    m->eq_x = m->alloc<int>(N);
+    h2d(m->eq_x, eqx.data(), N, st);
+    for (double **v : {&m->q, &m->d, &m->dp, &m->dpp, &m->ddq, &m->ddr, &m->dd, &m->dt, &m->r, &m->f,
+                       &m->zero, &m->ssd_o, &m->fcur, &m->fprev})
+        *v = m->alloc<double>(N);
+    h2d(m->q, h.q.data(), N, st);
+    // shells
+    if (E > 0) {
+        cb::DevShell &s = m->sh;
+        s.conn = m->alloc<int>(3 * E);
+        s.eq = m->alloc<int>(18 * E);
+        s.prop = m->alloc<double>(3 * E);
+        s.xl = m->alloc<double>(3 * E);
+        s.kem = m->alloc<double>(36 * E);
+        s.keb = m->alloc<double>(81 * E);
+        s.c_c = m->alloc<double>(9 * E);
+        s.c_ip = m->alloc<double>(9 * E);
+        s.c_i = m->alloc<double>(9 * E);
+        s.a_c = m->alloc<double>(E);
+        s.a_i = m->alloc<double>(E);
+        s.ef_c = m->alloc<double>(18 * E);
+        s.ef_ip = m->alloc<double>(18 * E);
+        s.ef_i = m->alloc<double>(18 * E);
+        std::vector<int> conn(3 * E), eq(18 * E);
+        std::vector<double> prop(3 * E);
+        for (long e = 0; e < E; ++e) {
+            for (int a = 0; a < 3; ++a) {
+                int n = h.sh_conn[e * 3 + a];
+                conn[a * E + e] = n;
+                for (int dof = 0; dof < 6; ++dof) eq[(a * 6 + dof) * E + e] = (int)h.jcode[n * 7 + dof] - 1;
+            }
+            prop[e] = h.sh_e[e];
+            prop[E + e] = h.sh_nu[e];
+            prop[2 * E + e] = h.sh_t[e];
+        }
+        h2d(s.conn, conn.data(), conn.size(), st);
+        h2d(s.eq, eq.data(), eq.size(), st);
+        h2d(s.prop, prop.data(), prop.size(), st);
+        cb::launch_shell_setup(s, m->x0, E, st);
+        CB_CUDA(cudaGetLastError());
+    }
+    if (T > 0) {
+        cb::DevTruss &t = m->tr;
+        t.conn = m->alloc<int>(2 * T);
+        t.eq = m->alloc<int>(6 * T);
+        t.ea = m->alloc<double>(T);
+        t.len0 = m->alloc<double>(T);
+        t.len_c = m->alloc<double>(T);
+        t.len_i = m->alloc<double>(T);
+        t.dir_c = m->alloc<double>(3 * T);
+        t.dir_i = m->alloc<double>(3 * T);
+        t.n_c = m->alloc<double>(T);
+        t.n_i = m->alloc<double>(T);
+        std::vector<int> conn(2 * T), eq(6 * T);
+        std::vector<double> ea(T), len0(T), dir0(3 * T);
+        for (long e = 0; e < T; ++e) {
+            int na = h.tr_conn[e * 2], nb = h.tr_conn[e * 2 + 1];
+            conn[e] = na;
+            conn[T + e] = nb;
+            for (int a = 0; a < 2; ++a)
+                for (int dof = 0; dof < 3; ++dof)
+                    eq[(a * 3 + dof) * T + e] = (int)h.jcode[h.tr_conn[e * 2 + a] * 7 + dof] - 1;
+            double el[3];
+            for (int k = 0; k < 3; ++k) el[k] = h.x0[nb * 3 + k] - h.x0[na * 3 + k];
+            double L = std::sqrt(el[0] * el[0] + el[1] * el[1] + el[2] * el[2]);
+            len0[e] = L;
+            for (int k = 0; k < 3; ++k) dir0[k * T + e] = el[k] / L;
+            ea[e] = h.tr_e[e] * h.tr_a[e];
+        }
+        h2d(t.conn, conn.data(), conn.size(), st);
+        h2d(t.eq, eq.data(), eq.size(), st);
+        h2d(t.ea, ea.data(), T, st);
+        h2d(t.len0, len0.data(), T, st);
+        d2d(t.len_c, t.len0, T, st);
+        h2d(t.dir_c, dir0.data(), 3 * T, st);
+    }
+    m->fe = m->alloc<double>(18 * E + 6 * T);
+    // gather maps
+    cb::GatherMap fm, tm;
+    cb::build_force_map(h, fm);
+    m->fmap_ptr = m->alloc<int>(fm.ptr.size());
+    m->fmap_src = m->alloc<int>(fm.src.size());
+    h2d(m->fmap_ptr, fm.ptr.data(), fm.ptr.size(), st);
+    h2d(m->fmap_src, fm.src.data(), fm.src.size(), st);
+    const bool fp32 = m->opt.precision == CB_MIXED;
+    cb::band_alloc(m->bf, N, h.bw, fp32);
+    const size_t es = fp32 ? 4 : 8;
+    m->bytes += es * ((size_t)m->bf.ld * m->bf.nblk * m->bf.s + 3 * (size_t)m->bf.nblk * m->bf.s * m->bf.s);
+    cb::build_tangent_map(h, m->bf.ld, tm);
+    m->tmap_n = (long)tm.dst.size();
+    m->tmap_ptr = m->alloc<int>(tm.ptr.size());
+    m->tmap_src = m->alloc<int>(tm.src.size());
+    m->tmap_dst = m->alloc<int64_t>(tm.dst.size());
+    h2d(m->tmap_ptr, tm.ptr.data(), tm.ptr.size(), st);
+    h2d(m->tmap_src, tm.src.data(), tm.src.size(), st);
+    h2d(m->tmap_dst, tm.dst.data(), tm.dst.size(), st);
+    if (fp32) m->kel = m->alloc<float>(171 * E + 21 * T);
+    else m->kel = m->alloc<double>(171 * E + 21 * T);
+    m->sc = m->alloc<cb::MsalScalars>(1);
+    m->partial = m->alloc<double>(16 * cb::kRedBlocks);
+    CB_CUDA(cudaMallocHost(&m->sc_h, sizeof(cb::MsalScalars)));
+    std::memset(m->sc_h, 0, sizeof(cb::MsalScalars));
+    CB_CUDA(cudaStreamSynchronize(st));
+}
+
+// ---- state transitions of main.c ----
+
+// i, ip <- converged (main.c:2582-2623, 2667-2707)
+void reset_to_converged(cb_model *m)
+{
+    const long NJ = m->h.nj, E = m->h.ne_sh, T = m->h.ne_tr;
+    cudaStream_t st = m->st;
+    d2d(m->x_t, m->x_c, NJ * 3, st);
+    if (E) {
+        d2d(m->sh.c_i, m->sh.c_c, 9 * E, st);
+        d2d(m->sh.c_ip, m->sh.c_c, 9 * E, st);
+        d2d(m->sh.a_i, m->sh.a_c, E, st);
+        d2d(m->sh.ef_i, m->sh.ef_c, 18 * E, st);
+        d2d(m->sh.ef_ip, m->sh.ef_c, 18 * E, st);
+    }
+    if (T) {
+        d2d(m->tr.len_i, m->tr.len_c, T, st);
+        d2d(m->tr.dir_i, m->tr.dir_c, 3 * T, st);
+        d2d(m->tr.n_i, m->tr.n_c, T, st);
+    }
+}
+
+// ip <- i after an iteration (main.c:2399-2428)
+void advance_iteration(cb_model *m)
+{
+    std::swap(m->sh.c_ip, m->sh.c_i);
+    std::swap(m->sh.ef_ip, m->sh.ef_i);
+}
+
+// converged <- i on acceptance (main.c:3060-3105); ip is left as it is
+void accept_state(cb_model *m)
+{
+    const long NJ = m->h.nj, E = m->h.ne_sh, T = m->h.ne_tr;
+    cudaStream_t st = m->st;
+    d2d(m->x_c, m->x_t, NJ * 3, st);
+    if (E) {
+        d2d(m->sh.c_c, m->sh.c_i, 9 * E, st);
+        d2d(m->sh.a_c, m->sh.a_i, E, st);
+        d2d(m->sh.ef_c, m->sh.ef_i, 18 * E, st);
+    }
+    if (T) {
+        d2d(m->tr.len_c, m->tr.len_i, T, st);
+        d2d(m->tr.dir_c, m->tr.dir_i, 3 * T, st);
+        d2d(m->tr.n_c, m->tr.n_i, T, st);
+    }
+}
+
+// updatc geometry + forces_tr + forces_sh + deterministic assembly into fout
+void internal_force(cb_model *m, const double *dd_vec, double *fout)
+{
+    PhaseTimer t(m, &m->tm.ms_force);
+    const long E = m->h.ne_sh, T = m->h.ne_tr;
+    if (T) cb::launch_truss_forces(m->tr, m->x_t, m->fe + 18 * E, T, m->st);
+    if (E) cb::launch_shell_forces(m->sh, m->x_t, dd_vec, m->fe, E, m->st);
+    cb::launch_gather_f64(m->fmap_ptr, m->fmap_src, m->fe, fout, m->h.neq, m->st);
+    m->tm.launches += (T ? 1 : 0) + (E ? 1 : 0) + 1;
+    m->tm.force_evals++;
+}
+
+// tangent of the converged state into the band (stiff_tr + stiff_sh)
+void assemble_tangent(cb_model *m)
+{
+    PhaseTimer t(m, &m->tm.ms_tangent);
+    const long E = m->h.ne_sh, T = m->h.ne_tr;
+    cb::BandFactor &bf = m->bf;
+    const size_t es = bf.fp32 ? 4 : 8;
+    CB_CUDA(cudaMemsetAsync(bf.band, 0, es * (size_t)bf.ld * bf.nblk * bf.s, m->st));
+    if (bf.fp32) {
+        float *k = (float *)m->kel;
+        if (E) cb::launch_shell_tangent<float>(m->sh, m->x_c, k, E, m->st);
+        if (T) cb::launch_truss_tangent<float>(m->tr, k + 171 * E, T, m->st);
+        cb::launch_gather_band<float>(m->tmap_ptr, m->tmap_src, m->tmap_dst, k, (float *)bf.band, m->tmap_n,
+                                      m->st);
+    } else {
+        double *k = (double *)m->kel;
+        if (E) cb::launch_shell_tangent<double>(m->sh, m->x_c, k, E, m->st);
+        if (T) cb::launch_truss_tangent<double>(m->tr, k + 171 * E, T, m->st);
+        cb::launch_gather_band<double>(m->tmap_ptr, m->tmap_src, m->tmap_dst, k, (double *)bf.band,
+                                       m->tmap_n, m->st);
+    }
+    m->tm.launches += 1 + (E ? 1 : 0) + (T ? 1 : 0);
+}
+
+void factor(cb_model *m)
+{
+    PhaseTimer t(m, &m->tm.ms_factor);
+    cb::band_factor(m->bf, m->st, m->opt.use_graphs != 0, &m->tm.launches);
+    m->tm.factorizations++;
+}
+
+void solve(cb_model *m, const double *rhs, double *x)
+{
+    PhaseTimer t(m, &m->tm.ms_solve);
+    cb::band_solve(m->bf, rhs, x, m->st, m->opt.use_graphs != 0, &m->tm.launches);
+    m->tm.solves++;
+}
+
+// Push the host-side scalars the device kernels read.
+void push_scalars(cb_model *m, double lam_t, double a, double intener1)
+{
+    cb::MsalScalars &s = *m->sc_h;
+    s.lam_t = lam_t;
+    s.lam_old = lam_t;
+    s.a = a;
+    s.arc = m->arc;
+    s.lamp = m->lpfp;
+    s.qq = m->qq;
+    s.psi_ge = m->psi >= m->h.psi_thresh;
+    s.toldisp = m->h.toldisp;
+    s.tolforc = m->h.tolforc;
+    s.tolener = m->h.tolener;
+    s.intener1 = intener1;
+    s.quad_status = 0;
+    s.convchk = 1;
+    s.test_err = 0;
+    h2d(m->sc, m->sc_h, 1, m->st);
+}
+
+// Read the scalar block back (one synchronisation point).
+cb::MsalScalars &pull_scalars(cb_model *m)
+{
+    d2h(m->sc_h, m->sc, 1, m->st);
+    CB_CUDA(cudaStreamSynchronize(m->st));
+    return *m->sc_h;
+}
+
+double device_dot(cb_model *m, const double *a, const double *b, bool diff = false)
+{
+    PhaseTimer t(m, &m->tm.ms_vector);
+    cb::launch_dot(a, b, m->partial, m->sc, 15, m->h.neq, m->st, diff);
+    m->tm.launches += 2;
+    double v = 0;
+    d2h(&v, &m->sc->dots[15], 1, m->st);
+    CB_CUDA(cudaStreamSynchronize(m->st));
+    return v;
+}
+
+double device_elem(cb_model *m, const double *v, long i)
+{
+    double x = 0;
+    d2h(&x, v + i, 1, m->st);
+    CB_CUDA(cudaStreamSynchronize(m->st));
+    return x;
+}
+
+double true_residual(cb_model *m, double lam, const double *fvec)
+{
+    // |lam q - f| / |lam q|
+    cb::launch_scale(m->q, lam, m->r, m->h.neq, m->st);
+    double num = device_dot(m, m->r, fvec, true);
+    double den = device_dot(m, m->r, nullptr);
+    return den > 0 ? std::sqrt(num / den) : 0.0;
+}
+
+int fail(cb_model *m, int code, const std::string &msg)
+{
+    m->err = msg;
+    return code;
+}
+
+// ---- the first increment (main.c:2296-2560) ----
+void msal_begin(cb_model *m, cb_step *out)
+{
+    HostModel &h = m->h;
+    const long N = h.neq;
+    cudaStream_t st = m->st;
+    reset_to_converged(m);
+    CB_CUDA(cudaMemsetAsync(m->d, 0, N * sizeof(double), st));
+    CB_CUDA(cudaMemsetAsync(m->dp, 0, N * sizeof(double), st));
+    CB_CUDA(cudaMemsetAsync(m->f, 0, N * sizeof(double), st));
+    m->lpfp = 0;
+    m->qq = device_dot(m, m->q, nullptr);
+    assemble_tangent(m);
+    factor(m);
+    solve(m, m->q, m->ddq);
+    d2d(m->ssd_o, m->bf.ssd, N, st);
+    double ddq_k = device_elem(m, m->ddq, h.dkdof);
+    double lpf = h.dk / ddq_k;
+    // d = dd = lpf ddq; intener1 = dd . (lpf q)
+    cb::launch_scale(m->ddq, lpf, m->dd, N, st);
+    d2d(m->d, m->dd, N, st);
+    double intener1 = lpf * device_dot(m, m->dd, m->q);
+    cb::launch_update_coords(m->eq_x, m->dd, m->x_t, N, st);
+    internal_force(m, m->dd, m->fcur);
+    int itecnt = 1;
+    advance_iteration(m);
+    int convchk = 1;
+    do {
+        push_scalars(m, lpf, 0.0, intener1);
+        {
+            PhaseTimer t(m, &m->tm.ms_vector);
+            cb::launch_residual(m->q, m->fcur, m->r, m->sc, N, st);
+        }
+        solve(m, m->r, m->ddr);
+        {
+            PhaseTimer t(m, &m->tm.ms_vector);
+            cb::launch_first_update(m->ddr, m->ddq, h.dkdof, m->d, m->dd, m->eq_x, m->x_t, m->sc, N, st);
+        }
+        std::swap(m->fcur, m->fprev);  // fprev = f_ip
+        internal_force(m, m->dd, m->fcur);
+        {
+            PhaseTimer t(m, &m->tm.ms_vector);
+            cb::launch_test(m->dd, m->d, m->zero, m->q, m->fcur, m->zero, m->fprev, m->partial, m->sc, N, st);
+        }
+        m->tm.launches += 4;
+        cb::MsalScalars &s = pull_scalars(m);
+        if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+        lpf = s.lam_t;
+        convchk = s.convchk;
+        itecnt++;
+        advance_iteration(m);
+    } while (convchk != 0 && itecnt <= h.itemax);
+    if (convchk != 0) throw cb_status_error(CB_ERR_DIVERGED, "initially prescribed displacement too large");
+    accept_state(m);
+    d2d(m->f, m->fcur, N, st);
+    m->lpf = lpf;
+    out->lam = lpf;
+    out->iterations = itecnt;
+    out->attempts = 1;
+    out->residual = true_residual(m, lpf, m->f);
+    out->dk = device_elem(m, m->d, h.dkdof);
+    out->done = 0;
+    m->dkc = std::fabs(out->dk);
+    m->lpfc = std::fabs(lpf);
+    d2d(m->dpp, m->dp, N, st);
+    d2d(m->dp, m->d, N, st);
+    m->lpfpp = m->lpfp;
+    m->lpfp = lpf;
+    reset_to_converged(m);
+    double nd = std::sqrt(device_dot(m, m->dp, nullptr));
+    m->dnorm = nd;
+    m->dnormallow = h.alpha * nd;
+    m->beta = std::sqrt((double)h.iteopt / (double)itecnt) * (m->dnormallow / m->dnorm);
+    m->psi = 1;
+    cb::launch_psi(m->bf.ssd, m->ssd_o, m->partial, m->sc, 14, N, st);
+    double ps = 0;
+    d2h(&ps, &m->sc->dots[14], 1, st);
+    CB_CUDA(cudaStreamSynchronize(st));
+    m->psi = ps;
+    m->errchk2 = m->subcnt = m->imagcnt = m->negcnt = 0;
+    m->itecnt = itecnt;
+    m->phase = 1;
+}
+
+// ---- one arc-length increment (main.c:2647-3134) ----
+void msal_step(cb_model *m, cb_step *out)
+{
+    HostModel &h = m->h;
+    const long N = h.neq;
+    cudaStream_t st = m->st;
+    out->done = 0;
+    if (!(m->lpfc <= h.lpfmax && m->dkc <= h.dkimax)) {
+        out->done = 1;
+        out->lam = m->lpf;
+        out->iterations = 0;
+        out->attempts = 0;
+        out->residual = 0;
+        out->dk = 0;
+        return;
+    }
+    int attempts = 0;
+    for (;;) {
+        ++attempts;
+        d2d(m->dt, m->d, N, st);
+        double lam_t = m->lpf;
+        if (m->errchk2 == 0) {
+            double dot = device_dot(m, m->dp, m->dpp, true);
+            m->arc = m->psi >= h.psi_thresh
+                         ? m->beta * std::sqrt(dot + (m->lpfp - m->lpfpp) * (m->lpfp - m->lpfpp))
+                         : m->beta * std::sqrt(dot);
+        } else {
+            reset_to_converged(m);
+            m->errchk2 = 0;
+        }
+        assemble_tangent(m);
+        factor(m);
+        solve(m, m->q, m->ddq);
+        int flags[2] = {0, 0};
+        d2h(flags, m->bf.flags, 2, st);
+        CB_CUDA(cudaStreamSynchronize(st));
+        if (flags[1]) throw cb_status_error(CB_ERR_NUMERIC, "singular stiffness matrix (zero pivot)");
+        const int det = flags[0];
+        double a = m->psi >= h.psi_thresh ? m->qq + device_dot(m, m->ddq, nullptr) : device_dot(m, m->ddq, nullptr);
+        double dlpf = det == 0 ? m->arc * std::sqrt(1 / a) : -m->arc * std::sqrt(1 / a);
+        lam_t += dlpf;
+        // predictor (main.c:2772-2782): dd = dlpf ddq; d_temp += dd;
+        // intener1 = dd . (dlpf q); x_temp += dd
+        cb::launch_scale(m->ddq, dlpf, m->dd, N, st);
+        double intener1 = dlpf * device_dot(m, m->dd, m->q);
+        cb::launch_axpy(m->dd, 1.0, m->dt, N, st);
+        cb::launch_update_coords(m->eq_x, m->dd, m->x_t, N, st);
+        m->tm.launches += 3;
+        internal_force(m, m->dd, m->fcur);
+        advance_iteration(m);
+        int itecnt = 1;
+        int convchk = 1;
+        push_scalars(m, lam_t, a, intener1);
+        do {
+            {
+                PhaseTimer t(m, &m->tm.ms_vector);
+                cb::launch_residual(m->q, m->fcur, m->r, m->sc, N, st);
+            }
+            solve(m, m->r, m->ddr);
+            {
+                PhaseTimer t(m, &m->tm.ms_vector);
+                cb::launch_quad_dots(m->dt, m->dp, m->ddr, m->ddq, m->partial, m->sc, N, st);
+                cb::launch_quad(m->partial, m->sc, st);
+                cb::launch_quad_update(m->ddr, m->ddq, m->dp, m->dt, m->dd, m->eq_x, m->x_t, m->sc, N, st);
+            }
+            std::swap(m->fcur, m->fprev);
+            internal_force(m, m->dd, m->fcur);
+            {
+                PhaseTimer t(m, &m->tm.ms_vector);
+                cb::launch_test(m->dd, m->dt, m->dp, m->q, m->fcur, m->f, m->fprev, m->partial, m->sc, N, st);
+            }
+            m->tm.launches += 6;
+            cb::MsalScalars &s = pull_scalars(m);
+            int status = s.quad_status;
+            if (status == 0) {
+                if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+                convchk = s.convchk;
+                if (convchk == 0) {
+                    m->dnorm = std::sqrt(s.dots[5]);
+                    if (m->dnorm > 100 * m->dnormallow) {
+                        m->arc /= m->beta;
+                        m->beta = m->dnormallow / m->dnorm;
+                        m->arc *= m->beta;
+                        m->errchk2 = 1;
+                    }
+                } else {
+                    itecnt++;
+                    if (itecnt > h.itemax) {
+                        m->arc *= 0.5;
+                        m->subcnt++;
+                        m->errchk2 = 1;
+                    }
+                    advance_iteration(m);
+                }
+            } else {
+                m->arc *= 0.5;
+                if (status == 2) m->imagcnt++;
+                else m->negcnt++;
+                m->errchk2 = status;
+                // the scalar block keeps lam_t; the increment is abandoned
+            }
+        } while (convchk != 0 && m->errchk2 == 0 && m->subcnt <= h.submax && m->imagcnt <= h.imagmax &&
+                 m->negcnt <= h.negmax);
+        if (m->subcnt > h.submax || m->imagcnt > h.imagmax || m->negcnt > h.negmax)
+            throw cb_status_error(CB_ERR_DIVERGED, "maximum allowable number of subdivisions exceeded");
+        if (m->errchk2 != 0) continue;
+        // accept (main.c:3045-3133)
+        cb::MsalScalars &s = *m->sc_h;
+        m->beta = std::sqrt((double)h.iteopt / (double)itecnt) * (m->dnormallow / m->dnorm);
+        d2d(m->dpp, m->dp, N, st);
+        d2d(m->dp, m->dt, N, st);
+        d2d(m->d, m->dt, N, st);
+        d2d(m->f, m->fcur, N, st);
+        m->lpfpp = m->lpfp;
+        m->lpf = m->lpfp = s.lam_t;
+        accept_state(m);
+        out->dk = device_elem(m, m->d, h.dkdof);
+        m->dkc = std::fabs(out->dk);
+        m->lpfc = std::fabs(m->lpf);
+        cb::launch_psi(m->bf.ssd, m->ssd_o, m->partial, m->sc, 14, N, st);
+        double ps = 0;
+        d2h(&ps, &m->sc->dots[14], 1, st);
+        CB_CUDA(cudaStreamSynchronize(st));
+        m->psi = ps;
+        m->subcnt = m->imagcnt = m->negcnt = 0;
+        m->itecnt = itecnt;
+        out->lam = m->lpf;
+        out->iterations = itecnt;
+        out->attempts = attempts;
+        out->residual = true_residual(m, m->lpf, m->f);
+        return;
+    }
+}
+
+template <typename F>
+int guarded(cb_model *m, F &&fn)
+{
+    try {
+        fn();
+        return CB_OK;
+    } catch (const cb_status_error &e) {
+        m->err = e.what();
+        return e.code;
+    } catch (const std::exception &e) {
+        m->err = e.what();
+        return CB_ERR_CUDA;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int cb_default_options(cb_options *opt)
+{
+    if (!opt) return CB_ERR_ARG;
+    std::memset(opt, 0, sizeof *opt);
+    opt->precision = CB_FP64;
+    opt->device = 0;
+    opt->use_graphs = 1;
+    return CB_OK;
+}
+
+int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb_model **out)
+{
+    if (!model_def || !out) return CB_ERR_ARG;
+    *out = nullptr;
+    cb_model *m = new cb_model();
+    if (opt) m->opt = *opt;
+    else cb_default_options(&m->opt);
+    int status = CB_OK;
+    std::string msg = cb::parse_model_def(model_def, len, m->h, status);
+    if (status != CB_OK) {
+        m->err = msg;
+        *out = m;  // the handle carries the message; caller destroys it
+        return status;
+    }
+    if (m->h.neq < 2) {
+        m->err = "fewer than two equations";
+        *out = m;
+        return CB_ERR_UNSUPPORTED;
+    }
+    int rc = guarded(m, [&] {
+        int ndev = 0;
+        CB_CUDA(cudaGetDeviceCount(&ndev));
+        if (ndev <= 0) throw cb_status_error(CB_ERR_CUDA, "no CUDA device");
+        CB_CUDA(cudaSetDevice(m->opt.device));
+        CB_CUDA(cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking));
+        CB_CUDA(cudaEventCreate(&m->ev[0]));
+        CB_CUDA(cudaEventCreate(&m->ev[1]));
+        upload_model(m);
+    });
+    *out = m;
+    return rc;
+}
+
+int cb_model_destroy(cb_model *m)
+{
+    if (!m) return CB_ERR_ARG;
+    if (m->st) cudaStreamSynchronize(m->st);
+    cb::band_free(m->bf);
+    for (void *p : m->allocs) cudaFree(p);
+    if (m->sc_h) cudaFreeHost(m->sc_h);
+    for (auto &e : m->ev)
+        if (e) cudaEventDestroy(e);
+    if (m->st) cudaStreamDestroy(m->st);
+    delete m;
+    return CB_OK;
+}
+
+int cb_model_info(const cb_model *m, cb_info *info)
+{
+    if (!m || !info) return CB_ERR_ARG;
+    info->nj = m->h.nj;
+    info->ne_tr = m->h.ne_tr;
+    info->ne_fr = m->h.ne_fr;
+    info->ne_sh = m->h.ne_sh;
+    info->neq = m->h.neq;
+    info->lss = m->h.lss;
+    info->bandwidth = m->h.bw;
+    info->block = m->bf.s;
+    info->nblocks = m->bf.nblk;
+    info->dkdof = m->h.dkdof;
+    info->device_bytes = m->bytes;
+    return CB_OK;
+}
+
+const char *cb_last_error(const cb_model *m) { return m ? m->err.c_str() : "null handle"; }
+
+int cb_msal_begin(cb_model *m, cb_step *out)
+{
+    if (!m || !out || !m->st) return CB_ERR_ARG;
+    return guarded(m, [&] { msal_begin(m, out); });
+}
+
+int cb_msal_step(cb_model *m, cb_step *out)
+{
+    if (!m || !out) return CB_ERR_ARG;
+    if (m->phase != 1) return fail(m, CB_ERR_STATE, "cb_msal_begin has not completed");
+    return guarded(m, [&] { msal_step(m, out); });
+}
+
+int cb_get_displacements(const cb_model *m, double *d, double *lam)
+{
+    if (!m || !d) return CB_ERR_ARG;
+    cb_model *mm = const_cast<cb_model *>(m);
+    return guarded(mm, [&] {
+        d2h(d, m->d, m->h.neq, m->st);
+        CB_CUDA(cudaStreamSynchronize(m->st));
+        if (lam) *lam = m->lpf;
+    });
+}
+
+int cb_get_topology(const cb_model *m, long *jcode, double *q)
+{
+    if (!m) return CB_ERR_ARG;
+    if (jcode) std::memcpy(jcode, m->h.jcode.data(), sizeof(long) * m->h.jcode.size());
+    if (q) std::memcpy(q, m->h.q.data(), sizeof(double) * m->h.q.size());
+    return CB_OK;
+}
+
+int cb_get_timers(const cb_model *m, cb_timers *t)
+{
+    if (!m || !t) return CB_ERR_ARG;
+    *t = m->tm;
+    return CB_OK;
+}
+
+int cb_reset_timers(cb_model *m)
+{
+    if (!m) return CB_ERR_ARG;
+    m->tm = cb_timers{};
+    return CB_OK;
+}
+
+int cb_set_timing(cb_model *m, int on)
+{
+    if (!m) return CB_ERR_ARG;
+    m->timing = on != 0;
+    return CB_OK;
+}
+
+int cb_eval_forces(cb_model *m, const double *x_temp, const double *dd, const double *c_ip,
+                   const double *ef_ip, double *c_i, double *area_i, double *ef_i, double *ef_tr,
+                   double *f)
+{
+    if (!m || !x_temp || !dd || !f) return CB_ERR_ARG;
+    const long E = m->h.ne_sh, T = m->h.ne_tr, N = m->h.neq;
+    if (E && (!c_ip || !ef_ip)) return CB_ERR_ARG;
+    return guarded(m, [&] {
+        cudaStream_t st = m->st;
+        h2d(m->x_t, x_temp, m->h.nj * 3, st);
+        h2d(m->dd, dd, N, st);
+        std::vector<double> cs, es;
+        if (E) {
+            cs = to_soa(c_ip, E, 9);
+            es = to_soa(ef_ip, E, 18);
+            h2d(m->sh.c_ip, cs.data(), cs.size(), st);
+            h2d(m->sh.ef_ip, es.data(), es.size(), st);
+        }
+        internal_force(m, m->dd, m->fcur);
+        d2h(f, m->fcur, N, st);
+        std::vector<double> c(9 * E), a(E), e(18 * E), n(T);
+        if (E) {
+            d2h(c.data(), m->sh.c_i, 9 * E, st);
+            d2h(a.data(), m->sh.a_i, E, st);
+            d2h(e.data(), m->sh.ef_i, 18 * E, st);
+        }
+        if (T) d2h(n.data(), m->tr.n_i, T, st);
+        CB_CUDA(cudaStreamSynchronize(st));
+        if (E) {
+            if (c_i) from_soa(c, E, 9, c_i);
+            if (area_i) std::memcpy(area_i, a.data(), sizeof(double) * E);
+            if (ef_i) from_soa(e, E, 18, ef_i);
+        }
+        if (T && ef_tr)
+            for (long k = 0; k < T; ++k) {
+                ef_tr[2 * k] = n[k];
+                ef_tr[2 * k + 1] = -n[k];
+            }
+    });
+}
+
+int cb_eval_tangent(cb_model *m, const double *x, const double *c_sh, const double *area_sh,
+                    const double *ef_tr, long *maxa, double *ss)
+{
+    if (!m || !x || !ss) return CB_ERR_ARG;
+    const long E = m->h.ne_sh, T = m->h.ne_tr, N = m->h.neq;
+    if ((E && (!c_sh || !area_sh)) || (T && !ef_tr)) return CB_ERR_ARG;
+    return guarded(m, [&] {
+        cudaStream_t st = m->st;
+        h2d(m->x_c, x, m->h.nj * 3, st);
+        std::vector<double> cs;
+        if (E) {
+            cs = to_soa(c_sh, E, 9);
+            h2d(m->sh.c_c, cs.data(), cs.size(), st);
+            h2d(m->sh.a_c, area_sh, E, st);
+        }
+        std::vector<double> len(T), dir(3 * T), nc(T);
+        for (long e = 0; e < T; ++e) {
+            int na = m->h.tr_conn[e * 2], nb = m->h.tr_conn[e * 2 + 1];
+            double el[3];
+            for (int k = 0; k < 3; ++k) el[k] = x[nb * 3 + k] - x[na * 3 + k];
+            double L = std::sqrt(el[0] * el[0] + el[1] * el[1] + el[2] * el[2]);
+            len[e] = L;
+            for (int k = 0; k < 3; ++k) dir[k * T + e] = el[k] / L;
+            nc[e] = ef_tr[2 * e];
+        }
+        if (T) {
+            h2d(m->tr.len_c, len.data(), T, st);
+            h2d(m->tr.dir_c, dir.data(), 3 * T, st);
+            h2d(m->tr.n_c, nc.data(), T, st);
+        }
+        assemble_tangent(m);
+        cb::BandFactor &bf = m->bf;
+        const long npad = bf.nblk * bf.s;
+        std::vector<double> band((size_t)bf.ld * npad);
+        if (bf.fp32) {
+            std::vector<float> bfl((size_t)bf.ld * npad);
+            d2h(bfl.data(), (const float *)bf.band, bfl.size(), st);
+            CB_CUDA(cudaStreamSynchronize(st));
+            for (size_t i = 0; i < bfl.size(); ++i) band[i] = bfl[i];
+        } else {
+            d2h(band.data(), (const double *)bf.band, band.size(), st);
+            CB_CUDA(cudaStreamSynchronize(st));
+        }
+        if (maxa) std::memcpy(maxa, m->h.maxa.data(), sizeof(long) * (N + 1));
+        for (long j = 1; j <= N; ++j) {
+            long hgt = m->h.maxa[j] - m->h.maxa[j - 1] - 1;
+            for (long off = 0; off <= hgt; ++off) {
+                long i = j - off;  // 1-based row above the diagonal of column j
+                ss[m->h.maxa[j - 1] - 1 + off] = band[(size_t)(i - 1) * bf.ld + off];
+            }
+        }
+    });
+}
+
+int cb_factor_solve(cb_model *m, const double *rhs, double *v, double *ssd, int *det)
+{
+    if (!m || !rhs || !v) return CB_ERR_ARG;
+    const long N = m->h.neq;
+    return guarded(m, [&] {
+        cudaStream_t st = m->st;
+        factor(m);
+        h2d(m->r, rhs, N, st);
+        solve(m, m->r, m->ddr);
+        d2h(v, m->ddr, N, st);
+        if (ssd) d2h(ssd, m->bf.ssd, N, st);
+        int fl[2] = {0, 0};
+        d2h(fl, m->bf.flags, 2, st);
+        CB_CUDA(cudaStreamSynchronize(st));
+        if (det) *det = fl[0];
+        if (fl[1]) throw cb_status_error(CB_ERR_NUMERIC, "zero pivot in the LDL^T factorisation");
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,225 @@
+"""cubens_gb300: GB300 (sm_103a) hot path of CU-BENs behind a C ABI.
+
+This package is the Python host mirror of the C ABI in include/cubens_gb300.h.
+It loads the in-tree CUDA library (cu-bens_gb300/lib/libcubens_gb300.so,
+built by ``cubens.build.build()``) through ctypes. There is no CPU fallback:
+if the library is missing or no GPU is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+from . import models  # noqa: F401  (re-exported generators)
+
+LIB_PATH = _build.LIB
+
+CB_OK = 0
+STATUS = {0: "ok", 1: "bad argument", 2: "parse error", 3: "CUDA error", 4: "unsupported",
+          5: "numeric failure", 6: "diverged", 7: "bad call order", 8: "timeout", 9: "limit"}
+
+FP64 = 0
+MIXED = 1
+
+
+class CubensError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("device", C.c_int), ("use_graphs", C.c_int),
+                ("reserved", C.c_int * 5)]
+
+
+class Info(C.Structure):
+    _fields_ = [("nj", C.c_long), ("ne_tr", C.c_long), ("ne_fr", C.c_long), ("ne_sh", C.c_long),
+                ("neq", C.c_long), ("lss", C.c_long), ("bandwidth", C.c_long), ("block", C.c_long),
+                ("nblocks", C.c_long), ("dkdof", C.c_long), ("device_bytes", C.c_size_t)]
+
+
+class Step(C.Structure):
+    _fields_ = [("lam", C.c_double), ("iterations", C.c_int), ("attempts", C.c_int),
+                ("residual", C.c_double), ("dk", C.c_double), ("done", C.c_int)]
+
+
+class Timers(C.Structure):
+    _fields_ = [("ms_tangent", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double),
+                ("ms_force", C.c_double), ("ms_vector", C.c_double), ("launches", C.c_long),
+                ("solves", C.c_long), ("factorizations", C.c_long), ("force_evals", C.c_long)]
+
+
+_lib = None
+
+
+def load(path: Path | None = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with cubens.build.build() (nvcc, sm_103a)")
+    L = C.CDLL(str(p))
+    dp = C.POINTER(C.c_double)
+    lp = C.POINTER(C.c_long)
+    ip = C.POINTER(C.c_int)
+    vp = C.c_void_p
+    L.cb_default_options.argtypes = [C.POINTER(Options)]
+    L.cb_model_create.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(Options), C.POINTER(vp)]
+    L.cb_model_destroy.argtypes = [vp]
+    L.cb_model_info.argtypes = [vp, C.POINTER(Info)]
+    L.cb_last_error.argtypes = [vp]
+    L.cb_last_error.restype = C.c_char_p
+    L.cb_msal_begin.argtypes = [vp, C.POINTER(Step)]
+    L.cb_msal_step.argtypes = [vp, C.POINTER(Step)]
+    L.cb_get_displacements.argtypes = [vp, dp, dp]
+    L.cb_get_topology.argtypes = [vp, lp, dp]
+    L.cb_get_timers.argtypes = [vp, C.POINTER(Timers)]
+    L.cb_reset_timers.argtypes = [vp]
+    L.cb_set_timing.argtypes = [vp, C.c_int]
+    L.cb_eval_forces.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+    L.cb_eval_tangent.argtypes = [vp, dp, dp, dp, dp, lp, dp]
+    L.cb_factor_solve.argtypes = [vp, dp, dp, dp, ip]
+    _lib = L
+    return L
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _c64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+@dataclass
+class StepResult:
+    lam: float
+    iterations: int
+    attempts: int
+    residual: float
+    dk: float
+    done: bool
+
+
+class Model:
+    """A model_def uploaded to the GPU, with its MSAL state (resident API)."""
+
+    def __init__(self, model_def: str, precision: int = FP64, device: int = 0, use_graphs: bool = True):
+        L = load()
+        opt = Options()
+        L.cb_default_options(C.byref(opt))
+        opt.precision = precision
+        opt.device = device
+        opt.use_graphs = 1 if use_graphs else 0
+        h = C.c_void_p()
+        raw = model_def.encode()
+        rc = L.cb_model_create(raw, len(raw), C.byref(opt), C.byref(h))
+        self.h = h
+        if rc != CB_OK:
+            msg = L.cb_last_error(h).decode() if h else ""
+            self.close()
+            raise CubensError(rc, msg)
+        inf = Info()
+        L.cb_model_info(self.h, C.byref(inf))
+        self.info = {k: getattr(inf, k) for k, _ in Info._fields_}
+        self.neq = inf.neq
+        self.nj, self.ne_tr, self.ne_sh = inf.nj, inf.ne_tr, inf.ne_sh
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            load().cb_model_destroy(self.h)
+        self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != CB_OK:
+            raise CubensError(rc, load().cb_last_error(self.h).decode())
+
+    def _step(self, fn) -> StepResult:
+        s = Step()
+        self._check(fn(self.h, C.byref(s)))
+        return StepResult(s.lam, s.iterations, s.attempts, s.residual, s.dk, bool(s.done))
+
+    def begin(self) -> StepResult:
+        return self._step(load().cb_msal_begin)
+
+    def step(self) -> StepResult:
+        return self._step(load().cb_msal_step)
+
+    def displacements(self):
+        d = np.zeros(self.neq)
+        lam = C.c_double()
+        self._check(load().cb_get_displacements(self.h, _d(d), C.byref(lam)))
+        return d, lam.value
+
+    def topology(self):
+        jc = np.zeros(self.nj * 7, dtype=np.int64)
+        q = np.zeros(self.neq)
+        self._check(load().cb_get_topology(self.h, jc.ctypes.data_as(C.POINTER(C.c_long)), _d(q)))
+        return jc, q
+
+    def run(self, steps: int, with_d: bool = True):
+        """First increment plus steps-1 arc-length increments (the output() records)."""
+        lam, its, res, ds = [], [], [], []
+        r = self.begin()
+        for k in range(steps):
+            if k > 0:
+                r = self.step()
+                if r.done:
+                    break
+            lam.append(r.lam)
+            its.append(r.iterations)
+            res.append(r.residual)
+            if with_d:
+                ds.append(self.displacements()[0])
+        return dict(lam=np.array(lam), its=np.array(its), res=np.array(res),
+                    d=np.array(ds) if with_d else None)
+
+    # ---- element-level entry points ----
+    def eval_forces(self, x_temp, dd, c_ip=None, ef_ip=None):
+        E, T = self.ne_sh, self.ne_tr
+        c_i, a_i, ef_i = np.zeros(9 * E), np.zeros(E), np.zeros(18 * E)
+        ef_tr, f = np.zeros(2 * T), np.zeros(self.neq)
+        args = [_c64(x_temp), _c64(dd), _c64(c_ip) if E else None, _c64(ef_ip) if E else None]
+        self._check(load().cb_eval_forces(self.h, *[_d(a) for a in args], _d(c_i), _d(a_i), _d(ef_i),
+                                          _d(ef_tr), _d(f)))
+        return c_i, a_i, ef_i, ef_tr, f
+
+    def eval_tangent(self, x, c_sh=None, area_sh=None, ef_tr=None):
+        maxa = np.zeros(self.neq + 1, dtype=np.int64)
+        ss = np.zeros(self.info["lss"])
+        args = [_c64(x), _c64(c_sh) if self.ne_sh else None, _c64(area_sh) if self.ne_sh else None,
+                _c64(ef_tr) if self.ne_tr else None]
+        self._check(load().cb_eval_tangent(self.h, *[_d(a) for a in args],
+                                           maxa.ctypes.data_as(C.POINTER(C.c_long)), _d(ss)))
+        return maxa, ss
+
+    def factor_solve(self, rhs):
+        v = np.zeros(self.neq)
+        ssd = np.zeros(self.neq)
+        det = C.c_int()
+        self._check(load().cb_factor_solve(self.h, _d(_c64(rhs)), _d(v), _d(ssd), C.byref(det)))
+        return v, ssd, det.value
+
+    def timers(self) -> dict:
+        t = Timers()
+        load().cb_get_timers(self.h, C.byref(t))
+        return {k: getattr(t, k) for k, _ in Timers._fields_}
+
+    def reset_timers(self):
+        load().cb_reset_timers(self.h)
+
+    def set_timing(self, on: bool):
+        load().cb_set_timing(self.h, 1 if on else 0)

@@ -1,0 +1,147 @@
+/* cubens_gb300 — GB300 (sm_103a) implementation of the CU-BENs nonlinear
+ * equilibrium-loop hot path, behind a plain C ABI.
+ *
+ * Two groups of entry points:
+ *
+ *  1. Resident API (cb_*): the model, its state and the factorisation live in
+ *     GPU memory; the host drives the modified spherical arc-length (MSAL)
+ *     loop of main.c:2158-3141 one converged increment at a time. This is
+ *     the fast path.
+ *
+ *  2. Drop-in API: the prototypes.h entry points of the hot path with the
+ *     reference's exact signatures (host pointers, sizes through the globals
+ *     NEQ, NJ, NE_TR, NE_FR, NE_SH, ANAFLAG, ALGFLAG that main.c defines),
+ *     declared in cubens_gb300_dropin.h. Each call copies its arrays to the
+ *     GPU and back, so main.c links against it unmodified.
+ *
+ * Every function returns a status code (CB_OK == 0); none calls exit().
+ * Handles are not thread-safe; one handle drives one CUDA stream.
+ */
+#ifndef CUBENS_GB300_H
+#define CUBENS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum cb_status {
+    CB_OK = 0,
+    CB_ERR_ARG = 1,          /* bad argument */
+    CB_ERR_PARSE = 2,        /* model_def text could not be read */
+    CB_ERR_CUDA = 3,         /* CUDA runtime error (no device, out of memory, launch failure) */
+    CB_ERR_UNSUPPORTED = 4,  /* model feature outside the GPU path (e.g. ANAFLAG 3) */
+    CB_ERR_NUMERIC = 5,      /* zero pivot, or a zero norm in the convergence test (misc.c:210-245) */
+    CB_ERR_DIVERGED = 6,     /* first increment failed or subdivisions exhausted (main.c:2535, 3040) */
+    CB_ERR_STATE = 7,        /* call out of order (e.g. cb_msal_step before cb_msal_begin) */
+    CB_ERR_TIMEOUT = 8,      /* a bounded device-side wait gave up */
+    CB_ERR_LIMIT = 9         /* a size beyond a stated maximum */
+};
+
+typedef struct cb_model cb_model;
+
+/* Precision of the tangent, its factorisation and the per-iteration solves.
+ * The internal forces, residual, arc-length algebra and state updates are
+ * FP64 in both modes. */
+enum cb_precision {
+    CB_FP64 = 0,   /* plain path: FP64 tangent and FP64 LDL^T (parity with the reference) */
+    CB_MIXED = 1   /* FP32 tangent and FP32 LDL^T; the modified-Newton loop refines in FP64 */
+};
+
+typedef struct {
+    int precision;   /* enum cb_precision */
+    int device;      /* CUDA device ordinal */
+    int use_graphs;  /* 1: replay the factor and solve launch sequences as CUDA graphs */
+    int reserved[5];
+} cb_options;
+
+typedef struct {
+    long nj, ne_tr, ne_fr, ne_sh;  /* joints and elements per type */
+    long neq;                      /* equations (codes, model.c:937-961) */
+    long lss;                      /* reference skyline length (skylin, model.c:1264-1277) */
+    long bandwidth;                /* max column height of the skyline */
+    long block;                    /* block size of the block-bidiagonal solve */
+    long nblocks;
+    long dkdof;                    /* 0-based DOF of the prescribed displacement */
+    size_t device_bytes;           /* GPU memory held by the handle */
+} cb_info;
+
+/* Result of one converged increment (what output() records, misc.c:402-417). */
+typedef struct {
+    double lam;            /* load proportionality factor */
+    int iterations;        /* itecnt at acceptance */
+    int attempts;          /* increments tried (1 + arc-length cuts) */
+    double residual;       /* |lam q - f| / |lam q| of the accepted state (FP64) */
+    double dk;             /* displacement at the control DOF */
+    int done;              /* 1: |lam| > lpfmax or |d_k| > dkimax, no increment taken (main.c:2647) */
+} cb_step;
+
+/* Per-kernel-class GPU time (ms, CUDA events on the handle's stream) and
+ * launch count since the last reset. */
+typedef struct {
+    double ms_tangent, ms_factor, ms_solve, ms_force, ms_vector;
+    long launches;
+    long solves, factorizations, force_evals;
+} cb_timers;
+
+/* ---- resident API -------------------------------------------------------- */
+
+int cb_default_options(cb_options *opt);
+
+/* Parse a model_def.txt text (ANAFLAG 2, ALGFLAG 3; truss and DKT shell
+ * elements; SLVFLAG 0; OPTFLAG 1) and upload the model. Replaces the setup
+ * part of main() (main.c:330-1648: struc, codes, skylin, prop_tr, prop_sh,
+ * load, msal). */
+int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb_model **out);
+int cb_model_destroy(cb_model *m);
+int cb_model_info(const cb_model *m, cb_info *info);
+/* Last error message of this handle (static storage owned by the handle). */
+const char *cb_last_error(const cb_model *m);
+
+/* First increment: Bathe-Dvorkin displacement control at the prescribed DOF
+ * (main.c:2296-2560). */
+int cb_msal_begin(cb_model *m, cb_step *out);
+/* One converged arc-length increment (main.c:2647-3134). */
+int cb_msal_step(cb_model *m, cb_step *out);
+/* Current converged displacements d (NEQ) and lambda. */
+int cb_get_displacements(const cb_model *m, double *d, double *lam);
+/* Reference load vector q (NEQ) and 1-based equation numbers jcode (NJ*7). */
+int cb_get_topology(const cb_model *m, long *jcode, double *q);
+
+int cb_get_timers(const cb_model *m, cb_timers *t);
+int cb_reset_timers(cb_model *m);
+/* Enable/disable per-phase CUDA-event timing (adds event records). */
+int cb_set_timing(cb_model *m, int on);
+
+/* ---- element-level resident entry points (used by the parity tests) ---- */
+
+/* Geometry update (updatc, misc.c:71-185) and internal forces of all
+ * elements (forces_tr truss.c:231-378, forces_sh shell.c:1593-2400) for an
+ * explicit state. Host arrays in the reference's layouts:
+ *   x_temp   NJ*3  coordinates after the increment dd
+ *   dd       NEQ   displacement increment
+ *   c_ip     NE_SH*9 previous-iteration shell triads (rows c1, c2, c3)
+ *   ef_ip    NE_SH*18 previous-iteration shell element forces
+ * Outputs: c_i (NE_SH*9), area_i (NE_SH), ef_i (NE_SH*18), truss ef_tr
+ * (NE_TR*2), f (NEQ). */
+int cb_eval_forces(cb_model *m, const double *x_temp, const double *dd, const double *c_ip,
+                   const double *ef_ip, double *c_i, double *area_i, double *ef_i,
+                   double *ef_tr, double *f);
+
+/* Tangent stiffness (stiff_tr truss.c:82-204, stiff_sh shell.c:110-344) at
+ * an explicit converged state, assembled on the GPU and returned in the
+ * reference's 1-based skyline layout (maxa, ss[lss]). State: x (NJ*3),
+ * c_sh (NE_SH*9), area_sh (NE_SH), ef_tr (NE_TR*2). */
+int cb_eval_tangent(cb_model *m, const double *x, const double *c_sh, const double *area_sh,
+                    const double *ef_tr, long *maxa, double *ss);
+
+/* Factor the tangent last assembled by cb_eval_tangent and solve K v = rhs
+ * (skyfact/skysolve, solve.c:539-698). Outputs v (NEQ), the LDL^T pivots ssd
+ * (NEQ) and det (1 when any pivot <= 0). */
+int cb_factor_solve(cb_model *m, const double *rhs, double *v, double *ssd, int *det);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

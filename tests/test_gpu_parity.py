@@ -1,0 +1,121 @@
+"""GPU path against the reference: element routines against golden vectors,
+whole MSAL paths against the reference's own runs, larger cases against the
+oracle. Every call goes through the C ABI (libcubens_gb300.so via ctypes).
+
+Tolerances: 1e-12 relative for element-level FP64 quantities; 1e-6 relative
+on load-displacement paths of the plain FP64 path and 1e-5 on the mixed
+(FP32 tangent) path, as the specification states.
+"""
+import numpy as np
+import pytest
+
+import cubens
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(1e-300, np.max(np.abs(b)))
+
+
+def test_shell_forces_match_reference(golden_dir):
+    z = np.load(golden_dir / "elem_shell_panel8.npz")
+    m = cubens.Model(str(z["model_def"]))
+    c_i, a_i, ef_i, _, f = m.eval_forces(z["x_after"], z["dd"], z["c_ip"], z["ef_ip"])
+    assert _rel(c_i, z["c_i"]) < 1e-13
+    assert _rel(a_i, z["area_i"]) < 1e-13
+    assert _rel(ef_i, z["ef_i"]) < 1e-12
+    assert _rel(f, z["f"]) < 1e-12
+
+
+def test_shell_tangent_factor_solve_match_reference(golden_dir):
+    z = np.load(golden_dir / "elem_shell_panel8.npz")
+    m = cubens.Model(str(z["model_def"]))
+    maxa, ss = m.eval_tangent(z["x_after"], z["c_i"], z["area_i"])
+    np.testing.assert_array_equal(maxa, z["maxa"])
+    assert _rel(ss, z["ss"]) < 1e-12
+    v, ssd, det = m.factor_solve(oracle.OracleModel(str(z["model_def"])).q)
+    assert det == int(z["det"])
+    assert _rel(ssd, z["ssd"]) < 1e-9
+    assert _rel(v, z["ldlt_solution"]) < 1e-8
+
+
+def test_truss_forces_and_tangent_match_reference(golden_dir):
+    z = np.load(golden_dir / "elem_truss_c1.npz")
+    m = cubens.Model(str(z["model_def"]))
+    _, _, _, ef_tr, f = m.eval_forces(z["x_after"], z["dd"])
+    assert _rel(ef_tr, z["ef_i"]) < 1e-12
+    assert _rel(f, z["f"]) < 1e-12
+    maxa, ss = m.eval_tangent(z["x_after"], ef_tr=z["ef_i"])
+    np.testing.assert_array_equal(maxa, z["maxa"])
+    assert _rel(ss, z["ss"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["truss_c1", "panel8", "panel16_imp"])
+def test_msal_path_matches_reference(golden_dir, name):
+    z = np.load(golden_dir / f"run_{name}.npz")
+    steps = len(z["lam"])
+    m = cubens.Model(str(z["model_def"]), precision=cubens.FP64)
+    r = m.run(steps)
+    np.testing.assert_array_equal(r["its"], z["iterations"])
+    assert _rel(r["lam"], z["lam"]) < 1e-6
+    for k in range(steps):
+        err = np.linalg.norm(r["d"][k] - z["d"][k]) / np.linalg.norm(z["d"][k])
+        assert err < 1e-6, (k, err)
+
+
+def test_msal_is_bit_reproducible(golden_dir):
+    z = np.load(golden_dir / "run_panel8.npz")
+    a = cubens.Model(str(z["model_def"])).run(6)
+    b = cubens.Model(str(z["model_def"])).run(6)
+    assert np.array_equal(a["d"], b["d"]) and np.array_equal(a["lam"], b["lam"])
+
+
+def test_msal_without_graphs_matches_graphs(golden_dir):
+    z = np.load(golden_dir / "run_panel8.npz")
+    a = cubens.Model(str(z["model_def"]), use_graphs=False).run(4)
+    b = cubens.Model(str(z["model_def"]), use_graphs=True).run(4)
+    assert np.array_equal(a["d"], b["d"])
+
+
+def _panel(n, seed=None, imp=0.0, toldisp=1e-5):
+    c = cubens.models.MsalControls(joint=n // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.2,
+                                   toldisp=toldisp, tolforc=1.0, tolener=1.0, itemax=100)
+    return cubens.models.cylindrical_panel(n, seed=seed, imperfection=imp, controls=c)
+
+
+def test_msal_panel32_matches_oracle():
+    m = _panel(32, seed=3, imp=0.05, toldisp=1e-4)
+    steps = 6
+    o = oracle.OracleModel(m.text).msal(steps)
+    assert o["rc"] == steps, o["error"]
+    g = cubens.Model(m.text).run(steps)
+    np.testing.assert_array_equal(g["its"], o["its"])
+    assert _rel(g["lam"], o["lam"]) < 1e-6
+    assert _rel(g["d"][-1], o["d"][-1]) < 1e-6
+
+
+def test_mixed_precision_path_tracks_fp64_curve():
+    """FP32 tangent and factor: the same load-displacement curve within 1e-5."""
+    m = _panel(16)
+    steps = 8
+    o = oracle.OracleModel(m.text).msal(steps)
+    g = cubens.Model(m.text, precision=cubens.MIXED).run(steps)
+    # the first increment is displacement controlled: same d_k, compare lambda
+    assert abs(g["lam"][0] - o["lam"][0]) / abs(o["lam"][0]) < 1e-5
+    # later increments: compare lambda against the oracle curve lambda(d_k)
+    k = int(np.argmax(np.abs(o["d"][0])))  # the control DOF carries the largest displacement
+    dk_o, lam_o = o["d"][:, k], o["lam"]
+    order = np.argsort(dk_o)
+    for dk, lam in zip(g["d"][:, k], g["lam"]):
+        if dk_o.min() <= dk <= dk_o.max():
+            ref = np.interp(dk, dk_o[order], lam_o[order])
+            assert abs(lam - ref) / abs(ref) < 1e-3
+    assert np.all(g["res"] < 1e-2)
+
+
+def test_status_codes_and_errors():
+    with pytest.raises(cubens.CubensError) as e:
+        cubens.Model("2\n1\n0\n1\n2\n1,0,0,0,0\n")
+    assert e.value.code in (2, 4)
