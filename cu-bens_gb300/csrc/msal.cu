@@ -285,16 +285,18 @@ void advance_iteration(cb_model *m)
     std::swap(m->sh.ef_ip, m->sh.ef_i);
 }
 
-// converged <- i on acceptance (main.c:3060-3105); ip is left as it is
-void accept_state(cb_model *m)
+// converged <- i on acceptance (main.c:3060-3105); ip is left as it is.
+// latest_in_ip: the caller already advanced (ip <- i by pointer swap), so the
+// newest triads and element forces are in the ip buffers.
+void accept_state(cb_model *m, bool latest_in_ip = false)
 {
     const long NJ = m->h.nj, E = m->h.ne_sh, T = m->h.ne_tr;
     cudaStream_t st = m->st;
     d2d(m->x_c, m->x_t, NJ * 3, st);
     if (E) {
-        d2d(m->sh.c_c, m->sh.c_i, 9 * E, st);
+        d2d(m->sh.c_c, latest_in_ip ? m->sh.c_ip : m->sh.c_i, 9 * E, st);
         d2d(m->sh.a_c, m->sh.a_i, E, st);
-        d2d(m->sh.ef_c, m->sh.ef_i, 18 * E, st);
+        d2d(m->sh.ef_c, latest_in_ip ? m->sh.ef_ip : m->sh.ef_i, 18 * E, st);
     }
     if (T) {
         d2d(m->tr.len_c, m->tr.len_i, T, st);
@@ -469,7 +471,9 @@ void msal_begin(cb_model *m, cb_step *out)
         advance_iteration(m);
     } while (convchk != 0 && itecnt <= h.itemax);
     if (convchk != 0) throw cb_status_error(CB_ERR_DIVERGED, "initially prescribed displacement too large");
-    accept_state(m);
+    // the first increment advances ip <- i after every iteration, converged or not
+    // (main.c:2399-2428 run before the loop condition), so the newest state is in ip
+    accept_state(m, true);
     d2d(m->f, m->fcur, N, st);
     m->lpf = lpf;
     out->lam = lpf;
