@@ -432,7 +432,32 @@ void solve_impl(BandFactor &f, const double *rhs, double *x, cudaStream_t st, lo
     CB_CUDA(cudaGetLastError());
 }
 
+template <typename T>
+void profile_impl(BandFactor &f, int which, cudaStream_t st)
+{
+    const long s = f.s;
+    if (which == 0) {
+        long i = f.nblk > 1 ? 1 : 0;
+        if (i == 0) return;
+        fwd_step_kernel<T><<<(unsigned)(s / 8), 256, 0, st>>>((const T *)f.pmat, s, i, (T *)f.work);
+    } else if (which == 4) {
+        long m = std::min(f.bw, f.nblk * f.s - NB);
+        if (m <= 0) return;
+        constexpr int TS = sizeof(T) == 8 ? 16 : 32;
+        unsigned nt = (unsigned)((m + TS - 1) / TS);
+        trailing_kernel<T, TS><<<dim3(nt, nt), 256, 0, st>>>((T *)f.band, f.ld, 0, m, (const T *)f.work,
+                                                              (const T *)f.dinv);
+    }
+}
+
 }  // namespace
+
+void band_profile_launch(BandFactor &f, int which, cudaStream_t st)
+{
+    if (f.fp32) profile_impl<float>(f, which, st);
+    else profile_impl<double>(f, which, st);
+    CB_CUDA(cudaGetLastError());
+}
 
 void band_alloc(BandFactor &f, long n, long bw, bool fp32)
 {

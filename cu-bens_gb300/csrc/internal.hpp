@@ -106,6 +106,9 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32);
 void band_free(BandFactor &f);
 // Factor the band in place: pivots to f.ssd, det/zero flags to f.flags.
 void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches);
+// One launch of a single band kernel for isolated timing: 0 = forward GEMV
+// step of block 1, 4 = trailing update of panel 0 (modifies the factor).
+void band_profile_launch(BandFactor &f, int which, cudaStream_t st);
 // Solve K x = rhs with the factor (rhs, x: FP64 device vectors of length n).
 void band_solve(BandFactor &f, const double *rhs, double *x, cudaStream_t st, bool use_graph,
                 long *launches);

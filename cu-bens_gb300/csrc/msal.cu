@@ -39,6 +39,7 @@ struct cb_model {
     std::string err;
     cudaStream_t st = nullptr;
     size_t bytes = 0;
+    size_t h2d_bytes = 0;
     std::vector<void *> allocs;
 
     // nodes and equations
@@ -71,6 +72,7 @@ struct cb_model {
     bool timing = false;
     cb_timers tm{};
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t marks[8] = {};
 
     template <typename T>
     T *alloc(size_t n)
@@ -141,6 +143,10 @@ void upload_model(cb_model *m)
 {
     HostModel &h = m->h;
     cudaStream_t st = m->st;
+    auto h2d = [m](auto *dst, const auto *src, size_t n, cudaStream_t s) {
+        m->h2d_bytes += n * sizeof(*src);
+        ::h2d(dst, src, n, s);
+    };
     const long NJ = h.nj, N = h.neq, E = h.ne_sh, T = h.ne_tr;
     m->x0 = m->alloc<double>(NJ * 3);
     m->x_c = m->alloc<double>(NJ * 3);
@@ -709,6 +715,8 @@ int cb_model_destroy(cb_model *m)
     if (m->sc_h) cudaFreeHost(m->sc_h);
     for (auto &e : m->ev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : m->marks)
+        if (e) cudaEventDestroy(e);
     if (m->st) cudaStreamDestroy(m->st);
     delete m;
     return CB_OK;
@@ -728,6 +736,7 @@ int cb_model_info(const cb_model *m, cb_info *info)
     info->nblocks = m->bf.nblk;
     info->dkdof = m->h.dkdof;
     info->device_bytes = m->bytes;
+    info->h2d_bytes = m->h2d_bytes;
     return CB_OK;
 }
 
@@ -784,6 +793,93 @@ int cb_set_timing(cb_model *m, int on)
     if (!m) return CB_ERR_ARG;
     m->timing = on != 0;
     return CB_OK;
+}
+
+int cb_event_mark(cb_model *m, int slot)
+{
+    if (!m || slot < 0 || slot >= 8) return CB_ERR_ARG;
+    return guarded(m, [&] {
+        if (!m->marks[slot]) CB_CUDA(cudaEventCreate(&m->marks[slot]));
+        CB_CUDA(cudaEventRecord(m->marks[slot], m->st));
+    });
+}
+
+int cb_event_elapsed(cb_model *m, int a, int b, double *ms)
+{
+    if (!m || !ms || a < 0 || a >= 8 || b < 0 || b >= 8 || !m->marks[a] || !m->marks[b]) return CB_ERR_ARG;
+    return guarded(m, [&] {
+        CB_CUDA(cudaEventSynchronize(m->marks[b]));
+        float v = 0;
+        CB_CUDA(cudaEventElapsedTime(&v, m->marks[a], m->marks[b]));
+        *ms = v;
+    });
+}
+
+int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch, double *bytes_per_launch,
+                      double *flops_per_launch)
+{
+    if (!m || reps <= 0 || !ms_per_launch) return CB_ERR_ARG;
+    return guarded(m, [&] {
+        cudaStream_t st = m->st;
+        const cb::BandFactor &bf = m->bf;
+        const double es = bf.fp32 ? 4.0 : 8.0;
+        const double s = (double)bf.s, nb = (double)bf.nblk;
+        const long E = m->h.ne_sh;
+        double bytes = 0, flops = 0;
+        auto once = [&] {
+            switch (which) {
+            case CB_K_SOLVE_STEP: cb::band_profile_launch(m->bf, 0, st); break;
+            case CB_K_SOLVE: cb::band_solve(m->bf, m->q, m->ddr, st, m->opt.use_graphs != 0, nullptr); break;
+            case CB_K_SHELL_FORCE: cb::launch_shell_forces(m->sh, m->x_t, m->dd, m->fe, E, st); break;
+            case CB_K_FACTOR: cb::band_factor(m->bf, st, m->opt.use_graphs != 0, nullptr); break;
+            case CB_K_TRAILING: cb::band_profile_launch(m->bf, 4, st); break;
+            default: throw cb_status_error(CB_ERR_ARG, "unknown kernel id");
+            }
+        };
+        switch (which) {
+        case CB_K_SOLVE_STEP:  // P_i (s*s) plus y_{i-1} and y_i
+            bytes = es * (s * s + 2 * s);
+            flops = 2 * s * s;
+            break;
+        case CB_K_SOLVE:  // Linv twice (lower halves), P and R^T once, vectors
+            bytes = es * nb * (s * s + 2 * s * s) + 8.0 * 2 * m->h.neq + es * 6 * nb * s;
+            flops = 2 * nb * (s * s + 2 * s * s);
+            break;
+        case CB_K_SHELL_FORCE:
+            // per element: reads conn 12 B, eq 72, xl 24, c_ip 72, ef_ip 144, ke_m columns 144,
+            // ke_b 648, 3 vertex coordinates 72, 18 gathered increments 144; writes c_i 72,
+            // area 8, ef_i 144, element force 144 (FP64)
+            bytes = (double)E * (12 + 72 + 24 + 72 + 144 + 144 + 648 + 72 + 144 + 72 + 8 + 144 + 144);
+            flops = (double)E * 2 * 430;
+            break;
+        case CB_K_FACTOR: {
+            double n = (double)m->h.neq, b = (double)bf.bw;
+            flops = 2 * (n * b * b / 2) + nb * 2 * (s * s * s / 6 + 2 * s * s * s / 3);
+            bytes = es * ((double)bf.ld * nb * s + 3 * nb * s * s);
+            break;
+        }
+        case CB_K_TRAILING: {
+            double mm = (double)std::min(bf.bw, bf.nblk * bf.s - 32);
+            flops = 2 * (mm * mm / 2) * 32;
+            bytes = es * (mm * mm / 2 * 2 + 2 * 32 * mm);
+            break;
+        }
+        default: throw cb_status_error(CB_ERR_ARG, "unknown kernel id");
+        }
+        once();  // warm-up (also builds a graph where one is used)
+        CB_CUDA(cudaStreamSynchronize(st));
+        if (!m->marks[6]) CB_CUDA(cudaEventCreate(&m->marks[6]));
+        if (!m->marks[7]) CB_CUDA(cudaEventCreate(&m->marks[7]));
+        CB_CUDA(cudaEventRecord(m->marks[6], st));
+        for (int k = 0; k < reps; ++k) once();
+        CB_CUDA(cudaEventRecord(m->marks[7], st));
+        CB_CUDA(cudaEventSynchronize(m->marks[7]));
+        float ms = 0;
+        CB_CUDA(cudaEventElapsedTime(&ms, m->marks[6], m->marks[7]));
+        *ms_per_launch = ms / reps;
+        if (bytes_per_launch) *bytes_per_launch = bytes;
+        if (flops_per_launch) *flops_per_launch = flops;
+    });
 }
 
 int cb_eval_forces(cb_model *m, const double *x_temp, const double *dd, const double *c_ip,

@@ -25,6 +25,8 @@ STATUS = {0: "ok", 1: "bad argument", 2: "parse error", 3: "CUDA error", 4: "uns
 FP64 = 0
 MIXED = 1
 
+K_SOLVE_STEP, K_SOLVE, K_SHELL_FORCE, K_FACTOR, K_TRAILING = range(5)
+
 
 class CubensError(RuntimeError):
     def __init__(self, code: int, msg: str):
@@ -40,7 +42,8 @@ class Options(C.Structure):
 class Info(C.Structure):
     _fields_ = [("nj", C.c_long), ("ne_tr", C.c_long), ("ne_fr", C.c_long), ("ne_sh", C.c_long),
                 ("neq", C.c_long), ("lss", C.c_long), ("bandwidth", C.c_long), ("block", C.c_long),
-                ("nblocks", C.c_long), ("dkdof", C.c_long), ("device_bytes", C.c_size_t)]
+                ("nblocks", C.c_long), ("dkdof", C.c_long), ("device_bytes", C.c_size_t),
+                ("h2d_bytes", C.c_size_t)]
 
 
 class Step(C.Structure):
@@ -83,6 +86,9 @@ def load(path: Path | None = None):
     L.cb_get_timers.argtypes = [vp, C.POINTER(Timers)]
     L.cb_reset_timers.argtypes = [vp]
     L.cb_set_timing.argtypes = [vp, C.c_int]
+    L.cb_event_mark.argtypes = [vp, C.c_int]
+    L.cb_event_elapsed.argtypes = [vp, C.c_int, C.c_int, dp]
+    L.cb_profile_kernel.argtypes = [vp, C.c_int, C.c_int, dp, dp, dp]
     L.cb_eval_forces.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
     L.cb_eval_tangent.argtypes = [vp, dp, dp, dp, dp, lp, dp]
     L.cb_factor_solve.argtypes = [vp, dp, dp, dp, ip]
@@ -212,6 +218,19 @@ class Model:
         det = C.c_int()
         self._check(load().cb_factor_solve(self.h, _d(_c64(rhs)), _d(v), _d(ssd), C.byref(det)))
         return v, ssd, det.value
+
+    def mark(self, slot: int):
+        self._check(load().cb_event_mark(self.h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        v = C.c_double()
+        self._check(load().cb_event_elapsed(self.h, a, b, C.byref(v)))
+        return v.value
+
+    def profile_kernel(self, which: int, reps: int = 20):
+        ms, by, fl = C.c_double(), C.c_double(), C.c_double()
+        self._check(load().cb_profile_kernel(self.h, which, reps, C.byref(ms), C.byref(by), C.byref(fl)))
+        return ms.value, by.value, fl.value
 
     def timers(self) -> dict:
         t = Timers()

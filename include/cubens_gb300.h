@@ -65,6 +65,7 @@ typedef struct {
     long nblocks;
     long dkdof;                    /* 0-based DOF of the prescribed displacement */
     size_t device_bytes;           /* GPU memory held by the handle */
+    size_t h2d_bytes;              /* bytes copied host -> device when the model was created */
 } cb_info;
 
 /* Result of one converged increment (what output() records, misc.c:402-417). */
@@ -113,6 +114,28 @@ int cb_get_timers(const cb_model *m, cb_timers *t);
 int cb_reset_timers(cb_model *m);
 /* Enable/disable per-phase CUDA-event timing (adds event records). */
 int cb_set_timing(cb_model *m, int on);
+
+/* ---- measurement hooks ---- */
+
+/* Record CUDA event `slot` (0..7) on the handle's stream. */
+int cb_event_mark(cb_model *m, int slot);
+/* Milliseconds between two recorded events (waits for event b). */
+int cb_event_elapsed(cb_model *m, int a, int b, double *ms);
+
+/* Kernels that cb_profile_kernel times in isolation. */
+enum cb_kernel_id {
+    CB_K_SOLVE_STEP = 0,   /* one block GEMV step of the forward solve (s x s) */
+    CB_K_SOLVE = 1,        /* one whole solve (forward + backward sweeps) */
+    CB_K_SHELL_FORCE = 2,  /* the DKT internal-force kernel over all shell elements */
+    CB_K_FACTOR = 3,       /* one whole band LDL^T + block inverses */
+    CB_K_TRAILING = 4      /* one trailing rank-32 update of the band (modifies the factor) */
+};
+/* Launch kernel `which` reps times back to back between two CUDA events and
+ * report the mean milliseconds per launch and the algorithmic bytes and
+ * flops of one launch. Timing a factor-modifying kernel leaves the handle's
+ * factorisation invalid until the next step refactors. */
+int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch,
+                      double *bytes_per_launch, double *flops_per_launch);
 
 /* ---- element-level resident entry points (used by the parity tests) ---- */
 

@@ -8,12 +8,21 @@
  * force, the root rule of quad, the three criteria of test) but is organised
  * around the 3x3 block structure of the element transformations.
  */
+#define _POSIX_C_SOURCE 199309L
 #include "cubens_oracle.h"
 
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
+
+static double now_s(void)
+{
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
 
 /* ------------------------------------------------------------------------ */
 /* Model                                                                     */
@@ -982,6 +991,12 @@ static double rel_residual(long neq, const double *q, double lpf, const double *
 int orc_msal(orc_model *m, int max_steps, double *lam, int *its, double *dout, double *res,
              char *err, int errlen)
 {
+    return orc_msal_timed(m, max_steps, lam, its, dout, res, NULL, err, errlen);
+}
+
+int orc_msal_timed(orc_model *m, int max_steps, double *lam, int *its, double *dout, double *res,
+                   double *tstamp, char *err, int errlen)
+{
     long N = m->neq;
     size_t nb = sizeof(double) * (size_t)(N + 1);
     double *d = calloc(1, nb), *dp = calloc(1, nb), *dpp = calloc(1, nb), *ddq = calloc(1, nb),
@@ -1050,8 +1065,9 @@ int orc_msal(orc_model *m, int max_steps, double *lam, int *its, double *dout, d
     if (nconv < max_steps) {
         lam[nconv] = lpf;
         its[nconv] = itecnt;
-        memcpy(dout + (size_t)nconv * N, d, sizeof(double) * (size_t)N);
+        if (dout) memcpy(dout + (size_t)nconv * N, d, sizeof(double) * (size_t)N);
         res[nconv] = rel_residual(N, q, lpf, f);
+        if (tstamp) tstamp[nconv] = now_s();
         nconv++;
     }
     double dkc = fabs(d[m->dkdof]), lpfc = fabs(lpf);
@@ -1189,8 +1205,9 @@ int orc_msal(orc_model *m, int max_steps, double *lam, int *its, double *dout, d
             subcnt = imagcnt = negcnt = 0;
             lam[nconv] = lpf;
             its[nconv] = itecnt;
-            memcpy(dout + (size_t)nconv * N, d, sizeof(double) * (size_t)N);
+            if (dout) memcpy(dout + (size_t)nconv * N, d, sizeof(double) * (size_t)N);
             res[nconv] = rel_residual(N, q, lpf, f);
+            if (tstamp) tstamp[nconv] = now_s();
             nconv++;
             /* No reset here: like the reference, the next increment's predictor
              * starts from the previous-iteration shell state (c_ip, ef_ip) that

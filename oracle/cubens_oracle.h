@@ -35,6 +35,10 @@ void orc_topology(const orc_model *m, long *jcode, double *q);
  * number of converged steps, or -(error code) with the reason in err. */
 int orc_msal(orc_model *m, int max_steps, double *lam, int *its, double *d, double *res,
              char *err, int errlen);
+/* As orc_msal, also recording the monotonic wall time (seconds) at which each
+ * converged step was accepted in tstamp[k] (may be NULL); d may be NULL. */
+int orc_msal_timed(orc_model *m, int max_steps, double *lam, int *its, double *d, double *res,
+                   double *tstamp, char *err, int errlen);
 
 /* ---- element-level entry points (state given explicitly) ---- */
 

@@ -39,6 +39,8 @@ def lib():
         L.orc_topology.argtypes = [P, lp, dp]
         L.orc_msal.restype = C.c_int
         L.orc_msal.argtypes = [P, C.c_int, dp, ip, dp, dp, C.c_char_p, C.c_int]
+        L.orc_msal_timed.restype = C.c_int
+        L.orc_msal_timed.argtypes = [P, C.c_int, dp, ip, dp, dp, dp, C.c_char_p, C.c_int]
         L.orc_shell_forces.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_truss_forces.argtypes = [P, dp, dp, dp, dp, dp]
         L.orc_tangent.argtypes = [P, dp, dp, dp, dp, dp, dp, lp, dp]
@@ -88,6 +90,20 @@ class OracleModel:
         nconv = int(np.count_nonzero(its))
         return dict(rc=n, error=err.value.decode(), lam=lam[:nconv], its=its[:nconv],
                     d=d[:nconv], res=res[:nconv])
+
+    def msal_timed(self, steps: int, keep_d: bool = False):
+        """MSAL run with the wall time of every accepted step (seconds, monotonic)."""
+        lam = np.zeros(steps)
+        its = np.zeros(steps, dtype=np.int32)
+        d = np.zeros((steps, self.neq)) if keep_d else None
+        res = np.zeros(steps)
+        ts = np.zeros(steps)
+        err = C.create_string_buffer(256)
+        n = lib().orc_msal_timed(self.h, steps, _d(lam), _i(its), _d(d) if keep_d else None, _d(res),
+                                 _d(ts), err, 256)
+        nconv = int(np.count_nonzero(its))
+        return dict(rc=n, error=err.value.decode(), lam=lam[:nconv], its=its[:nconv], res=res[:nconv],
+                    t=ts[:nconv], d=d[:nconv] if keep_d else None)
 
     def shell_initial(self):
         c = np.zeros(self.ne_sh * 9)
