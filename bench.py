@@ -242,24 +242,29 @@ def run_ours(args, world, rank, local, pg):
     p.close()
 
     # ---- end to end through the public API from host data ----
-    barrier(pg)
-    w0 = time.perf_counter()
-    e = cubens.Model(text, precision=cubens.MIXED, device=device)
-    e.begin()
-    d2h = 0
-    for _ in range(args.warmup + args.steps):
-        e.step()
-        d, lam = e.displacements()
-        d2h += d.nbytes + 8
-    e2e_s = time.perf_counter() - w0
-    h2d = e.info["h2d_bytes"]
-    e.close()
-    nsteps_e2e = 1 + args.warmup + args.steps
-    e2e_value = world * nsteps_e2e / (allmax(pg, e2e_s))
+    e2e = None
+    if not args.skip_e2e:
+        barrier(pg)
+        w0 = time.perf_counter()
+        e = cubens.Model(text, precision=cubens.MIXED, device=device)
+        e.begin()
+        d2h = 0
+        for _ in range(args.warmup + args.steps):
+            e.step()
+            d, lam = e.displacements()
+            d2h += d.nbytes + 8
+        e2e_s = time.perf_counter() - w0
+        h2d = e.info["h2d_bytes"]
+        e.close()
+        nsteps_e2e = 1 + args.warmup + args.steps
+        e2e = {"value": world * nsteps_e2e / allmax(pg, e2e_s), "unit": "steps/s",
+               "h2d_bytes_per_step": h2d / nsteps_e2e, "d2h_bytes_per_step": d2h / (nsteps_e2e - 1),
+               "includes": "model_def parse + upload, first increment, warm-up and timed steps, "
+                           "d read back after every step"}
 
     line = None
     if rank == 0:
-        cpu = cpu_baseline(text) if world == 1 else None
+        cpu = cpu_baseline(text) if world == 1 and not args.skip_cpu else None
         achieved = bytes_step / (ms_step * 1e-3) / 1e9
         line = {
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -288,10 +293,7 @@ def run_ours(args, world, rank, local, pg):
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": None,
                          "bytes_per_launch": bytes_step, "ms_per_launch": ms_step},
             "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
-            "e2e": {"value": e2e_value, "unit": "steps/s",
-                    "h2d_bytes_per_step": h2d / nsteps_e2e, "d2h_bytes_per_step": d2h / (nsteps_e2e - 1),
-                    "includes": "model_def parse + upload, first increment, warm-up and timed steps, "
-                                "d read back after every step"},
+            "e2e": e2e,
             "clocks": clk,
             "gpu_launches": launches,
         }
@@ -305,6 +307,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample (profiling runs)")
+    ap.add_argument("--skip-e2e", action="store_true", help="omit the end-to-end leg (profiling runs)")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
