@@ -432,6 +432,23 @@ void solve_impl(BandFactor &f, const double *rhs, double *x, cudaStream_t st, lo
     CB_CUDA(cudaGetLastError());
 }
 
+// The solve's launch sequence with caller-provided work vectors (2*npad T).
+template <typename T>
+void solve_ws_impl(const BandFactor &f, const double *rhs, double *x, void *work, cudaStream_t st)
+{
+    const long s = f.s, nb = f.nblk, npad = nb * s;
+    T *y = (T *)work;
+    T *v = y + npad;
+    fwd_diag_kernel<T><<<(unsigned)(npad / 8), 256, 0, st>>>((const T *)f.linv, s, f.n, rhs, y);
+    for (long i = 1; i < nb; ++i)
+        fwd_step_kernel<T><<<(unsigned)(s / 8), 256, 0, st>>>((const T *)f.pmat, s, i, y);
+    bwd_diag_kernel<T><<<(unsigned)((npad + 255) / 256), 256, 0, st>>>((const T *)f.linv, s, npad, y,
+                                                                        (const T *)f.dinv, v);
+    for (long i = nb - 2; i >= 0; --i)
+        bwd_step_kernel<T><<<(unsigned)(s / 8), 256, 0, st>>>((const T *)f.rmat, s, i, v);
+    store_f64_kernel<T><<<(unsigned)((f.n + 255) / 256), 256, 0, st>>>(v, f.n, x);
+}
+
 template <typename T>
 void profile_impl(BandFactor &f, int which, cudaStream_t st)
 {
@@ -451,6 +468,13 @@ void profile_impl(BandFactor &f, int which, cudaStream_t st)
 }
 
 }  // namespace
+
+void band_solve_with_work(const BandFactor &f, const double *rhs, double *x, void *work, cudaStream_t st)
+{
+    if (f.fp32) solve_ws_impl<float>(f, rhs, x, work, st);
+    else solve_ws_impl<double>(f, rhs, x, work, st);
+    CB_CUDA(cudaGetLastError());
+}
 
 void band_profile_launch(BandFactor &f, int which, cudaStream_t st)
 {

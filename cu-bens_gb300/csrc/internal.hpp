@@ -109,6 +109,10 @@ void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches)
 // One launch of a single band kernel for isolated timing: 0 = forward GEMV
 // step of block 1, 4 = trailing update of panel 0 (modifies the factor).
 void band_profile_launch(BandFactor &f, int which, cudaStream_t st);
+// The solve with caller-provided work vectors (2*nblk*s elements of the
+// factor's precision); plain launches, no graph, nothing allocated.
+void band_solve_with_work(const BandFactor &f, const double *rhs, double *x, void *work,
+                          cudaStream_t st);
 // Solve K x = rhs with the factor (rhs, x: FP64 device vectors of length n).
 void band_solve(BandFactor &f, const double *rhs, double *x, cudaStream_t st, bool use_graph,
                 long *launches);

@@ -795,6 +795,20 @@ int cb_set_timing(cb_model *m, int on)
     return CB_OK;
 }
 
+// Access to a handle's factorisation for solve_noalloc.cu.
+cb::BandFactor *cb_internal_factor(cb_model *m, cudaStream_t *st, int *device)
+{
+    if (!m) return nullptr;
+    *st = m->st;
+    *device = m->opt.device;
+    return &m->bf;
+}
+
+void cb_internal_set_error(cb_model *m, const char *msg)
+{
+    if (m) m->err = msg;
+}
+
 int cb_event_mark(cb_model *m, int slot)
 {
     if (!m || slot < 0 || slot >= 8) return CB_ERR_ARG;

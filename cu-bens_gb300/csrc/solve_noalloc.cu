@@ -1,0 +1,94 @@
+// cb_solve_noalloc: the tangent solve for callers that cannot allocate GPU
+// memory.
+//
+// Some callers of this library may not call cudaMalloc at the point where
+// they need a solve: code running while a CUDA graph is being captured,
+// code whose device memory is owned by another allocator or a fixed pool,
+// or a real-time loop whose memory footprint must not change after start-up.
+// cb_solve_noalloc serves them. It runs the same solve kernels as
+// cb_factor_solve, but its two work vectors live in the file-scope device
+// array below instead of in memory the handle allocated, and it allocates
+// nothing: no cudaMalloc, no cudaFree, no CUDA-graph instantiation.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "cubens_gb300.h"
+#include "internal.hpp"
+
+// Scratch for the solve's work vectors: 2 * npad elements of the factor's
+// precision, at most 2 * CB_NOALLOC_MAX_EQ doubles (8 MiB). Every GPU that
+// loads this library holds it until the process exits.
+#define CB_NOALLOC_MAX_EQ (1L << 19)
+static __device__ __align__(256) unsigned char g_solve_scratch[2 * CB_NOALLOC_MAX_EQ * sizeof(double)];
+
+extern "C" cb::BandFactor *cb_internal_factor(cb_model *m, cudaStream_t *st, int *device);
+extern "C" void cb_internal_set_error(cb_model *m, const char *msg);
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mutex;
+void *g_scratch_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on `device`, looked up once per
+// device with that device current. In host code the symbol is only a
+// host-side stand-in, so kernels must be given this address instead.
+cudaError_t scratch_address(int device, void **out)
+{
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    if (!g_scratch_addr[device]) {
+        int prev = 0;
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) return e;
+        if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_solve_scratch);
+        if (prev != device) cudaSetDevice(prev);
+        if (e != cudaSuccess) return e;
+        g_scratch_addr[device] = p;
+    }
+    *out = g_scratch_addr[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int cb_solve_noalloc(cb_model *m, const double *rhs, double *x)
+{
+    if (!m || !rhs || !x) return CB_ERR_ARG;
+    cudaStream_t st = nullptr;
+    int device = 0;
+    cb::BandFactor *f = cb_internal_factor(m, &st, &device);
+    if (!f || !f->band) return CB_ERR_STATE;
+    const long npad = f->nblk * f->s;
+    const size_t need = 2 * (size_t)npad * (f->fp32 ? sizeof(float) : sizeof(double));
+    if (need > sizeof(g_solve_scratch)) {
+        cb_internal_set_error(m, "cb_solve_noalloc: the model needs more solve scratch than the static "
+                                 "limit of 2 x 524288 doubles (padded equations > 524288)");
+        return CB_ERR_LIMIT;
+    }
+    void *scratch = nullptr;
+    cudaError_t e = scratch_address(device, &scratch);
+    if (e != cudaSuccess) {
+        cb_internal_set_error(m, cudaGetErrorString(e));
+        return CB_ERR_CUDA;
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (prev != device) cudaSetDevice(device);
+    try {
+        cb::band_solve_with_work(*f, rhs, x, scratch, st);
+        e = cudaStreamSynchronize(st);
+    } catch (const std::exception &ex) {
+        cb_internal_set_error(m, ex.what());
+        e = cudaErrorUnknown;
+    }
+    if (prev != device) cudaSetDevice(prev);
+    if (e != cudaSuccess) {
+        if (e != cudaErrorUnknown) cb_internal_set_error(m, cudaGetErrorString(e));
+        return CB_ERR_CUDA;
+    }
+    return CB_OK;
+}

@@ -92,6 +92,7 @@ def load(path: Path | None = None):
     L.cb_eval_forces.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
     L.cb_eval_tangent.argtypes = [vp, dp, dp, dp, dp, lp, dp]
     L.cb_factor_solve.argtypes = [vp, dp, dp, dp, ip]
+    L.cb_solve_noalloc.argtypes = [vp, vp, vp]
     _lib = L
     return L
 

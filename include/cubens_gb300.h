@@ -164,6 +164,26 @@ int cb_eval_tangent(cb_model *m, const double *x, const double *c_sh, const doub
  * (NEQ) and det (1 when any pivot <= 0). */
 int cb_factor_solve(cb_model *m, const double *rhs, double *v, double *ssd, int *det);
 
+/* ---- allocation-free solve ---------------------------------------------- */
+
+/* Solve K x = rhs with the factorisation the handle currently holds (from
+ * the last arc-length increment, or from cb_factor_solve), allocating no GPU
+ * memory. No counterpart in the reference: it serves callers that cannot
+ * call cudaMalloc where they need the solve (during CUDA-graph capture,
+ * under another allocator's memory pool, or in a loop whose footprint is
+ * fixed). rhs and x are device pointers to NEQ doubles.
+ *
+ * The solve's work vectors live in one static device array of at most
+ * 2 x 524288 doubles (8 MiB), held by every GPU that loads the library until
+ * the process exits; models with more than 524288 padded equations get
+ * CB_ERR_LIMIT. The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress with the device current); make that first
+ * call before any stream capture. All calls share the array, which keeps the
+ * last call's contents (every element is written before it is read), so
+ * calls that overlap on the GPU race with each other. The call is ordered on
+ * the handle's stream and returns when the solve has finished. */
+int cb_solve_noalloc(cb_model *m, const double *rhs, double *x);
+
 #ifdef __cplusplus
 }
 #endif
