@@ -78,39 +78,48 @@ struct DevTruss {
     double *n_c = nullptr, *n_i = nullptr;      // T: axial force ef[0]
 };
 
+// Counters of the bounded grid barrier of the persistent solve kernel.
+struct GridBarrier {
+    unsigned count;
+    unsigned gen;
+    int err;  // 1 when a wait gave up (CB_ERR_TIMEOUT)
+    int pad;
+};
+
 // The band LDL^T factor in precision T and its block-bidiagonal inverse form.
 struct BandFactor {
     long n = 0, bw = 0, ld = 0;  // lower band L[j*ld + (i-j)], 0 <= i-j <= bw
-    long s = 0, nblk = 0;        // block size (>= bw, multiple of 32) and block count
+    long w = 0;                  // coupling width: bw rounded up to 32
+    long s = 0, nblk = 0;        // block size (>= w, multiple of 32) and block count
     void *band = nullptr;        // ld * npad elements
     void *dinv = nullptr;        // npad: 1/d
-    void *linv = nullptr;        // nblk * s*s: inverse of the unit-lower diagonal block
-    void *pmat = nullptr;        // nblk * s*s: P_i = Linv_i L_{i,i-1}   (row-major)
-    void *rmat = nullptr;        // nblk * s*s: R_i = L_{i+1,i} Linv_i (stored transposed)
-    void *work = nullptr;        // 2 * npad solve work vectors
+    void *linv = nullptr;        // nblk * s*s: inverse of the unit-lower diagonal block (row-major)
+    void *linvt = nullptr;       // nblk * s*s: its transpose (row-major)
+    void *pmat = nullptr;        // nblk * s*w: Pn_i = Linv_i L_{i,i-1}[:, s-w:s] (row-major)
+    void *rmat = nullptr;        // nblk * s*w: Rn_i = (L_{i+1,i}[0:w,:] Linv_i)^T (row-major)
+    void *work = nullptr;        // max(3*npad, 32*bw) work elements
     double *ssd = nullptr;       // n pivots (FP64 copy)
     int *flags = nullptr;        // [0] det (any pivot <= 0), [1] zero pivot seen
+    GridBarrier *bar = nullptr;  // persistent-solve barrier
+    void *stage = nullptr;       // 32x32 factored diagonal block handed from panel to trailing kernel
     bool fp32 = false;
-    int inv_width = 32;          // columns per CTA of the block inversion
+    int solve_grid = 1;          // CTAs of the cooperative solve launch
+    size_t bytes = 0;            // device memory held
     cudaGraphExec_t factor_graph = nullptr;
     long factor_launches = 0;
-    struct SolveGraph {
-        const double *in = nullptr;  // pointers baked into the graph
-        double *out = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        long launches = 0;
-    } solve_graphs[4];
 };
 
 void band_alloc(BandFactor &f, long n, long bw, bool fp32);
 void band_free(BandFactor &f);
 // Factor the band in place: pivots to f.ssd, det/zero flags to f.flags.
 void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches);
-// One launch of a single band kernel for isolated timing: 0 = forward GEMV
-// step of block 1, 4 = trailing update of panel 0 (modifies the factor).
+// One launch of a single band kernel for isolated timing: 3 = trailing update
+// of panel 0, 4 = fused panel factor of panel 0 (both modify the factor).
 void band_profile_launch(BandFactor &f, int which, cudaStream_t st);
-// The solve with caller-provided work vectors (2*nblk*s elements of the
-// factor's precision); plain launches, no graph, nothing allocated.
+// Bytes band_solve_with_work needs: 256 for the barrier + 3*npad work elements.
+size_t band_work_bytes(const BandFactor &f);
+// The solve with caller-provided work memory (band_work_bytes(f): the grid
+// barrier counters, then 3*npad work elements); nothing allocated.
 void band_solve_with_work(const BandFactor &f, const double *rhs, double *x, void *work,
                           cudaStream_t st);
 // Solve K x = rhs with the factor (rhs, x: FP64 device vectors of length n).

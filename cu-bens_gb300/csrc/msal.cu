@@ -243,8 +243,7 @@ void upload_model(cb_model *m)
     h2d(m->fmap_src, fm.src.data(), fm.src.size(), st);
     const bool fp32 = m->opt.precision == CB_MIXED;
     cb::band_alloc(m->bf, N, h.bw, fp32);
-    const size_t es = fp32 ? 4 : 8;
-    m->bytes += es * ((size_t)m->bf.ld * m->bf.nblk * m->bf.s + 3 * (size_t)m->bf.nblk * m->bf.s * m->bf.s);
+    m->bytes += m->bf.bytes;
     cb::build_tangent_map(h, m->bf.ld, tm);
     m->tmap_n = (long)tm.dst.size();
     m->tmap_ptr = m->alloc<int>(tm.ptr.size());
@@ -386,7 +385,10 @@ void push_scalars(cb_model *m, double lam_t, double a, double intener1)
 cb::MsalScalars &pull_scalars(cb_model *m)
 {
     d2h(m->sc_h, m->sc, 1, m->st);
+    cb::GridBarrier bar{};
+    d2h(&bar, m->bf.bar, 1, m->st);
     CB_CUDA(cudaStreamSynchronize(m->st));
+    if (bar.err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier of the solve timed out");
     return *m->sc_h;
 }
 
@@ -842,22 +844,20 @@ int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch, d
         double bytes = 0, flops = 0;
         auto once = [&] {
             switch (which) {
-            case CB_K_SOLVE_STEP: cb::band_profile_launch(m->bf, 0, st); break;
-            case CB_K_SOLVE: cb::band_solve(m->bf, m->q, m->ddr, st, m->opt.use_graphs != 0, nullptr); break;
+            case CB_K_SOLVE: cb::band_solve(m->bf, m->q, m->ddr, st, false, nullptr); break;
             case CB_K_SHELL_FORCE: cb::launch_shell_forces(m->sh, m->x_t, m->dd, m->fe, E, st); break;
             case CB_K_FACTOR: cb::band_factor(m->bf, st, m->opt.use_graphs != 0, nullptr); break;
-            case CB_K_TRAILING: cb::band_profile_launch(m->bf, 4, st); break;
+            case CB_K_TRAILING: cb::band_profile_launch(m->bf, 3, st); break;
+            case CB_K_PANEL: cb::band_profile_launch(m->bf, 4, st); break;
             default: throw cb_status_error(CB_ERR_ARG, "unknown kernel id");
             }
         };
+        const double w = (double)bf.w, n = (double)m->h.neq, b = (double)bf.bw;
+        const double mm = (double)std::min(bf.bw, bf.nblk * bf.s - 32);
         switch (which) {
-        case CB_K_SOLVE_STEP:  // P_i (s*s) plus y_{i-1} and y_i
-            bytes = es * (s * s + 2 * s);
-            flops = 2 * s * s;
-            break;
-        case CB_K_SOLVE:  // Linv twice (lower halves), P and R^T once, vectors
-            bytes = es * nb * (s * s + 2 * s * s) + 8.0 * 2 * m->h.neq + es * 6 * nb * s;
-            flops = 2 * nb * (s * s + 2 * s * s);
+        case CB_K_SOLVE:  // Linv lower halves twice, Pn and Rn once, vectors
+            bytes = es * nb * (s * s + 2 * s * w) + 8.0 * 2 * n + es * 4 * nb * s;
+            flops = 2 * nb * (s * s + 2 * s * w);
             break;
         case CB_K_SHELL_FORCE:
             // per element: reads conn 12 B, eq 72, xl 24, c_ip 72, ef_ip 144, ke_m columns 144,
@@ -866,18 +866,18 @@ int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch, d
             bytes = (double)E * (12 + 72 + 24 + 72 + 144 + 144 + 648 + 72 + 144 + 72 + 8 + 144 + 144);
             flops = (double)E * 2 * 430;
             break;
-        case CB_K_FACTOR: {
-            double n = (double)m->h.neq, b = (double)bf.bw;
-            flops = 2 * (n * b * b / 2) + nb * 2 * (s * s * s / 6 + 2 * s * s * s / 3);
-            bytes = es * ((double)bf.ld * nb * s + 3 * nb * s * s);
+        case CB_K_FACTOR:
+            flops = 2 * (n * b * b / 2) + nb * 2 * (s * s * s / 6 + s * s * w);
+            bytes = es * ((double)bf.ld * nb * s * 2 + nb * s * (s + 2 * w));
             break;
-        }
-        case CB_K_TRAILING: {
-            double mm = (double)std::min(bf.bw, bf.nblk * bf.s - 32);
+        case CB_K_TRAILING:
             flops = 2 * (mm * mm / 2) * 32;
             bytes = es * (mm * mm / 2 * 2 + 2 * 32 * mm);
             break;
-        }
+        case CB_K_PANEL:
+            flops = 2 * (32.0 * 32 * 32 / 6 + mm * 32 * 32 / 2);
+            bytes = es * (32.0 * 32 + 2 * mm * 32 * 2);
+            break;
         default: throw cb_status_error(CB_ERR_ARG, "unknown kernel id");
         }
         once();  // warm-up (also builds a graph where one is used)

@@ -16,11 +16,12 @@
 #include "cubens_gb300.h"
 #include "internal.hpp"
 
-// Scratch for the solve's work vectors: 2 * npad elements of the factor's
-// precision, at most 2 * CB_NOALLOC_MAX_EQ doubles (8 MiB). Every GPU that
-// loads this library holds it until the process exits.
+// Scratch for the solve: 256 bytes of grid-barrier counters, then the three
+// work vectors (3 * npad elements of the factor's precision), at most
+// 3 * CB_NOALLOC_MAX_EQ doubles (12 MiB). Every GPU that loads this library
+// holds it until the process exits.
 #define CB_NOALLOC_MAX_EQ (1L << 19)
-static __device__ __align__(256) unsigned char g_solve_scratch[2 * CB_NOALLOC_MAX_EQ * sizeof(double)];
+static __device__ __align__(256) unsigned char g_solve_scratch[256 + 3 * CB_NOALLOC_MAX_EQ * sizeof(double)];
 
 extern "C" cb::BandFactor *cb_internal_factor(cb_model *m, cudaStream_t *st, int *device);
 extern "C" void cb_internal_set_error(cb_model *m, const char *msg);
@@ -62,11 +63,10 @@ extern "C" int cb_solve_noalloc(cb_model *m, const double *rhs, double *x)
     int device = 0;
     cb::BandFactor *f = cb_internal_factor(m, &st, &device);
     if (!f || !f->band) return CB_ERR_STATE;
-    const long npad = f->nblk * f->s;
-    const size_t need = 2 * (size_t)npad * (f->fp32 ? sizeof(float) : sizeof(double));
+    const size_t need = cb::band_work_bytes(*f);
     if (need > sizeof(g_solve_scratch)) {
         cb_internal_set_error(m, "cb_solve_noalloc: the model needs more solve scratch than the static "
-                                 "limit of 2 x 524288 doubles (padded equations > 524288)");
+                                 "limit of 3 x 524288 doubles (padded equations > 524288)");
         return CB_ERR_LIMIT;
     }
     void *scratch = nullptr;

@@ -124,11 +124,11 @@ int cb_event_elapsed(cb_model *m, int a, int b, double *ms);
 
 /* Kernels that cb_profile_kernel times in isolation. */
 enum cb_kernel_id {
-    CB_K_SOLVE_STEP = 0,   /* one block GEMV step of the forward solve (s x s) */
-    CB_K_SOLVE = 1,        /* one whole solve (forward + backward sweeps) */
-    CB_K_SHELL_FORCE = 2,  /* the DKT internal-force kernel over all shell elements */
-    CB_K_FACTOR = 3,       /* one whole band LDL^T + block inverses */
-    CB_K_TRAILING = 4      /* one trailing rank-32 update of the band (modifies the factor) */
+    CB_K_SOLVE = 0,        /* one solve: the persistent block-bidiagonal solve kernel */
+    CB_K_SHELL_FORCE = 1,  /* the DKT internal-force kernel over all shell elements */
+    CB_K_FACTOR = 2,       /* one whole band LDL^T + block inverses (graph replay) */
+    CB_K_TRAILING = 3,     /* one trailing rank-32 update of the band (modifies the factor) */
+    CB_K_PANEL = 4         /* one fused panel factor + TRSM (modifies the factor) */
 };
 /* Launch kernel `which` reps times back to back between two CUDA events and
  * report the mean milliseconds per launch and the algorithmic bytes and
@@ -173,14 +173,15 @@ int cb_factor_solve(cb_model *m, const double *rhs, double *v, double *ssd, int 
  * under another allocator's memory pool, or in a loop whose footprint is
  * fixed). rhs and x are device pointers to NEQ doubles.
  *
- * The solve's work vectors live in one static device array of at most
- * 2 x 524288 doubles (8 MiB), held by every GPU that loads the library until
- * the process exits; models with more than 524288 padded equations get
- * CB_ERR_LIMIT. The first call on a device looks up that array's device
+ * The solve's work vectors and its grid-barrier counters live in one
+ * static device array of 3 x 524288 doubles plus 256 bytes (12 MiB), held by
+ * every GPU that loads the library until the process exits; models with more
+ * than 524288 padded equations get CB_ERR_LIMIT. The first call on a device looks up that array's device
  * address (cudaGetSymbolAddress with the device current); make that first
  * call before any stream capture. All calls share the array, which keeps the
- * last call's contents (every element is written before it is read), so
- * calls that overlap on the GPU race with each other. The call is ordered on
+ * last call's contents: each call clears the barrier counters before its
+ * launch (every work element is written before it is read), and calls that
+ * overlap on the GPU race with each other. The call is ordered on
  * the handle's stream and returns when the solve has finished. */
 int cb_solve_noalloc(cb_model *m, const double *rhs, double *x);
 
