@@ -212,3 +212,154 @@ def batch_sizes(count: int = 512, seed: int = 2024,
     """Mesh sizes drawn uniformly from {16, 24, ..., 96}, seeded."""
     rng = np.random.default_rng(seed)
     return [int(v) for v in rng.choice(np.array(choices), size=count)]
+
+
+@dataclass
+class NewmarkControls:
+    """Nonlinear Newmark parameters in the order main.c:3320-3326 reads them.
+
+    numopt 0 with spectrds 1 gives alpha_m = alpha_f = 0, i.e. the average
+    acceleration rule beta = 0.25, gamma = 0.5 (main.c:3329-3343)."""
+
+    numopt: int = 0
+    spectrds: float = 1.0
+    lpfmax: float = 1.0
+    lpf: float = 1.0
+    dlpf: float = 1.0
+    dlpfmax: float = 1.0
+    dlpfmin: float = 1.0
+    itemax: int = 20
+    submax: int = 10
+    solmin: int = 3
+    toldisp: float = 1e-8
+    tolforc: float = 1.0
+    tolener: float = 1e-8
+
+    def lines(self) -> list[str]:
+        return [
+            f"{self.numopt},{self.spectrds!r}",
+            f"{self.lpfmax!r},{self.lpf!r},{self.dlpf!r},{self.dlpfmax!r},{self.dlpfmin!r}",
+            f"{self.itemax},{self.submax},{self.solmin}",
+            f"{self.toldisp!r},{self.tolforc!r},{self.tolener!r}",
+        ]
+
+
+FRAME_E = 200e9
+FRAME_NU = 0.3
+FRAME_RHO = 7850.0
+COLUMN_A, COLUMN_I = 0.02, 2e-4
+BEAM_A, BEAM_I = 0.012, 1e-4
+
+
+def band_limited_noise(nt: int, dt: float, rms: float, seed: int,
+                       band: tuple[float, float] = (0.5, 10.0)) -> np.ndarray:
+    """Seeded Gaussian white noise, band-passed in the FFT domain to ``band`` Hz
+    (bins outside the band zeroed) and scaled to the given RMS."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(nt)
+    spec = np.fft.rfft(w)
+    freq = np.fft.rfftfreq(nt, dt)
+    spec[(freq < band[0]) | (freq > band[1])] = 0.0
+    s = np.fft.irfft(spec, nt)
+    r = math.sqrt(float(np.mean(s * s)))
+    return s * (rms / r) if r > 0 else s
+
+
+def frame_building(bays_x: int = 20, bays_y: int = 20, storeys: int = 30,
+                   bay: float = 6.0, storey: float = 3.5, warping: str = "fixed",
+                   steps: int = 2000, dt: float = 0.005, rms: float = 5e3, seed: int = 4,
+                   loaded_face: bool = True, newmark: NewmarkControls | None = None,
+                   msal: MsalControls | None = None, msal_load: float = 1e3) -> ModelSpec:
+    """Rigid-jointed 3D frame building of co-rotational 14-DOF frame members.
+
+    Joint (i, j, s) at (bay*i, bay*j, storey*s) is number
+    s*(bx+1)*(by+1) + j*(bx+1) + i + 1. Columns join (i, j, s) to (i, j, s+1)
+    and come first; then each floor s >= 1 has beams along x, then along y.
+    The base joints (s = 0) are fixed. ``warping`` "fixed" writes "j,7,0" for
+    every joint (6 DOF per joint); "member" writes "j,7,1" (one warping DOF per
+    member end, model.c:941-961). Columns: A = 0.02, I = 2e-4; beams: A =
+    0.012, I = 1e-4 (both bending axes); J = 2I, no warping constant; steel
+    E = 200 GPa, nu = 0.3, rho = 7850. Aux points lie one unit along global x
+    from a column's first joint and one unit up from a beam's first joint.
+
+    Dynamic (default, ALGFLAG 5): every floor s >= 1 gets its own seeded
+    band-limited (0.5-10 Hz) noise history scaled to ``rms`` N, applied in
+    global x at each joint of the floor's x = 0 face (one history per floor,
+    ``steps`` + 1 time points of ``dt``). With ``msal`` given the model is an
+    MSAL model instead: ``msal_load`` in x at every joint of the roof's x = 0
+    face is the reference load.
+    """
+    bx, by, ns = bays_x, bays_y, storeys
+    nper = (bx + 1) * (by + 1)
+
+    def jid(i: int, j: int, s: int) -> int:
+        return s * nper + j * (bx + 1) + i + 1
+
+    nodes = [(bay * i, bay * j, storey * s) for s in range(ns + 1) for j in range(by + 1)
+             for i in range(bx + 1)]
+    cols, beams = [], []
+    for s in range(ns):
+        for j in range(by + 1):
+            for i in range(bx + 1):
+                cols.append((jid(i, j, s), jid(i, j, s + 1)))
+    for s in range(1, ns + 1):
+        for j in range(by + 1):
+            for i in range(bx):
+                beams.append((jid(i, j, s), jid(i + 1, j, s)))
+        for j in range(by):
+            for i in range(bx + 1):
+                beams.append((jid(i, j, s), jid(i, j + 1, s)))
+    members = cols + beams
+    gmod = FRAME_E / (2 * (1 + FRAME_NU))
+    wflag = {"fixed": 0, "member": 1}[warping]
+    cons = []
+    for k in range(1, len(nodes) + 1):
+        if k <= nper:
+            cons += [f"{k},{d}" for d in range(1, 7)]
+        cons.append(f"{k},7,{wflag}")
+    props, aux = [], []
+    for n, (a, b) in enumerate(members):
+        col = n < len(cols)
+        A, I = (COLUMN_A, COLUMN_I) if col else (BEAM_A, BEAM_I)
+        props.append(f"{_fmt(FRAME_E)},{_fmt(gmod)},{_fmt(FRAME_RHO)},{_fmt(A)},{_fmt(I)},{_fmt(I)},"
+                     f"{_fmt(2 * I)},0.0")
+        x0 = nodes[a - 1]
+        off = (1.0, 0.0, 0.0) if col else (0.0, 0.0, 1.0)
+        aux.append(",".join(_fmt(x0[k] + off[k]) for k in range(3)))
+    face = lambda s: [jid(0, j, s) for j in range(by + 1)]  # noqa: E731
+    dynamic = msal is None
+    out = ["2", "5" if dynamic else "3"]
+    if dynamic:
+        out.append("0,0")                     # CHKPT, RFLAG
+    out += ["0", "1", str(len(nodes)), f"0,{len(members)},0,0,0"]
+    out += [f"{a},{b}" for a, b in members]
+    out += cons + ["0,0"]
+    if dynamic:
+        out.append("0,0")                     # no prescribed support motion
+    out += [f"{_fmt(x)},{_fmt(y)},{_fmt(z)}" for x, y, z in nodes]
+    out += props
+    out.append("0,0,0,0,0,0,0")               # no member end offsets
+    out += aux
+    out += ["1e30,1.0,1.0"] * len(members)    # yield stress, plastic moduli (unused, ANAFLAG 2)
+    out.append("0,0,0,0,0")                   # no member end releases
+    params: dict = {"bays_x": bx, "bays_y": by, "storeys": ns, "columns": len(cols),
+                    "beams": len(beams), "warping": warping}
+    if dynamic:
+        nt = steps + 1
+        ttot = steps * dt
+        out.append(f"{steps},{_fmt(ttot)}")
+        for s in range(1, ns + 1):
+            hist = band_limited_noise(nt, dt, rms, seed * 1000 + s)
+            joints = face(s) if loaded_face else [jid(0, 0, s)]
+            for jt in joints:
+                out += [f"{jt},1,{_fmt(v)}" for v in hist]
+        out += ["0,0,0", "0,0,0", "0,0,0,0,0"]
+        out += (newmark or NewmarkControls()).lines()
+        params.update(steps=steps, dt=dt, rms=rms)
+    else:
+        out += [f"{jt},1,{_fmt(msal_load)}" for jt in face(ns)] + ["0,0,0"]
+        out.append("0,0,0")                   # no distributed loads
+        out += msal.lines()
+    name = f"frame{bx}x{by}x{ns}" + ("" if dynamic else "_msal")
+    return ModelSpec(name, "\n".join(out) + "\n", nj=len(nodes), ne_fr=len(members),
+                     seed=seed if dynamic else None, params=params)

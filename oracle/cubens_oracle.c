@@ -46,10 +46,24 @@ struct orc_model {
     double *sh_c0;   /* NE_SH*9 initial triads (rows c1, c2, c3) */
     double *sh_kem;  /* NE_SH*36 membrane stiffness (stiffe_m_sh) */
     double *sh_keb;  /* NE_SH*81 plate bending stiffness (stiffe_b_sh) */
+    /* frame (14 DOF: 7 per end incl. warping) */
+    long *fr_conn;   /* NE_FR*2 (0-based joints) */
+    double *fr_e, *fr_g, *fr_dens, *fr_a, *fr_iz, *fr_iy, *fr_ip, *fr_iw; /* iz strong, iy weak */
+    double *fr_aux;  /* NE_FR*3 auxiliary points */
+    double *fr_len0; /* NE_FR initial lengths */
+    double *fr_c0;   /* NE_FR*9 initial triads */
+    long *fr_mc;     /* NE_FR*14 1-based equation numbers (0 = fixed), warping numbered per member */
+    int alg;         /* ALGFLAG: 3 (MSAL) or 5 (nonlinear Newmark) */
     /* MSAL controls (main.c:2240-2245, arc.c:48) */
     long dkdof;      /* 0-based */
     double dk, alpha, psi_thresh, lpfmax, dkimax, toldisp, tolforc, tolener;
     int iteopt, itemax, submax, imagmax, negmax;
+    /* nonlinear Newmark input (main.c:3320-3326, model.c:1492-1609) */
+    long ntin;       /* input time points (ntsteps + 1) */
+    long nsteps;     /* NTSTPS = (long)(ttot/dt + 1) */
+    double dt, ttot, numopt, spectrds, lpf0, dlpf0, dlpfmax, dlpfmin;
+    int solmin;
+    double *pinpt;   /* NEQ*ntin per-step joint forces */
 };
 
 /* ---- token reader: the model_def layout is positional numbers ---- */
@@ -290,7 +304,47 @@ void orc_free(orc_model *m)
     free(m->sh_c0);
     free(m->sh_kem);
     free(m->sh_keb);
+    free(m->fr_conn);
+    free(m->fr_e);
+    free(m->fr_g);
+    free(m->fr_dens);
+    free(m->fr_a);
+    free(m->fr_iz);
+    free(m->fr_iy);
+    free(m->fr_ip);
+    free(m->fr_iw);
+    free(m->fr_aux);
+    free(m->fr_len0);
+    free(m->fr_c0);
+    free(m->fr_mc);
+    free(m->pinpt);
     free(m);
+}
+
+/* Frame triad from prop_fr (frame.c:130-160) / updatc (misc.c:110-147):
+ * x^ along the member, z^ = x^ x (aux - end 1) normalised, y^ = z^ x x^. */
+static void frame_geometry(const double *pa, const double *pb, const double *aux, double *c, double *len)
+{
+    double el[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+    double L = sqrt(dot3(el, el));
+    double lx[3] = {el[0] / L, el[1] / L, el[2] / L};
+    double tmp[3] = {aux[0] - pa[0], aux[1] - pa[1], aux[2] - pa[2]};
+    double lz[3], ly[3];
+    cross3(lx, tmp, lz, 1);
+    cross3(lz, lx, ly, 1);
+    for (int m = 0; m < 3; ++m) {
+        c[m] = lx[m];
+        c[3 + m] = ly[m];
+        c[6 + m] = lz[m];
+    }
+    *len = L;
+}
+
+static orc_model *load_fail(orc_model *m, char *err, int errlen, const char *msg)
+{
+    set_err(err, errlen, msg);
+    orc_free(m);
+    return NULL;
 }
 
 orc_model *orc_load(const char *text, char *err, int errlen)
@@ -299,90 +353,125 @@ orc_model *orc_load(const char *text, char *err, int errlen)
     orc_model *m = calloc(1, sizeof *m);
     int ana = (int)tok_num(&t);
     int alg = (int)tok_num(&t);
-    if (ana != 2 || alg != 3) {
-        set_err(err, errlen, "oracle supports ANAFLAG 2 with ALGFLAG 3 (MSAL)");
-        orc_free(m);
-        return NULL;
+    if (ana != 2 || (alg != 3 && alg != 5))
+        return load_fail(m, err, errlen, "oracle supports ANAFLAG 2 with ALGFLAG 3 (MSAL) or 5 (Newmark)");
+    m->alg = alg;
+    if (alg > 3) {
+        int chkpt = (int)tok_num(&t), rflag = (int)tok_num(&t);
+        (void)chkpt;
+        if (rflag != 0) return load_fail(m, err, errlen, "restart input (RFLAG 1) is not supported");
     }
     int slv = (int)tok_num(&t);
     int opt = (int)tok_num(&t);
-    if (slv != 0 || opt != 1) {
-        set_err(err, errlen, "oracle supports SLVFLAG 0 and OPTFLAG 1");
-        orc_free(m);
-        return NULL;
-    }
+    if (slv != 0 || opt != 1) return load_fail(m, err, errlen, "oracle supports SLVFLAG 0 and OPTFLAG 1");
     m->nj = (long)tok_num(&t);
     m->ne_tr = (long)tok_num(&t);
     m->ne_fr = (long)tok_num(&t);
     m->ne_sh = (long)tok_num(&t);
     long nsbr = (long)tok_num(&t), nfbr = (long)tok_num(&t);
-    if (m->ne_fr || nsbr || nfbr || !t.ok) {
-        set_err(err, errlen, "oracle supports truss and shell elements only");
-        orc_free(m);
-        return NULL;
-    }
+    if (nsbr || nfbr || !t.ok) return load_fail(m, err, errlen, "brick elements are not supported");
+    if (alg == 5 && (m->ne_tr || m->ne_sh))
+        return load_fail(m, err, errlen, "the Newmark oracle supports frame-only models");
     long NJ = m->nj;
     m->tr_conn = calloc((size_t)(2 * m->ne_tr + 1), sizeof(long));
+    m->fr_conn = calloc((size_t)(2 * m->ne_fr + 1), sizeof(long));
     m->sh_conn = calloc((size_t)(3 * m->ne_sh + 1), sizeof(long));
-    /* joint-element connectivity flags (model.c:95-133) */
+    /* joint-element connectivity (model.c:95-133) and frames per joint */
     int *has_tr = calloc((size_t)NJ, sizeof(int)), *has_sh = calloc((size_t)NJ, sizeof(int));
-    for (long i = 0; i < m->ne_tr; ++i)
-        for (int k = 0; k < 2; ++k) {
-            m->tr_conn[i * 2 + k] = (long)tok_num(&t) - 1;
-            has_tr[m->tr_conn[i * 2 + k]] = 1;
-        }
-    for (long i = 0; i < m->ne_sh; ++i)
-        for (int k = 0; k < 3; ++k) {
-            m->sh_conn[i * 3 + k] = (long)tok_num(&t) - 1;
-            has_sh[m->sh_conn[i * 3 + k]] = 1;
-        }
-    /* constraints (model.c:216-264): free = -1, fixed = 0 */
+    int *nfr = calloc((size_t)NJ, sizeof(int)), *wrp = calloc((size_t)NJ, sizeof(int));
+    for (long i = 0; i < 2 * m->ne_tr; ++i) {
+        m->tr_conn[i] = (long)tok_num(&t) - 1;
+        has_tr[m->tr_conn[i]] = 1;
+    }
+    for (long i = 0; i < 2 * m->ne_fr; ++i) {
+        m->fr_conn[i] = (long)tok_num(&t) - 1;
+        nfr[m->fr_conn[i]]++;
+    }
+    for (long i = 0; i < 3 * m->ne_sh; ++i) {
+        m->sh_conn[i] = (long)tok_num(&t) - 1;
+        has_sh[m->sh_conn[i]] = 1;
+    }
+    /* constraints (model.c:216-264): free = -1, fixed = 0; "j,7,r" sets the
+     * warping restraint flag r (1 = one warping DOF per member) */
     m->jcode = malloc(sizeof(long) * (size_t)NJ * 7);
     for (long i = 0; i < NJ * 7; ++i) m->jcode[i] = -1;
     for (;;) {
         long j = (long)tok_num(&t), k = (long)tok_num(&t);
-        if (!t.ok) break;
-        if (j == 0) break;
+        if (!t.ok || j == 0) break;
         if (k < 1 || k > 7 || j > NJ) {
-            set_err(err, errlen, "bad constraint line");
             free(has_tr);
             free(has_sh);
-            orc_free(m);
-            return NULL;
+            free(nfr);
+            free(wrp);
+            return load_fail(m, err, errlen, "bad constraint line");
         }
-        if (k == 7) (void)tok_num(&t);
+        if (k == 7) wrp[j - 1] = (int)tok_num(&t);
         m->jcode[(j - 1) * 7 + k - 1] = 0;
     }
     /* DOFs that no element type uses (model.c:267-285) */
     for (long i = 0; i < NJ; ++i) {
-        if (!has_sh[i]) {
-            if (!has_tr[i]) {
-                for (int j = 0; j < 7; ++j) m->jcode[i * 7 + j] = 0;
+        if (nfr[i] == 0) {
+            if (!has_sh[i]) {
+                int from = has_tr[i] ? 3 : 0;
+                for (int j = from; j < 7; ++j) m->jcode[i * 7 + j] = 0;
             } else {
-                for (int j = 3; j < 7; ++j) m->jcode[i * 7 + j] = 0;
+                m->jcode[i * 7 + 6] = 0;
             }
-        } else {
-            m->jcode[i * 7 + 6] = 0;
         }
     }
+    /* equation numbers (codes, model.c:941-961) */
+    long neq = 0;
+    for (long i = 0; i < NJ; ++i) {
+        for (int j = 0; j < 6; ++j)
+            if (m->jcode[i * 7 + j] != 0) m->jcode[i * 7 + j] = ++neq;
+        if (m->jcode[i * 7 + 6] != 0) {
+            m->jcode[i * 7 + 6] = ++neq;
+        } else if (wrp[i] == 1) {
+            m->jcode[i * 7 + 6] = ++neq;
+            neq += nfr[i] - 1;
+        }
+    }
+    m->neq = neq;
+    /* frame member codes: the warping DOF of a joint with one warping DOF
+     * per member counts up over the members in element order (model.c:1007-1032) */
+    m->fr_mc = calloc((size_t)(14 * m->ne_fr + 1), sizeof(long));
+    int *cnt = calloc((size_t)NJ, sizeof(int));
+    for (long i = 0; i < NJ; ++i) cnt[i] = nfr[i];
+    for (long e = 0; e < m->ne_fr; ++e)
+        for (int a = 0; a < 2; ++a) {
+            long j = m->fr_conn[e * 2 + a];
+            for (int d = 0; d < 6; ++d) m->fr_mc[e * 14 + a * 7 + d] = m->jcode[j * 7 + d];
+            if (wrp[j] == 1) {
+                m->fr_mc[e * 14 + a * 7 + 6] = m->jcode[j * 7 + 6] + nfr[j] - cnt[j];
+                cnt[j]--;
+            } else {
+                m->fr_mc[e * 14 + a * 7 + 6] = m->jcode[j * 7 + 6];
+            }
+        }
+    free(cnt);
     free(has_tr);
     free(has_sh);
-    /* equation numbers (codes, model.c:941-961; no frames so no warping DOF) */
-    long neq = 0;
-    for (long i = 0; i < NJ; ++i)
-        for (int j = 0; j < 7; ++j)
-            if (m->jcode[i * 7 + j] != 0) m->jcode[i * 7 + j] = ++neq;
-    m->neq = neq;
-    /* skyline profile (skylin, model.c:1204-1277) */
+    free(nfr);
+    free(wrp);
+    /* prescribed motion list of dynamic analyses (skylin, model.c:1156-1201) */
+    if (alg > 3) {
+        long j = (long)tok_num(&t), k = (long)tok_num(&t);
+        (void)k;
+        if (j != 0) return load_fail(m, err, errlen, "prescribed support motion (NBC > 0) is not supported");
+    }
+    /* skyline profile (skylin, model.c:1204-1277): trusses, frames, shells */
     long *kht = calloc((size_t)neq + 1, sizeof(long));
-    for (long e = 0; e < m->ne_tr + m->ne_sh; ++e) {
+    for (long e = 0; e < m->ne_tr + m->ne_fr + m->ne_sh; ++e) {
         long mc[18];
         int nd = 0;
         if (e < m->ne_tr) {
             for (int a = 0; a < 2; ++a)
                 for (int d = 0; d < 3; ++d) mc[nd++] = m->jcode[m->tr_conn[e * 2 + a] * 7 + d];
+        } else if (e < m->ne_tr + m->ne_fr) {
+            long f = e - m->ne_tr;
+            for (int k = 0; k < 14; ++k) mc[nd++] = m->fr_mc[f * 14 + k];
         } else {
-            long s = e - m->ne_tr;
+            long s = e - m->ne_tr - m->ne_fr;
             for (int a = 0; a < 3; ++a)
                 for (int d = 0; d < 6; ++d) mc[nd++] = m->jcode[m->sh_conn[s * 3 + a] * 7 + d];
         }
@@ -415,6 +504,28 @@ orc_model *orc_load(const char *text, char *err, int errlen)
         (void)tok_num(&t); /* density */
         (void)tok_num(&t); /* yield */
     }
+    /* frame properties (prop_fr, frame.c:43-224) */
+    long F = m->ne_fr;
+    double **fp[] = {&m->fr_e, &m->fr_g, &m->fr_dens, &m->fr_a, &m->fr_iz, &m->fr_iy, &m->fr_ip, &m->fr_iw};
+    for (int k = 0; k < 8; ++k) *fp[k] = calloc((size_t)F + 1, sizeof(double));
+    m->fr_aux = calloc((size_t)F * 3 + 1, sizeof(double));
+    m->fr_len0 = calloc((size_t)F + 1, sizeof(double));
+    m->fr_c0 = calloc((size_t)F * 9 + 1, sizeof(double));
+    if (F > 0) {
+        for (long i = 0; i < F; ++i)
+            for (int k = 0; k < 8; ++k) (*fp[k])[i] = tok_num(&t);
+        long j = (long)tok_num(&t);
+        for (int k = 0; k < 6; ++k) (void)tok_num(&t);
+        if (j != 0) return load_fail(m, err, errlen, "frame member end offsets are not supported");
+        for (long i = 0; i < F * 3; ++i) m->fr_aux[i] = tok_num(&t);
+        for (long i = 0; i < F * 3; ++i) (void)tok_num(&t); /* yield, plastic moduli */
+        j = (long)tok_num(&t);
+        for (int k = 0; k < 4; ++k) (void)tok_num(&t);
+        if (j != 0) return load_fail(m, err, errlen, "frame member end releases are not supported");
+        for (long i = 0; i < F; ++i)
+            frame_geometry(m->x0 + m->fr_conn[i * 2] * 3, m->x0 + m->fr_conn[i * 2 + 1] * 3,
+                           m->fr_aux + i * 3, m->fr_c0 + i * 9, m->fr_len0 + i);
+    }
     /* shell properties and geometry (prop_sh, shell.c:43-108) */
     long E = m->ne_sh;
     m->sh_e = calloc((size_t)E + 1, sizeof(double));
@@ -441,42 +552,92 @@ orc_model *orc_load(const char *text, char *err, int errlen)
         shell_keb(m->sh_e[i], m->sh_nu[i], m->sh_t[i], m->sh_area0[i], m->sh_xl + i * 3,
                   m->sh_slen0 + i * 3, m->sh_keb + i * 81);
     }
-    /* joint loads (load, model.c:1313-1335) */
     m->q = calloc((size_t)neq + 1, sizeof(double));
-    for (;;) {
+    if (alg == 3) {
+        /* joint loads (load, model.c:1313-1335), then frame distributed loads */
+        for (;;) {
+            long jt = (long)tok_num(&t);
+            long dir = (long)tok_num(&t);
+            double mag = tok_num(&t);
+            if (!t.ok || jt == 0) break;
+            long k = m->jcode[(jt - 1) * 7 + dir - 1];
+            if (k != 0) m->q[k - 1] = mag;
+        }
+        if (F > 0) {
+            long fr = (long)tok_num(&t);
+            (void)tok_num(&t);
+            (void)tok_num(&t);
+            if (fr != 0) return load_fail(m, err, errlen, "frame distributed loads are not supported");
+        }
+        /* MSAL controls (msal, arc.c:41-68; main.c:2240-2245) */
         long jt = (long)tok_num(&t);
         long dir = (long)tok_num(&t);
-        double mag = tok_num(&t);
-        if (!t.ok || jt == 0) break;
-        long k = m->jcode[(jt - 1) * 7 + dir - 1];
-        if (k != 0) m->q[k - 1] = mag;
-    }
-    /* MSAL controls (msal, arc.c:41-68; main.c:2240-2245) */
-    long jt = (long)tok_num(&t);
-    long dir = (long)tok_num(&t);
-    m->dk = tok_num(&t);
-    m->alpha = tok_num(&t);
-    m->psi_thresh = tok_num(&t);
-    m->iteopt = (int)tok_num(&t);
-    m->lpfmax = tok_num(&t);
-    m->dkimax = tok_num(&t);
-    m->itemax = (int)tok_num(&t);
-    m->submax = (int)tok_num(&t);
-    m->imagmax = (int)tok_num(&t);
-    m->negmax = (int)tok_num(&t);
-    m->toldisp = tok_num(&t);
-    m->tolforc = tok_num(&t);
-    m->tolener = tok_num(&t);
-    if (!t.ok) {
-        set_err(err, errlen, "model_def ended early");
-        orc_free(m);
-        return NULL;
-    }
-    m->dkdof = m->jcode[(jt - 1) * 7 + dir - 1] - 1;
-    if (m->dkdof < 0) {
-        set_err(err, errlen, "initially prescribed displacement at a fixed DOF");
-        orc_free(m);
-        return NULL;
+        m->dk = tok_num(&t);
+        m->alpha = tok_num(&t);
+        m->psi_thresh = tok_num(&t);
+        m->iteopt = (int)tok_num(&t);
+        m->lpfmax = tok_num(&t);
+        m->dkimax = tok_num(&t);
+        m->itemax = (int)tok_num(&t);
+        m->submax = (int)tok_num(&t);
+        m->imagmax = (int)tok_num(&t);
+        m->negmax = (int)tok_num(&t);
+        m->toldisp = tok_num(&t);
+        m->tolforc = tok_num(&t);
+        m->tolener = tok_num(&t);
+        if (!t.ok) return load_fail(m, err, errlen, "model_def ended early");
+        m->dkdof = m->jcode[(jt - 1) * 7 + dir - 1] - 1;
+        if (m->dkdof < 0) return load_fail(m, err, errlen, "initially prescribed displacement at a fixed DOF");
+    } else {
+        /* time points (main.c:1600-1607) */
+        long ntsteps = (long)tok_num(&t);
+        m->ttot = tok_num(&t);
+        m->dt = m->ttot / (double)ntsteps;
+        m->ntin = ntsteps + 1;
+        m->nsteps = (long)(m->ttot / m->dt + 1);
+        /* per-step joint forces (load, model.c:1516-1549): lines of one DOF
+         * are consecutive time points; a zero force is stored as 1e-30 */
+        m->pinpt = calloc((size_t)(neq * m->ntin + 1), sizeof(double));
+        long kps = 0, i = 0;
+        for (;;) {
+            long jt = (long)tok_num(&t);
+            long dir = (long)tok_num(&t);
+            double mag = tok_num(&t);
+            if (!t.ok || jt == 0) break;
+            if (mag == 0) mag = 1e-30;
+            long ks = m->jcode[(jt - 1) * 7 + dir - 1];
+            if (ks != kps) i = 0;
+            if (ks != 0 && i < m->ntin) m->pinpt[(ks - 1) * m->ntin + i] = mag;
+            kps = ks;
+            ++i;
+        }
+        /* prescribed support displacements (none supported) and initial conditions */
+        long jt = (long)tok_num(&t);
+        (void)tok_num(&t);
+        (void)tok_num(&t);
+        if (jt != 0) return load_fail(m, err, errlen, "prescribed displacements are not supported");
+        for (;;) {
+            jt = (long)tok_num(&t);
+            for (int k = 0; k < 4; ++k) (void)tok_num(&t);
+            if (!t.ok || jt == 0) break;
+        }
+        /* Newmark controls (main.c:3320-3326) */
+        m->numopt = tok_num(&t);
+        m->spectrds = tok_num(&t);
+        m->lpfmax = tok_num(&t);
+        m->lpf0 = tok_num(&t);
+        m->dlpf0 = tok_num(&t);
+        m->dlpfmax = tok_num(&t);
+        m->dlpfmin = tok_num(&t);
+        m->itemax = (int)tok_num(&t);
+        m->submax = (int)tok_num(&t);
+        m->solmin = (int)tok_num(&t);
+        m->toldisp = tok_num(&t);
+        m->tolforc = tok_num(&t);
+        m->tolener = tok_num(&t);
+        if (!t.ok) return load_fail(m, err, errlen, "model_def ended early");
+        if (m->numopt == 0 && m->spectrds != 1)
+            return load_fail(m, err, errlen, "invalid spectral radius for Newmark without dissipation");
     }
     return m;
 }
@@ -491,6 +652,12 @@ void orc_sizes(const orc_model *m, long *out)
     out[5] = m->lss;
     out[6] = m->dkdof;
     out[7] = m->itemax;
+}
+
+void orc_dyn_sizes(const orc_model *m, long *nsteps, double *dt)
+{
+    *nsteps = m->nsteps;
+    *dt = m->dt;
 }
 
 void orc_topology(const orc_model *m, long *jcode, double *q)
@@ -623,6 +790,221 @@ void orc_truss_forces(const orc_model *m, const double *x_temp, double *length_i
 }
 
 /* ------------------------------------------------------------------------ */
+/* Frame element (14 DOF)                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Local 14x14 stiffness of the frame: elastic part (stiffe_fr,
+ * frame.c:364-408) with reference length L0, plus the geometric part
+ * (stiffg_fr, frame.c:410-579) from the previous total end forces ef and
+ * deformed length L. DOFs per end: u, v, w, thx, thy, thz, warping. */
+#define KSYM(i, j, v)                 \
+    do {                              \
+        double v_ = (v);              \
+        k[i][j] += v_;                \
+        if ((i) != (j)) k[j][i] += v_; \
+    } while (0)
+
+static void frame_klocal(const orc_model *m, long e, double L0, const double *ef, double L,
+                         double k[14][14])
+{
+    const double E = m->fr_e[e], G = m->fr_g[e], A = m->fr_a[e], Iz = m->fr_iz[e], Iy = m->fr_iy[e],
+                 J = m->fr_ip[e], Iw = m->fr_iw[e];
+    memset(k, 0, sizeof(double) * 196);
+    k[0][0] = k[7][7] = E * A / L0;
+    k[7][0] = k[0][7] = -k[0][0];
+    k[1][1] = k[8][8] = 12 * E * Iz / pow(L0, 3);
+    k[8][1] = k[1][8] = -k[1][1];
+    k[2][2] = k[9][9] = 12 * E * Iy / pow(L0, 3);
+    k[9][2] = k[2][9] = -k[2][2];
+    k[3][3] = k[10][10] = 6 * G * J / (5 * L0) + 12 * E * Iw / pow(L0, 3);
+    k[10][3] = k[3][10] = -k[3][3];
+    k[5][5] = k[12][12] = 4 * E * Iz / L0;
+    k[4][4] = k[11][11] = 4 * E * Iy / L0;
+    k[6][6] = k[13][13] = 2 * G * J * L0 / 15 + 4 * E * Iw / L0;
+    k[5][1] = k[1][5] = k[12][1] = k[1][12] = 6 * E * Iz / pow(L0, 2);
+    k[8][5] = k[5][8] = k[12][8] = k[8][12] = -k[5][1];
+    k[9][4] = k[4][9] = k[11][9] = k[9][11] = 6 * E * Iy / pow(L0, 2);
+    k[4][2] = k[2][4] = k[11][2] = k[2][11] = -k[9][4];
+    k[6][3] = k[3][6] = k[13][3] = k[3][13] = G * J / 10 + 6 * E * Iw / pow(L0, 2);
+    k[10][6] = k[6][10] = k[13][10] = k[10][13] = -k[6][3];
+    k[12][5] = k[5][12] = 2 * E * Iz / L0;
+    k[11][4] = k[4][11] = 2 * E * Iy / L0;
+    k[13][6] = k[6][13] = -(G * J * L0 / 30 - 2 * E * Iw / L0);
+    /* geometric stiffness of the axial force P = ef[7] and the end moments */
+    const double P = ef[7], e4 = ef[4], e5 = ef[5], e10 = ef[10], e11 = ef[11], e12 = ef[12];
+    k[0][0] += P / L;
+    k[7][7] += P / L;
+    KSYM(7, 0, -(P / L));
+    k[1][1] += 6 * P / (5 * L);
+    k[8][8] += 6 * P / (5 * L);
+    k[2][2] += 6 * P / (5 * L);
+    k[9][9] += 6 * P / (5 * L);
+    KSYM(8, 1, -(6 * P / (5 * L)));
+    KSYM(9, 2, -(6 * P / (5 * L)));
+    k[3][3] += 6 * P * J / (5 * A * L);
+    k[10][10] += 6 * P * J / (5 * A * L);
+    KSYM(10, 3, -(6 * P * J / (5 * A * L)));
+    k[4][4] += 2 * P * L / 15;
+    k[11][11] += 2 * P * L / 15;
+    k[5][5] += 2 * P * L / 15;
+    k[12][12] += 2 * P * L / 15;
+    k[6][6] += 2 * P * J / (15 * A);
+    k[13][13] += 2 * P * J / (15 * A);
+    KSYM(3, 1, (11 * e4 - e11) / (10 * L));
+    KSYM(8, 3, -((11 * e4 - e11) / (10 * L)));
+    KSYM(4, 1, e10 / L);
+    KSYM(5, 2, e10 / L);
+    KSYM(11, 8, e10 / L);
+    KSYM(12, 9, e10 / L);
+    KSYM(11, 1, -(e10 / L));
+    KSYM(12, 2, -(e10 / L));
+    KSYM(8, 4, -(e10 / L));
+    KSYM(9, 5, -(e10 / L));
+    KSYM(5, 1, P / 10);
+    KSYM(12, 1, P / 10);
+    KSYM(9, 4, P / 10);
+    KSYM(11, 9, P / 10);
+    KSYM(4, 2, -(P / 10));
+    KSYM(11, 2, -(P / 10));
+    KSYM(8, 5, -(P / 10));
+    KSYM(12, 8, -(P / 10));
+    KSYM(6, 1, e4 / 10);
+    KSYM(8, 6, -(e4 / 10));
+    KSYM(10, 8, (e4 - 11 * e11) / (10 * L));
+    KSYM(10, 1, -((e4 - 11 * e11) / (10 * L)));
+    KSYM(13, 8, e11 / 10);
+    KSYM(13, 1, -(e11 / 10));
+    KSYM(3, 2, (11 * e5 - e12) / (10 * L));
+    KSYM(9, 3, -((11 * e5 - e12) / (10 * L)));
+    KSYM(6, 2, e5 / 10);
+    KSYM(9, 6, -(e5 / 10));
+    KSYM(10, 9, (e5 - 11 * e12) / (10 * L));
+    KSYM(10, 2, -((e5 - 11 * e12) / (10 * L)));
+    KSYM(13, 9, e12 / 10);
+    KSYM(13, 2, -(e12 / 10));
+    KSYM(4, 3, -((2 * e5 - e12) / 5));
+    KSYM(5, 3, (2 * e4 - e11) / 5);
+    KSYM(6, 3, P * J / (10 * A));
+    KSYM(13, 3, P * J / (10 * A));
+    KSYM(10, 6, -(P * J / (10 * A)));
+    KSYM(13, 10, -(P * J / (10 * A)));
+    KSYM(11, 3, -((2 * e5 + e12) / 10));
+    KSYM(12, 3, (2 * e4 + e11) / 10);
+    KSYM(6, 4, -((3 * e5 - e12) * L / 30));
+    KSYM(10, 4, -((e5 + 2 * e12) / 10));
+    KSYM(11, 4, -(P * L / 30));
+    KSYM(12, 5, -(P * L / 30));
+    KSYM(12, 4, e10 / 2);
+    KSYM(11, 5, -(e10 / 2));
+    KSYM(13, 4, e5 * L / 30);
+    KSYM(6, 5, (3 * e4 - e11) * L / 30);
+    KSYM(10, 5, (e4 + 2 * e11) / 10);
+    KSYM(13, 5, -(e4 * L / 30));
+    KSYM(11, 6, -(e12 * L / 30));
+    KSYM(12, 6, e11 * L / 30);
+    KSYM(13, 6, -(P * J / (30 * A)));
+    KSYM(11, 10, (e5 - 2 * e12) / 5);
+    KSYM(12, 10, -((e4 - 2 * e11) / 5));
+    KSYM(13, 11, -((e5 - 3 * e12) * L / 30));
+    KSYM(13, 12, (e4 - 3 * e11) * L / 30);
+}
+#undef KSYM
+
+/* 14x14 frame transformation T: the triad on the four 3x3 translation and
+ * rotation blocks, 1 on the two warping DOFs (frame.c:284-296). */
+static void frame_T(const double *c, double T[14][14])
+{
+    memset(T, 0, sizeof(double) * 196);
+    static const int base[4] = {0, 3, 7, 10};
+    for (int b = 0; b < 4; ++b)
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) T[base[b] + r][base[b] + q] = c[r * 3 + q];
+    T[6][6] = T[13][13] = 1;
+}
+
+/* One frame of forces_fr, ANAFLAG 2, no offsets (frame.c:902-1312) with the
+ * frame part of updatc (misc.c:108-147). */
+static void frame_force_element(const orc_model *m, long e, const double *x_temp, const double *dd,
+                                const double *cip, const double *efip, double len_ip, double lref,
+                                double *ci, double *len_i, double *efi, double *fe)
+{
+    const long *cn = m->fr_conn + e * 2;
+    frame_geometry(x_temp + cn[0] * 3, x_temp + cn[1] * 3, m->fr_aux + e * 3, ci, len_i);
+    double k[14][14], Tip[14][14], Ti[14][14];
+    frame_klocal(m, e, lref, efip, len_ip, k);
+    frame_T(cip, Tip);
+    frame_T(ci, Ti);
+    double DD[14], dl[14], def[14];
+    for (int i = 0; i < 14; ++i) {
+        long q = m->fr_mc[e * 14 + i];
+        DD[i] = q ? dd[q - 1] : 0.0;
+    }
+    for (int i = 0; i < 14; ++i) {
+        double sum = 0;
+        for (int j = 0; j < 14; ++j) sum += Tip[i][j] * DD[j];
+        dl[i] = sum;
+    }
+    for (int i = 0; i < 14; ++i) {
+        double sum = 0;
+        for (int j = 0; j < 14; ++j) sum += k[i][j] * dl[j];
+        def[i] = sum;
+    }
+    double TT[14][14];
+    for (int i = 0; i < 14; ++i)
+        for (int j = 0; j < 14; ++j) {
+            double sum = 0;
+            for (int q = 0; q < 14; ++q) sum += Ti[i][q] * Tip[j][q];
+            TT[i][j] = sum;
+        }
+    for (int i = 0; i < 14; ++i) {
+        double sum = 0;
+        for (int j = 0; j < 14; ++j) sum += TT[i][j] * (efip[j] + def[j]);
+        efi[i] = sum;
+    }
+    for (int i = 0; i < 14; ++i) {
+        double sum = 0;
+        for (int j = 0; j < 14; ++j) sum += Ti[j][i] * efi[j];
+        fe[i] = sum;
+    }
+}
+
+/* Frame tangent K = T^T k T (stiff_fr, frame.c:226-362, transform misc.c:41-69). */
+static void frame_tangent_element(const orc_model *m, long e, const double *c, const double *ef,
+                                  double len, double lref, double K[14][14])
+{
+    double k[14][14], T[14][14], tmp[14][14];
+    frame_klocal(m, e, lref, ef, len, k);
+    frame_T(c, T);
+    for (int i = 0; i < 14; ++i)
+        for (int j = 0; j < 14; ++j) {
+            double sum = 0;
+            for (int q = 0; q < 14; ++q) sum += T[q][i] * k[q][j];
+            tmp[i][j] = sum;
+        }
+    for (int i = 0; i < 14; ++i)
+        for (int j = 0; j < 14; ++j) {
+            double sum = 0;
+            for (int q = 0; q < 14; ++q) sum += tmp[i][q] * T[q][j];
+            K[i][j] = sum;
+        }
+}
+
+/* Lumped frame mass (mass_fr, frame.c:1314-1391): rho A L / 24 * 12 on the
+ * translations, rho A L / 24 * L^2 on the rotations, nothing on warping,
+ * with L the member length at the coordinates x; also returns L. */
+static double frame_mass_element(const orc_model *m, long e, const double *x, double *mt, double *mr)
+{
+    const long *cn = m->fr_conn + e * 2;
+    double el[3];
+    for (int k = 0; k < 3; ++k) el[k] = x[cn[1] * 3 + k] - x[cn[0] * 3 + k];
+    double L = sqrt(dot3(el, el));
+    double rAL = m->fr_dens[e] * m->fr_a[e] * L;
+    *mt = rAL / 24 * 12;
+    *mr = rAL / 24 * pow(L, 2);
+    return L;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Tangent stiffness                                                         */
 /* ------------------------------------------------------------------------ */
 
@@ -692,11 +1074,13 @@ static void shell_local_tangent(const orc_model *m, long s, const double *x, con
         }
 }
 
-void orc_tangent(const orc_model *m, const double *x, const double *c_sh, const double *area_sh,
-                 const double *len_tr, const double *dir_tr, const double *ef_tr, long *maxa,
-                 double *ss)
+/* Tangent of the whole model in the skyline: stiff_tr, stiff_fr, stiff_sh in
+ * that order (main.c:2716-2734). Frame state may be NULL when NE_FR == 0. */
+static void tangent_all(const orc_model *m, const double *x, const double *c_sh, const double *area_sh,
+                        const double *len_tr, const double *dir_tr, const double *ef_tr,
+                        const double *c_fr, const double *ef_fr, const double *len_fr,
+                        const double *lref_fr, double *ss)
 {
-    memcpy(maxa, m->maxa, sizeof(long) * (size_t)(m->neq + 1));
     memset(ss, 0, sizeof(double) * (size_t)m->lss);
     /* truss: EA L^2/L0^3 axial plus N/L geometric term (truss.c:100-166) */
     for (long e = 0; e < m->ne_tr; ++e) {
@@ -705,14 +1089,10 @@ void orc_tangent(const orc_model *m, const double *x, const double *c_sh, const 
         double K[36];
         for (int i = 0; i < 6; ++i)
             for (int j = 0; j < 6; ++j) {
-                int si = i < 3 ? 1 : -1, sj = j < 3 ? 1 : -1;
                 /* T^T k T with T = [[c,0],[0,c]] and k = kax [[1,-1],[-1,1]] */
                 double tk = (i < 3 ? c[i] * kax : c[i - 3] * -kax);
                 double tk2 = (i < 3 ? c[i] * -kax : c[i - 3] * kax);
-                double v = j < 3 ? tk * c[j] : tk2 * c[j - 3];
-                (void)si;
-                (void)sj;
-                K[i * 6 + j] = v;
+                K[i * 6 + j] = j < 3 ? tk * c[j] : tk2 * c[j - 3];
             }
         double g = ef_tr[e * 2] / len_tr[e];
         for (int i = 0; i < 6; ++i) K[i * 6 + i] += g;
@@ -724,6 +1104,11 @@ void orc_tangent(const orc_model *m, const double *x, const double *c_sh, const 
         for (int a = 0; a < 2; ++a)
             for (int d = 0; d < 3; ++d) mc[a * 3 + d] = m->jcode[m->tr_conn[e * 2 + a] * 7 + d];
         sky_add(m, ss, mc, 6, K);
+    }
+    for (long e = 0; e < m->ne_fr; ++e) {
+        double K[14][14];
+        frame_tangent_element(m, e, c_fr + e * 9, ef_fr + e * 14, len_fr[e], lref_fr[e], K);
+        sky_add(m, ss, m->fr_mc + e * 14, 14, &K[0][0]);
     }
     /* shell: T^T k T with T = diag(R, ..., R) (misc.c:41-69) */
     for (long s = 0; s < m->ne_sh; ++s) {
@@ -748,6 +1133,64 @@ void orc_tangent(const orc_model *m, const double *x, const double *c_sh, const 
     }
 }
 
+void orc_tangent(const orc_model *m, const double *x, const double *c_sh, const double *area_sh,
+                 const double *len_tr, const double *dir_tr, const double *ef_tr, long *maxa,
+                 double *ss)
+{
+    memcpy(maxa, m->maxa, sizeof(long) * (size_t)(m->neq + 1));
+    double *ef0 = calloc((size_t)(14 * m->ne_fr + 1), sizeof(double));
+    tangent_all(m, x, c_sh, area_sh, len_tr, dir_tr, ef_tr, m->fr_c0, ef0, m->fr_len0, m->fr_len0, ss);
+    free(ef0);
+}
+
+void orc_tangent_fr(const orc_model *m, const double *c_fr, const double *ef_fr, const double *len_fr,
+                    const double *lref_fr, long *maxa, double *ss)
+{
+    memcpy(maxa, m->maxa, sizeof(long) * (size_t)(m->neq + 1));
+    tangent_all(m, m->x0, NULL, NULL, NULL, NULL, NULL, c_fr, ef_fr, len_fr, lref_fr, ss);
+}
+
+void orc_frame_forces(const orc_model *m, const double *x_temp, const double *dd, const double *c_ip,
+                      const double *ef_ip, const double *len_ip, const double *lref, double *c_i,
+                      double *len_i, double *ef_i, double *f)
+{
+    memset(f, 0, sizeof(double) * (size_t)m->neq);
+    for (long e = 0; e < m->ne_fr; ++e) {
+        double fe[14];
+        frame_force_element(m, e, x_temp, dd, c_ip + e * 9, ef_ip + e * 14, len_ip[e], lref[e], c_i + e * 9,
+                            len_i + e, ef_i + e * 14, fe);
+        for (int i = 0; i < 14; ++i) {
+            long q = m->fr_mc[e * 14 + i];
+            if (q) f[q - 1] += fe[i];
+        }
+    }
+}
+
+void orc_frame_mcode(const orc_model *m, long *mc)
+{
+    memcpy(mc, m->fr_mc, sizeof(long) * 14 * (size_t)m->ne_fr);
+}
+
+void orc_frame_initial(const orc_model *m, double *c, double *len)
+{
+    memcpy(c, m->fr_c0, sizeof(double) * 9 * (size_t)m->ne_fr);
+    memcpy(len, m->fr_len0, sizeof(double) * (size_t)m->ne_fr);
+}
+
+void orc_frame_mass(const orc_model *m, const double *x, double *sm)
+{
+    memset(sm, 0, sizeof(double) * (size_t)m->neq);
+    for (long e = 0; e < m->ne_fr; ++e) {
+        double mt, mr;
+        frame_mass_element(m, e, x, &mt, &mr);
+        for (int i = 0; i < 14; ++i) {
+            long q = m->fr_mc[e * 14 + i];
+            int d = i % 7;
+            if (q && d < 6) sm[q - 1] += d < 3 ? mt : mr;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Skyline LDL^T (Bathe's active-column COLSOL; solve.c:539-698)             */
 /* ------------------------------------------------------------------------ */
@@ -755,7 +1198,9 @@ void orc_tangent(const orc_model *m, const double *x, const double *c_sh, const 
 /* a(i, n) for the upper triangle, i <= n, 1-based; only valid inside column n */
 #define SKY(ss, maxa, i, n) ((ss)[(maxa)[(n)-1] + ((n) - (i)) - 1])
 
-static int sky_factor(long neq, const long *maxa, double *ss, double *ssd, int *det)
+/* stop_nonpos: the ALGFLAG != 3 behaviour, returning at the first pivot <= 0
+ * and leaving the later columns unfactored (solve.c:558-561, 608-611). */
+static int sky_factor(long neq, const long *maxa, double *ss, double *ssd, int *det, int stop_nonpos)
 {
     *det = 0;
     for (long n = 1; n <= neq; ++n) {
@@ -781,6 +1226,10 @@ static int sky_factor(long neq, const long *maxa, double *ss, double *ssd, int *
         }
         SKY(ss, maxa, n, n) -= b;
         double piv = SKY(ss, maxa, n, n);
+        if (stop_nonpos) {
+            if (!(piv > 0)) return 1;
+            continue;
+        }
         ssd[n - 1] = piv;
         if (piv == 0) return 1;
         if (!(piv > 0)) *det = 1;
@@ -806,7 +1255,7 @@ static void sky_solve(long neq, const long *maxa, const double *ss, double *v)
 void orc_skyline_solve(const orc_model *m, double *ss, double *rhs, double *ssd, int *det,
                        int fact)
 {
-    if (fact == 0) sky_factor(m->neq, m->maxa, ss, ssd, det);
+    if (fact == 0) sky_factor(m->neq, m->maxa, ss, ssd, det, 0);
     else *det = 0;
     sky_solve(m->neq, m->maxa, ss, rhs);
 }
@@ -878,6 +1327,8 @@ typedef struct {
     double *sh_c_c, *sh_c_ip, *sh_c_i, *sh_a_c, *sh_a_ip, *sh_a_i;
     double *sh_ef_c, *sh_ef_ip, *sh_ef_i;
     double *tr_l_c, *tr_l_i, *tr_d_c, *tr_d_i, *tr_ef_c, *tr_ef_i;
+    double *fr_c_c, *fr_c_ip, *fr_c_i, *fr_ef_c, *fr_ef_ip, *fr_ef_i, *fr_l_c, *fr_l_ip, *fr_l_i;
+    double *fr_lref;  /* reference (undeformed) length used by the frame stiffness */
     double *x, *x_temp;
 } state_t;
 
@@ -899,6 +1350,17 @@ static void state_alloc(const orc_model *m, state_t *s)
     s->tr_d_i = malloc(sizeof(double) * 3 * T);
     s->tr_ef_c = calloc(2 * T, sizeof(double));
     s->tr_ef_i = calloc(2 * T, sizeof(double));
+    size_t F = (size_t)m->ne_fr + 1;
+    s->fr_c_c = malloc(sizeof(double) * 9 * F);
+    s->fr_c_ip = malloc(sizeof(double) * 9 * F);
+    s->fr_c_i = malloc(sizeof(double) * 9 * F);
+    s->fr_ef_c = calloc(14 * F, sizeof(double));
+    s->fr_ef_ip = calloc(14 * F, sizeof(double));
+    s->fr_ef_i = calloc(14 * F, sizeof(double));
+    s->fr_l_c = malloc(sizeof(double) * F);
+    s->fr_l_ip = malloc(sizeof(double) * F);
+    s->fr_l_i = malloc(sizeof(double) * F);
+    s->fr_lref = malloc(sizeof(double) * F);
     s->x = malloc(sizeof(double) * 3 * (size_t)m->nj);
     s->x_temp = malloc(sizeof(double) * 3 * (size_t)m->nj);
 }
@@ -907,7 +1369,9 @@ static void state_free(state_t *s)
 {
     double **p[] = {&s->sh_c_c, &s->sh_c_ip, &s->sh_c_i, &s->sh_a_c, &s->sh_a_ip, &s->sh_a_i,
                     &s->sh_ef_c, &s->sh_ef_ip, &s->sh_ef_i, &s->tr_l_c, &s->tr_l_i, &s->tr_d_c,
-                    &s->tr_d_i, &s->tr_ef_c, &s->tr_ef_i, &s->x, &s->x_temp};
+                    &s->tr_d_i, &s->tr_ef_c, &s->tr_ef_i, &s->x, &s->x_temp, &s->fr_c_c, &s->fr_c_ip,
+                    &s->fr_c_i, &s->fr_ef_c, &s->fr_ef_ip, &s->fr_ef_i, &s->fr_l_c, &s->fr_l_ip,
+                    &s->fr_l_i, &s->fr_lref};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; ++i) {
         free(*p[i]);
         *p[i] = NULL;
@@ -929,6 +1393,15 @@ static void internal_force(const orc_model *m, state_t *s, const double *dd, dou
 {
     memset(f, 0, sizeof(double) * (size_t)m->neq);
     if (m->ne_tr) orc_truss_forces(m, s->x_temp, s->tr_l_i, s->tr_d_i, s->tr_ef_i, f);
+    for (long e = 0; e < m->ne_fr; ++e) {
+        double fe[14];
+        frame_force_element(m, e, s->x_temp, dd, s->fr_c_ip + e * 9, s->fr_ef_ip + e * 14, s->fr_l_ip[e],
+                            s->fr_lref[e], s->fr_c_i + e * 9, s->fr_l_i + e, s->fr_ef_i + e * 14, fe);
+        for (int i = 0; i < 14; ++i) {
+            long q = m->fr_mc[e * 14 + i];
+            if (q) f[q - 1] += fe[i];
+        }
+    }
     for (long e = 0; e < m->ne_sh; ++e) {
         double fe[18];
         long mc[18];
@@ -946,6 +1419,9 @@ static void advance_iteration(const orc_model *m, state_t *s)
     memcpy(s->sh_ef_ip, s->sh_ef_i, sizeof(double) * 18 * (size_t)m->ne_sh);
     memcpy(s->sh_c_ip, s->sh_c_i, sizeof(double) * 9 * (size_t)m->ne_sh);
     memcpy(s->sh_a_ip, s->sh_a_i, sizeof(double) * (size_t)m->ne_sh);
+    memcpy(s->fr_ef_ip, s->fr_ef_i, sizeof(double) * 14 * (size_t)m->ne_fr);
+    memcpy(s->fr_c_ip, s->fr_c_i, sizeof(double) * 9 * (size_t)m->ne_fr);
+    memcpy(s->fr_l_ip, s->fr_l_i, sizeof(double) * (size_t)m->ne_fr);
 }
 
 /* "i, ip <- converged" at the start of an increment (main.c:2582-2623) */
@@ -962,6 +1438,13 @@ static void reset_to_converged(const orc_model *m, state_t *s)
     memcpy(s->tr_ef_i, s->tr_ef_c, sizeof(double) * 2 * T);
     memcpy(s->tr_l_i, s->tr_l_c, sizeof(double) * T);
     memcpy(s->tr_d_i, s->tr_d_c, sizeof(double) * 3 * T);
+    size_t F = (size_t)m->ne_fr;
+    memcpy(s->fr_c_i, s->fr_c_c, sizeof(double) * 9 * F);
+    memcpy(s->fr_c_ip, s->fr_c_c, sizeof(double) * 9 * F);
+    memcpy(s->fr_ef_i, s->fr_ef_c, sizeof(double) * 14 * F);
+    memcpy(s->fr_ef_ip, s->fr_ef_c, sizeof(double) * 14 * F);
+    memcpy(s->fr_l_i, s->fr_l_c, sizeof(double) * F);
+    memcpy(s->fr_l_ip, s->fr_l_c, sizeof(double) * F);
 }
 
 /* "converged <- i" when an increment is accepted (main.c:3060-3105) */
@@ -975,6 +1458,10 @@ static void accept_state(const orc_model *m, state_t *s)
     memcpy(s->tr_ef_c, s->tr_ef_i, sizeof(double) * 2 * T);
     memcpy(s->tr_l_c, s->tr_l_i, sizeof(double) * T);
     memcpy(s->tr_d_c, s->tr_d_i, sizeof(double) * 3 * T);
+    size_t F = (size_t)m->ne_fr;
+    memcpy(s->fr_c_c, s->fr_c_i, sizeof(double) * 9 * F);
+    memcpy(s->fr_ef_c, s->fr_ef_i, sizeof(double) * 14 * F);
+    memcpy(s->fr_l_c, s->fr_l_i, sizeof(double) * F);
 }
 
 static double rel_residual(long neq, const double *q, double lpf, const double *f)
@@ -1014,10 +1501,14 @@ int orc_msal_timed(orc_model *m, int max_steps, double *lam, int *its, double *d
     memcpy(s.sh_a_c, m->sh_area0, sizeof(double) * (size_t)m->ne_sh);
     memcpy(s.tr_l_c, m->tr_len0, sizeof(double) * (size_t)m->ne_tr);
     memcpy(s.tr_d_c, m->tr_dir0, sizeof(double) * 3 * (size_t)m->ne_tr);
+    memcpy(s.fr_c_c, m->fr_c0, sizeof(double) * 9 * (size_t)m->ne_fr);
+    memcpy(s.fr_l_c, m->fr_len0, sizeof(double) * (size_t)m->ne_fr);
+    memcpy(s.fr_lref, m->fr_len0, sizeof(double) * (size_t)m->ne_fr);
     reset_to_converged(m, &s);
 
     /* ---- first increment: displacement control at dkdof (main.c:2296-2560) ---- */
-    orc_tangent(m, s.x, s.sh_c_c, s.sh_a_c, s.tr_l_c, s.tr_d_c, s.tr_ef_c, maxa, ss);
+    tangent_all(m, s.x, s.sh_c_c, s.sh_a_c, s.tr_l_c, s.tr_d_c, s.tr_ef_c, s.fr_c_c, s.fr_ef_c, s.fr_l_c,
+                s.fr_lref, ss);
     memcpy(ddq, q, sizeof(double) * (size_t)N);
     orc_skyline_solve(m, ss, ddq, ssd, &det, 0);
     double lpf = m->dk / ddq[m->dkdof];
@@ -1103,7 +1594,8 @@ int orc_msal_timed(orc_model *m, int max_steps, double *lam, int *its, double *d
             reset_to_converged(m, &s);
             errchk2 = 0;
         }
-        orc_tangent(m, s.x, s.sh_c_c, s.sh_a_c, s.tr_l_c, s.tr_d_c, s.tr_ef_c, maxa, ss);
+        tangent_all(m, s.x, s.sh_c_c, s.sh_a_c, s.tr_l_c, s.tr_d_c, s.tr_ef_c, s.fr_c_c, s.fr_ef_c, s.fr_l_c,
+                    s.fr_lref, ss);
         memcpy(ddq, q, sizeof(double) * (size_t)N);
         orc_skyline_solve(m, ss, ddq, ssd, &det, 0);
         double a = psi >= m->psi_thresh ? qq + vdot(N, ddq, ddq) : vdot(N, ddq, ddq);
@@ -1236,4 +1728,247 @@ done:
     free(ss);
     free(maxa);
     return rc < 0 ? rc : nconv;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Nonlinear Newmark driver (main.c:3305-3960, solve.c:139-222, 469-533)     */
+/* ------------------------------------------------------------------------ */
+
+/* Runs the reference's ALGFLAG 5 time loop for frame-only models (SLVFLAG 0,
+ * no prescribed motion, NBC = 0) and records, for each of the first
+ * max_steps time steps k: time[k] = k dt, its[k] = the iteration count of the
+ * accepted pass, d[k*NEQ ...] (may be NULL), res[k] = |dyn - f| / |dyn| with
+ * dyn = qtot - M a (the dynamic equilibrium the convergence test judges).
+ * Returns the number of steps recorded, or -(error code) with err set. */
+int orc_newmark(orc_model *m, long max_steps, double *time_out, int *its_out, double *dout,
+                double *res_out, char *err, int errlen)
+{
+    if (m->alg != 5) {
+        set_err(err, errlen, "model is not a nonlinear Newmark model (ALGFLAG 5)");
+        return -1;
+    }
+    long N = m->neq, F = m->ne_fr, NT = m->nsteps;
+    if (NT != m->ntin) {
+        set_err(err, errlen, "ttot/dt + 1 differs from the number of input time points");
+        return -1;
+    }
+    size_t nb = sizeof(double) * (size_t)(N + 1);
+    double *d = calloc(1, nb), *f = calloc(1, nb), *d_temp = calloc(1, nb), *f_temp = calloc(1, nb),
+           *fp = calloc(1, nb), *f_ip = calloc(1, nb), *dd = calloc(1, nb), *r = calloc(1, nb),
+           *qtot = calloc(1, nb), *dyn = calloc(1, nb), *uc = calloc(1, nb), *vc = calloc(1, nb),
+           *ac = calloc(1, nb), *uc_i = calloc(1, nb), *vc_i = calloc(1, nb), *ac_i = calloc(1, nb),
+           *um = calloc(1, nb), *vm = calloc(1, nb), *am = calloc(1, nb), *sm = calloc(1, nb),
+           *ssd = calloc(1, nb), *ss = malloc(sizeof(double) * (size_t)m->lss),
+           *lt = malloc(sizeof(double) * (size_t)(F + 1));
+    const double *pin = m->pinpt;
+    state_t s;
+    state_alloc(m, &s);
+    int rc = 0, nrec = 0, det = 0;
+    /* Newmark / HHT / WBZ parameters (main.c:3329-3343) */
+    double alpham = 0, alphaf = 0;
+    if (m->numopt == 1) {
+        alpham = (2 * m->spectrds - 1) / (m->spectrds + 1);
+        alphaf = m->spectrds / (m->spectrds + 1);
+    } else if (m->numopt == 2) {
+        alphaf = (1 - m->spectrds) / (1 + m->spectrds);
+    } else if (m->numopt == 3) {
+        alpham = (m->spectrds - 1) / (m->spectrds + 1);
+    }
+    const double alpha = pow(1 - alpham + alphaf, 2) / 4;
+    const double delta = 0.5 - alpham + alphaf;
+    const double dt = m->dt;
+    double ddt = 1, sub_dt = 1, dt_temp = dt, tsflag = 0;
+    const double lpfi = m->lpf0, dlpfi = m->dlpf0, lpfmax = m->lpfmax;
+    double lpf = lpfi, dlpf = dlpfi, dlpfp = dlpf, intener1 = 0;
+    int convchk = 1, itecnt = 0;
+    /* initial state (main.c:3398-3447): zero motion, frame lengths L0 */
+    memcpy(s.x, m->x0, sizeof(double) * 3 * (size_t)m->nj);
+    memcpy(s.fr_c_c, m->fr_c0, sizeof(double) * 9 * (size_t)F);
+    memcpy(s.fr_l_c, m->fr_len0, sizeof(double) * (size_t)F);
+    memcpy(lt, m->fr_len0, sizeof(double) * (size_t)F);
+    long k = 0;
+    do {
+        dt_temp = ddt * dt;
+        sub_dt = ddt;
+        tsflag = 0;
+        do {
+            const double a0 = 1 / (alpha * pow(dt_temp, 2));
+            const double a2 = 1 / (alpha * dt_temp);
+            const double a3 = 1 / (2 * alpha) - 1;
+            const double a6 = (dt_temp) * (1 - delta);
+            const double a7 = delta * (dt_temp);
+            int solcnt = 0, subcnt = 0;
+            lpf = lpfi;
+            dlpf = dlpfi;
+            do {
+                if (lpf > lpfmax) lpf = lpfmax;
+                for (long i = 0; i < N; ++i) {
+                    fp[i] = f[i];
+                    d_temp[i] = d[i];
+                    f_temp[i] = f[i];
+                }
+                dlpfp = dlpf;
+                reset_to_converged(m, &s);
+                for (long i = 0; i < N; ++i) {
+                    um[i] = uc_i[i] = uc[i];
+                    vm[i] = vc_i[i] = vc[i];
+                    am[i] = ac_i[i] = ac[i];
+                }
+                itecnt = 0;
+                do {
+                    if (itecnt == 0) {
+                        if (k == 0) {
+                            for (long i = 0; i < N; ++i) {
+                                qtot[i] = pin[i * NT + k] * sub_dt * lpf;
+                                r[i] = qtot[i] - f_temp[i];
+                            }
+                        } else {
+                            for (long i = 0; i < N; ++i) {
+                                qtot[i] = (pin[i * NT + k - 1] + (pin[i * NT + k] - pin[i * NT + k - 1]) * (sub_dt)) * lpf;
+                                r[i] = (qtot[i] - f_temp[i]) + alphaf / (1 - alphaf) * (pin[i * NT + k - 1] - f_temp[i]);
+                            }
+                        }
+                    } else {
+                        for (long i = 0; i < N; ++i) {
+                            r[i] = (f_temp[i] - qtot[i]);
+                            r[i] = r[i] + sm[i] * ac_i[i] -
+                                   sm[i] * ((a2 * vc_i[i] + a3 * ac_i[i]) * (1 - alpham) - ac_i[i] * alpham) /
+                                       (1 - alphaf);
+                        }
+                    }
+                    /* tangent from the previous iteration's state, lengths lt from
+                     * the last mass_fr call; mass at the converged coordinates,
+                     * which also rewrites lt (frame.c:1339) */
+                    tangent_all(m, s.x, NULL, NULL, NULL, NULL, NULL, s.fr_c_ip, s.fr_ef_ip, s.fr_l_ip, lt, ss);
+                    memset(sm, 0, nb);
+                    for (long e = 0; e < F; ++e) {
+                        double mt, mr;
+                        lt[e] = frame_mass_element(m, e, s.x, &mt, &mr);
+                        for (int i = 0; i < 14; ++i) {
+                            long q = m->fr_mc[e * 14 + i];
+                            int dof = i % 7;
+                            if (q && dof < 6) sm[q - 1] += dof < 3 ? mt : mr;
+                        }
+                    }
+                    if (m->lss == 1) {
+                        dd[0] = r[0] / ss[0];
+                    } else {
+                        /* Keff = K + a0 (1 - am) / (1 - af) M on the diagonal
+                         * (solve.c:203-210), factored every iteration */
+                        for (long i = 0; i < N; ++i) ss[m->maxa[i] - 1] += a0 * (1 - alpham) * sm[i] / (1 - alphaf);
+                        sky_factor(N, m->maxa, ss, ssd, &det, 1);
+                        /* Reff (solve.c:478-487); inside solve the "m" vectors are
+                         * the current uc_i, vc_i, ac_i */
+                        for (long i = 0; i < N; ++i)
+                            dd[i] = r[i] + sm[i] * ((1 - alpham) * (vc_i[i] * a2 + ac_i[i] * a3) - alpham * ac_i[i]) /
+                                               (1 - alphaf);
+                        sky_solve(N, m->maxa, ss, dd);
+                    }
+                    for (long i = 0; i < N; ++i) {
+                        if (itecnt > 0) dd[i] = dd[i] * (-1);
+                        d_temp[i] += dd[i];
+                        f_ip[i] = f_temp[i];
+                        f_temp[i] = 0;
+                    }
+                    for (long i = 0; i < N; ++i) {
+                        uc_i[i] = d_temp[i];
+                        ac_i[i] = (uc_i[i] - um[i]) * a0 - a2 * vm[i] - a3 * am[i];
+                        vc_i[i] = vm[i] + a6 * am[i] + a7 * ac_i[i];
+                    }
+                    update_coords(m, s.x_temp, dd);
+                    for (long e = 0; e < F; ++e) {
+                        double fe[14];
+                        frame_force_element(m, e, s.x_temp, dd, s.fr_c_ip + e * 9, s.fr_ef_ip + e * 14,
+                                            s.fr_l_ip[e], lt[e], s.fr_c_i + e * 9, s.fr_l_i + e,
+                                            s.fr_ef_i + e * 14, fe);
+                        for (int i = 0; i < 14; ++i) {
+                            long q = m->fr_mc[e * 14 + i];
+                            if (q) f_temp[q - 1] += fe[i];
+                        }
+                    }
+                    for (long i = 0; i < N; ++i) dyn[i] = qtot[i] - sm[i] * ac_i[i];
+                    if (itecnt == 0) {
+                        intener1 = 0;
+                        for (long i = 0; i < N; ++i) intener1 += dd[i] * (dyn[i] - fp[i]);
+                    }
+                    if (orc_test(N, d_temp, dd, f_temp, fp, dyn, f_ip, intener1, &convchk, m->toldisp,
+                                 m->tolforc, m->tolener)) {
+                        set_err(err, errlen, "zero norm in the convergence test");
+                        rc = -1;
+                        goto done;
+                    }
+                    advance_iteration(m, &s);
+                    itecnt++;
+                } while (convchk != 0 && itecnt <= m->itemax);
+                if (convchk != 0 && subcnt <= m->submax) {
+                    if (lpf == lpfmax) break;
+                    else if (dlpfp == m->dlpfmin) break;
+                    dlpf = dlpfp / 2;
+                    if (dlpf < m->dlpfmin) dlpf = m->dlpfmin;
+                    lpf = lpf - dlpfp + dlpf;
+                    subcnt++;
+                    solcnt = 0;
+                } else if (subcnt > m->submax) {
+                    break;
+                } else {
+                    solcnt++;
+                    subcnt = 0;
+                    if (solcnt >= m->solmin) {
+                        dlpf *= 2;
+                        solcnt = 0;
+                    }
+                    lpf += dlpf;
+                }
+            } while (lpf <= lpfmax);
+            if (convchk != 0) {
+                ddt = ddt / 2;
+                dt_temp = ddt * dt;
+                if (tsflag == 0) sub_dt = ddt;
+                else if (tsflag == 1) sub_dt = sub_dt - ddt;
+            } else {
+                memcpy(d, d_temp, nb);
+                memcpy(f, f_temp, nb);
+                memcpy(uc, uc_i, nb);
+                memcpy(vc, vc_i, nb);
+                memcpy(ac, ac_i, nb);
+                accept_state(m, &s);
+            }
+            if (ddt < 1) {
+                if (sub_dt <= 1) {
+                    sub_dt = sub_dt + ddt;
+                    tsflag = 1;
+                }
+                if (sub_dt > 1) {
+                    ddt = ddt * 2;
+                    tsflag = 2;
+                }
+            } else if (ddt == 1) {
+                tsflag = 2;
+            }
+        } while (ddt >= 0.0001 && tsflag != 2);
+        if (convchk != 0) {
+            set_err(err, errlen, "minimum time increment interval reached without convergence");
+            rc = -2;
+            goto done;
+        }
+        if (nrec < max_steps) {
+            time_out[nrec] = (double)k * dt;
+            its_out[nrec] = itecnt;
+            if (dout) memcpy(dout + (size_t)nrec * N, d, sizeof(double) * (size_t)N);
+            double num = 0, den = 0;
+            for (long i = 0; i < N; ++i) {
+                num += (dyn[i] - f[i]) * (dyn[i] - f[i]);
+                den += dyn[i] * dyn[i];
+            }
+            res_out[nrec] = den > 0 ? sqrt(num / den) : 0;
+            nrec++;
+        }
+        ++k;
+    } while (k < NT && nrec < max_steps);
+done:
+    state_free(&s);
+    double *bufs[] = {d, f, d_temp, f_temp, fp, f_ip, dd, r, qtot, dyn, uc, vc, ac, uc_i, vc_i, ac_i,
+                      um, vm, am, sm, ssd, ss, lt};
+    for (size_t i = 0; i < sizeof bufs / sizeof bufs[0]; ++i) free(bufs[i]);
+    return rc < 0 ? rc : nrec;
 }

@@ -18,13 +18,17 @@ extern "C" {
 
 typedef struct orc_model orc_model;
 
-/* Parse a model_def.txt text (ANAFLAG 2, ALGFLAG 3 with truss and DKT shell
- * elements, SLVFLAG 0, OPTFLAG 1). Returns NULL and fills err on failure. */
+/* Parse a model_def.txt text (ANAFLAG 2, SLVFLAG 0, OPTFLAG 1): ALGFLAG 3
+ * (MSAL) with truss, frame and DKT shell elements, or ALGFLAG 5 (nonlinear
+ * Newmark) with frame elements only. Returns NULL and fills err on failure. */
 orc_model *orc_load(const char *text, char *err, int errlen);
 void orc_free(orc_model *m);
 
 /* out[0..7] = NJ, NE_TR, NE_FR, NE_SH, NEQ, lss (skyline length), dkdof, itemax */
 void orc_sizes(const orc_model *m, long *out);
+
+/* ALGFLAG 5 models: number of time steps NTSTPS and dt */
+void orc_dyn_sizes(const orc_model *m, long *nsteps, double *dt);
 
 /* jcode (NJ*7, 1-based equation numbers, 0 = fixed), reference load q (NEQ) */
 void orc_topology(const orc_model *m, long *jcode, double *q);
@@ -39,6 +43,12 @@ int orc_msal(orc_model *m, int max_steps, double *lam, int *its, double *d, doub
  * converged step was accepted in tstamp[k] (may be NULL); d may be NULL. */
 int orc_msal_timed(orc_model *m, int max_steps, double *lam, int *its, double *d, double *res,
                    double *tstamp, char *err, int errlen);
+
+/* Nonlinear Newmark time loop (main.c:3305-3960). Per recorded time step k:
+ * time[k], its[k], d[k*NEQ ...] (d may be NULL), res[k] = |dyn - f| / |dyn|.
+ * Returns the number of steps recorded, or -(error code) with err set. */
+int orc_newmark(orc_model *m, long max_steps, double *time, int *its, double *d, double *res,
+                char *err, int errlen);
 
 /* ---- element-level entry points (state given explicitly) ---- */
 
@@ -66,6 +76,29 @@ void orc_truss_forces(const orc_model *m, const double *x_temp, double *length_i
 void orc_tangent(const orc_model *m, const double *x, const double *c_sh, const double *area_sh,
                  const double *len_tr, const double *dir_tr, const double *ef_tr, long *maxa,
                  double *ss);
+
+/* Frame elements (14 DOF per member, warping included; frame.c).
+ *   orc_frame_initial: initial triads c (NE_FR*9, rows x^, y^, z^) and
+ *     lengths (NE_FR) from prop_fr (frame.c:130-160).
+ *   orc_frame_forces: forces_fr, ANAFLAG 2 (frame.c:902-1312), preceded by the
+ *     frame part of updatc (misc.c:108-147): x_temp (NJ*3) current joint
+ *     coordinates, dd (NEQ), previous-iteration triads c_ip, element forces
+ *     ef_ip (NE_FR*14) and deformed lengths len_ip; lref the reference
+ *     lengths used by the elastic stiffness. Outputs c_i, len_i, ef_i and
+ *     f (NEQ, overwritten).
+ *   orc_tangent_fr: stiff_fr (frame.c:226-362) into the skyline layout.
+ *   orc_frame_mass: mass_fr lumped diagonal mass (frame.c:1314-1391) at the
+ *     joint coordinates x, into sm (NEQ, overwritten). */
+void orc_frame_initial(const orc_model *m, double *c, double *len);
+void orc_frame_forces(const orc_model *m, const double *x_temp, const double *dd, const double *c_ip,
+                      const double *ef_ip, const double *len_ip, const double *lref, double *c_i,
+                      double *len_i, double *ef_i, double *f);
+void orc_tangent_fr(const orc_model *m, const double *c_fr, const double *ef_fr, const double *len_fr,
+                    const double *lref_fr, long *maxa, double *ss);
+void orc_frame_mass(const orc_model *m, const double *x, double *sm);
+
+/* Frame member equation numbers (NE_FR*14, 1-based, 0 = fixed) */
+void orc_frame_mcode(const orc_model *m, long *mc);
 
 /* Skyline LDL^T (solve.c:539-698): factor ss in place (fact == 0), then solve
  * in place on rhs; pivots to ssd, det = 1 when any pivot <= 0. */

@@ -46,6 +46,14 @@ def lib():
         L.orc_tangent.argtypes = [P, dp, dp, dp, dp, dp, dp, lp, dp]
         L.orc_skyline_solve.argtypes = [P, dp, dp, dp, ip, C.c_int]
         L.orc_shell_initial.argtypes = [P, dp, dp]
+        L.orc_dyn_sizes.argtypes = [P, lp, dp]
+        L.orc_newmark.restype = C.c_int
+        L.orc_newmark.argtypes = [P, C.c_long, dp, ip, dp, dp, C.c_char_p, C.c_int]
+        L.orc_frame_initial.argtypes = [P, dp, dp]
+        L.orc_frame_forces.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.orc_tangent_fr.argtypes = [P, dp, dp, dp, dp, lp, dp]
+        L.orc_frame_mass.argtypes = [P, dp, dp]
+        L.orc_frame_mcode.argtypes = [P, lp]
         _lib = L
     return _lib
 
@@ -104,6 +112,56 @@ class OracleModel:
         nconv = int(np.count_nonzero(its))
         return dict(rc=n, error=err.value.decode(), lam=lam[:nconv], its=its[:nconv], res=res[:nconv],
                     t=ts[:nconv], d=d[:nconv] if keep_d else None)
+
+    def dyn_sizes(self):
+        n = np.zeros(1, dtype=np.int64)
+        dt = np.zeros(1)
+        lib().orc_dyn_sizes(self.h, _l(n), _d(dt))
+        return int(n[0]), float(dt[0])
+
+    def newmark(self, steps: int, keep_d: bool = True):
+        """Nonlinear Newmark run; per recorded time step: time, its, d, res."""
+        t = np.zeros(steps)
+        its = np.zeros(steps, dtype=np.int32)
+        d = np.zeros((steps, self.neq)) if keep_d else None
+        res = np.zeros(steps)
+        err = C.create_string_buffer(256)
+        n = lib().orc_newmark(self.h, steps, _d(t), _i(its), _d(d) if keep_d else None, _d(res), err, 256)
+        k = max(n, 0)
+        return dict(rc=n, error=err.value.decode(), time=t[:k], its=its[:k], res=res[:k],
+                    d=d[:k] if keep_d else None)
+
+    def frame_initial(self):
+        c = np.zeros(self.ne_fr * 9)
+        L = np.zeros(self.ne_fr)
+        lib().orc_frame_initial(self.h, _d(c), _d(L))
+        return c, L
+
+    def frame_mcode(self):
+        mc = np.zeros(self.ne_fr * 14, dtype=np.int64)
+        lib().orc_frame_mcode(self.h, _l(mc))
+        return mc
+
+    def frame_forces(self, x_temp, dd, c_ip, ef_ip, len_ip, lref):
+        c_i = np.zeros(self.ne_fr * 9)
+        len_i = np.zeros(self.ne_fr)
+        ef_i = np.zeros(self.ne_fr * 14)
+        f = np.zeros(self.neq)
+        args = [np.ascontiguousarray(v, dtype=np.float64) for v in (x_temp, dd, c_ip, ef_ip, len_ip, lref)]
+        lib().orc_frame_forces(self.h, *[_d(v) for v in args], _d(c_i), _d(len_i), _d(ef_i), _d(f))
+        return c_i, len_i, ef_i, f
+
+    def tangent_fr(self, c, ef, length, lref):
+        maxa = np.zeros(self.neq + 1, dtype=np.int64)
+        ss = np.zeros(self.lss)
+        args = [np.ascontiguousarray(v, dtype=np.float64) for v in (c, ef, length, lref)]
+        lib().orc_tangent_fr(self.h, *[_d(v) for v in args], _l(maxa), _d(ss))
+        return maxa, ss
+
+    def frame_mass(self, x):
+        sm = np.zeros(self.neq)
+        lib().orc_frame_mass(self.h, _d(np.ascontiguousarray(x, dtype=np.float64)), _d(sm))
+        return sm
 
     def shell_initial(self):
         c = np.zeros(self.ne_sh * 9)

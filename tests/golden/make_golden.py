@@ -6,9 +6,12 @@ unmodified from its sources by ``make -C oracle ref``:
 * whole-run fixtures: the reference driver (oracle/_ref/cuben_ref, main.c's
   MSAL loop) run on seeded models, with every converged step's lambda,
   iteration count and FP64 displacement vector dumped by the output() shim;
-* element fixtures: the reference's prop_sh/prop_tr, updatc, forces_sh,
-  forces_tr, stiff_sh, stiff_tr, skyfact and skysolve called through
-  oracle/_ref/libcuben_ref_elem.so on seeded random states.
+  The Newmark fixtures run main.c's ALGFLAG 5 loop the same way and record,
+  per time step, the time (in the "lam" slot), iteration count and d;
+* element fixtures: the reference's prop_sh/prop_tr/prop_fr, updatc,
+  forces_sh, forces_tr, forces_fr, stiff_sh, stiff_tr, stiff_fr, mass_fr,
+  skyfact and skysolve called through oracle/_ref/libcuben_ref_elem.so on
+  seeded random states.
 
 Run in a tree that has the reference (it is not needed to *use* the fixtures):
 
@@ -52,8 +55,27 @@ def panel_controls(n: int, toldisp: float = 1e-5) -> models.MsalControls:
                                tolforc=1.0, tolener=1.0, itemax=100)
 
 
+def frame_msal_controls(nj: int) -> models.MsalControls:
+    # lateral roof displacement control at the last joint; the path passes a
+    # limit point within 40 steps
+    return models.MsalControls(joint=nj, direction=1, dk=0.2, toldisp=1e-8, tolforc=1.0,
+                               tolener=1e-8, itemax=20)
+
+
+def frame_msal_model(warping: str = "member") -> models.ModelSpec:
+    nj = models.frame_building(2, 2, 3, msal=models.MsalControls(1, 1, 0.1)).nj
+    return models.frame_building(2, 2, 3, warping=warping, msal=frame_msal_controls(nj), msal_load=1.0)
+
+
+def frame_newmark_model(warping: str = "fixed", steps: int = 40) -> models.ModelSpec:
+    return models.frame_building(2, 2, 3, warping=warping, steps=steps, dt=0.005, seed=4)
+
+
 def whole_runs():
     cases = {
+        "frame_msal": (frame_msal_model("member"), 40),
+        "frame_newmark_fixed": (frame_newmark_model("fixed"), 41),
+        "frame_newmark_member": (frame_newmark_model("member", 30), 31),
         "truss_c1": (models.space_truss(controls=truss_controls()), 50),
         "panel8": (models.cylindrical_panel(8, controls=panel_controls(8)), 12),
         "panel16_imp": (models.cylindrical_panel(16, seed=7, imperfection=0.1,
@@ -228,8 +250,91 @@ def truss_element_fixture(seed: int = 5):
     print("truss element fixture: T", T, "NEQ", NEQ)
 
 
+def frame_element_fixture(seed: int = 9):
+    m = frame_msal_model("member")
+    o = oracle.OracleModel(m.text)
+    rng = np.random.default_rng(seed)
+    R = RefElem()
+    F, NJ, NEQ = o.ne_fr, o.nj, o.neq
+    R.L.href_set_sizes(C.c_long(NJ), C.c_long(0), C.c_long(F), C.c_long(0), C.c_long(NEQ),
+                       C.c_int(2), C.c_int(3))
+    lines = m.text.splitlines()
+    head = 6 + F
+    ncons = lines[head:].index("0,0") + 1
+    x0 = np.array([[float(v) for v in ln.split(",")] for ln in lines[head + ncons:head + ncons + NJ]])
+    # property lines, offsets terminator, aux points, yield lines, releases terminator
+    k0 = head + ncons + NJ
+    R.read_props("\n".join(lines[k0:k0 + 3 * F + 2]) + "\n")
+    x = np.ascontiguousarray(x0.reshape(-1))
+    emod, gmod, dens, carea, llen = (np.zeros(F) for _ in range(5))
+    istr, iweak, ipol, iwarp, yld, zs, zw = (np.zeros(F) for _ in range(7))
+    xfr, offset, auxpt = np.zeros(6 * F), np.zeros(6 * F), np.zeros(3 * F)
+    osflag = np.zeros(F, dtype=np.int32)
+    mendrel = np.zeros(5 * F, dtype=np.int32)
+    c1, c2, c3 = np.zeros(3 * F), np.zeros(3 * F), np.zeros(3 * F)
+    minc = np.array([[int(v) for v in ln.split(",")] for ln in lines[6:6 + F]], dtype=np.int64).reshape(-1)
+    R.L.prop_fr(p(x), p(xfr), p(emod), p(gmod), p(dens), p(offset), p(osflag), p(auxpt), p(carea),
+                p(llen), p(istr), p(iweak), p(ipol), p(iwarp), p(yld), p(zs), p(zw), p(c1), p(c2),
+                p(c3), p(mendrel), p(minc))
+    jcode = o.jcode.copy()
+    mcode = o.frame_mcode()
+    x_ip = np.zeros(3 * NJ)
+    z = np.zeros(max(1, 3 * F))
+
+    def updatc(xt, dd, cc1, cc2, cc3, dl):
+        xfr_t = xfr.copy()
+        R.L.updatc(p(xt), p(x_ip), p(xfr_t), p(dd), p(dl), p(z), p(z), p(offset), p(osflag),
+                   p(auxpt), p(cc1), p(cc2), p(cc3), p(minc), p(jcode))
+
+    x_temp = x.copy()
+    dd1 = rng.normal(scale=0.05, size=NEQ)
+    c1_ip, c2_ip, c3_ip = c1.copy(), c2.copy(), c3.copy()
+    len_ip = np.zeros(F)
+    updatc(x_temp, dd1, c1_ip, c2_ip, c3_ip, len_ip)
+    x_before = x_temp.copy()
+    dd2 = rng.normal(scale=0.01, size=NEQ)
+    c1_i, c2_i, c3_i = c1.copy(), c2.copy(), c3.copy()
+    len_i = np.zeros(F)
+    updatc(x_temp, dd2, c1_i, c2_i, c3_i, len_i)
+    ef_ip = rng.normal(scale=1e4, size=14 * F)
+    ef_ip_in = ef_ip.copy()
+    ef_i = np.zeros(14 * F)
+    efFE = np.zeros(14 * F)
+    efFE_ip, efFE_i = np.zeros(14 * F), np.zeros(14 * F)
+    yldflag = np.zeros(2 * F, dtype=np.int32)
+    f = np.zeros(NEQ)
+    dlpf = np.zeros(1)
+    itecnt = np.zeros(1, dtype=np.int32)
+    rc = R.L.forces_fr(p(f), p(ef_ip), p(ef_i), p(efFE), p(efFE_ip), p(efFE_i), p(yldflag), p(dd2),
+                       p(emod), p(gmod), p(carea), p(offset), p(osflag), p(llen), p(len_ip), p(istr),
+                       p(iweak), p(ipol), p(iwarp), p(yld), p(zs), p(zw), p(c1_ip), p(c2_ip), p(c3_ip),
+                       p(c1_i), p(c2_i), p(c3_i), p(mendrel), p(mcode), p(dlpf), p(itecnt))
+    assert rc == 0
+    maxa = o.tangent_fr(np.zeros(9 * F), np.zeros(14 * F), np.ones(F), np.ones(F))[0]
+    ss = np.zeros(o.lss)
+    R.L.stiff_fr(p(ss), p(emod), p(gmod), p(carea), p(offset), p(osflag), p(llen), p(len_i), p(istr),
+                 p(iweak), p(ipol), p(iwarp), p(yldflag), p(yld), p(zs), p(zw), p(c1_i), p(c2_i),
+                 p(c3_i), p(ef_i), p(efFE_i), p(mendrel), p(maxa), p(mcode))
+    sm = np.zeros(NEQ)
+    lmass = llen.copy()
+    xfr_m = xfr.copy()
+    jac = np.zeros(1)
+    R.L.mass_fr(p(sm), p(carea), p(lmass), p(istr), p(iweak), p(ipol), p(iwarp), p(dens), p(osflag),
+                p(offset), p(x_temp), p(xfr_m), p(minc), p(mcode), p(jac))
+
+    def triads(a1, a2, a3):
+        return np.stack([a1.reshape(F, 3), a2.reshape(F, 3), a3.reshape(F, 3)], axis=1).reshape(-1)
+
+    np.savez_compressed(OUT / "elem_frame_2x2x3.npz", model_def=np.array(m.text), x_before=x_before,
+                        dd=dd2, c_ip=triads(c1_ip, c2_ip, c3_ip), ef_ip=ef_ip_in, len_ip=len_ip,
+                        lref=llen, x_after=x_temp, c_i=triads(c1_i, c2_i, c3_i), len_i=len_i,
+                        ef_i=ef_i, f=f, maxa=maxa, ss=ss, sm=sm, mass_len=lmass)
+    print("frame element fixture: F", F, "NEQ", NEQ, "lss", o.lss)
+
+
 if __name__ == "__main__":
     oracle.build()
+    frame_element_fixture()
     shell_element_fixture()
     truss_element_fixture()
     whole_runs()

@@ -14,7 +14,7 @@ def _model(z):
     return oracle.OracleModel(str(z["model_def"]))
 
 
-@pytest.mark.parametrize("name", ["truss_c1", "panel8", "panel16_imp"])
+@pytest.mark.parametrize("name", ["truss_c1", "panel8", "panel16_imp", "frame_msal"])
 def test_msal_path_matches_reference(golden_dir, name):
     z = np.load(golden_dir / f"run_{name}.npz")
     o = _model(z)
@@ -66,3 +66,35 @@ def test_truss_forces_and_tangent_match_reference(golden_dir):
     maxa, ss = o.tangent(z["x_after"], np.zeros(0), np.zeros(0), L, dr, ef)
     np.testing.assert_array_equal(maxa, z["maxa"])
     np.testing.assert_allclose(ss, z["ss"], rtol=0, atol=1e-12 * np.abs(z["ss"]).max())
+
+
+@pytest.mark.parametrize("name", ["frame_newmark_fixed", "frame_newmark_member"])
+def test_newmark_path_matches_reference(golden_dir, name):
+    """Nonlinear Newmark time loop (ALGFLAG 5) on a 2x2-bay, 3-storey frame,
+    warping fixed (6 DOF per joint) and one warping DOF per member end."""
+    z = np.load(golden_dir / f"run_{name}.npz")
+    o = _model(z)
+    assert o.neq == int(z["neq"])
+    steps = len(z["lam"])
+    r = o.newmark(steps)
+    assert r["rc"] == steps, r["error"]
+    np.testing.assert_array_equal(r["its"], z["iterations"])
+    np.testing.assert_array_equal(r["time"], z["lam"])
+    np.testing.assert_array_equal(r["d"], z["d"])
+    assert np.all(r["res"] < 1e-6)
+
+
+def test_frame_forces_tangent_mass_match_reference(golden_dir):
+    z = np.load(golden_dir / "elem_frame_2x2x3.npz")
+    o = _model(z)
+    c_i, len_i, ef_i, f = o.frame_forces(z["x_after"], z["dd"], z["c_ip"], z["ef_ip"], z["len_ip"],
+                                         z["lref"])
+    np.testing.assert_allclose(c_i, z["c_i"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(len_i, z["len_i"], rtol=1e-15)
+    np.testing.assert_allclose(ef_i, z["ef_i"], rtol=0, atol=1e-12 * np.abs(z["ef_i"]).max())
+    np.testing.assert_allclose(f, z["f"], rtol=0, atol=1e-12 * np.abs(z["f"]).max())
+    maxa, ss = o.tangent_fr(z["c_i"], z["ef_i"], z["len_i"], z["lref"])
+    np.testing.assert_array_equal(maxa, z["maxa"])
+    np.testing.assert_allclose(ss, z["ss"], rtol=0, atol=1e-12 * np.abs(z["ss"]).max())
+    sm = o.frame_mass(z["x_after"])
+    np.testing.assert_array_equal(sm, z["sm"])
