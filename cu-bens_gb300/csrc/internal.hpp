@@ -24,6 +24,17 @@ struct HostModel {
     std::vector<double> tr_e, tr_a;
     std::vector<int> sh_conn;  // NE_SH*3
     std::vector<double> sh_e, sh_nu, sh_t;
+    std::vector<int> fr_conn;  // NE_FR*2
+    std::vector<double> fr_prop;  // NE_FR*8, per member: E, G, rho, A, I strong, I weak, J, I warping
+    std::vector<double> fr_aux;   // NE_FR*3 auxiliary points
+    std::vector<long> fr_mc;      // NE_FR*14 1-based equation numbers (0 = fixed), warping per member
+    int alg = 3;                  // ALGFLAG: 3 MSAL, 5 nonlinear Newmark
+    // nonlinear Newmark input (main.c:1600-1607, 3320-3326; load, model.c:1492-1609)
+    long ntin = 0;                // input time points
+    long nsteps = 0;              // NTSTPS = (long)(ttot/dt + 1)
+    double dt = 0, ttot = 0, numopt = 0, spectrds = 1, lpf0 = 1, dlpf0 = 1, dlpfmax = 1, dlpfmin = 1;
+    int solmin = 1;
+    std::vector<double> pin;      // ntin*NEQ joint forces, time-major: pin[k*NEQ + i]
     // MSAL controls (arc.c:48, main.c:2240-2245)
     long dkdof = -1;
     double dk = 0, alpha = 1, psi_thresh = 0.1, lpfmax = 0, dkimax = 0;
@@ -66,6 +77,18 @@ struct DevShell {
     double *c_c = nullptr, *c_ip = nullptr, *c_i = nullptr;     // 9*E triads
     double *a_c = nullptr, *a_i = nullptr;                      // E areas
     double *ef_c = nullptr, *ef_ip = nullptr, *ef_i = nullptr;  // 18*E element forces
+};
+
+// Frame member data, structure-of-arrays (index k*F + e).
+struct DevFrame {
+    int *conn = nullptr;       // 2*F
+    int *eq = nullptr;         // 14*F, 0-based equation or -1
+    double *prop = nullptr;    // 8*F: E, G, rho, A, I strong, I weak, J, I warping
+    double *aux = nullptr;     // 3*F auxiliary points
+    double *len0 = nullptr;    // F initial lengths
+    double *c_c = nullptr, *c_ip = nullptr, *c_i = nullptr;        // 9*F triads (rows x^, y^, z^)
+    double *ef_c = nullptr, *ef_ip = nullptr, *ef_i = nullptr;     // 14*F local element forces
+    double *len_c = nullptr, *len_ip = nullptr, *len_i = nullptr;  // F deformed lengths
 };
 
 struct DevTruss {
@@ -138,6 +161,18 @@ template <typename T>
 void launch_shell_tangent(const DevShell &s, const double *x_c, T *kel, long ne, cudaStream_t st);
 template <typename T>
 void launch_truss_tangent(const DevTruss &t, T *kel, long nt, cudaStream_t st);
+void launch_frame_geometry(const DevFrame &fr, const double *x, double *c, double *len, long F,
+                           cudaStream_t st);
+// forces_fr with the frame part of updatc: c_i, len_i, ef_i and the element
+// forces fe[k*F + e]; lref are the lengths the elastic stiffness uses
+void launch_frame_forces(const DevFrame &fr, const double *x_t, const double *dd, const double *lref,
+                         double *fe, long F, cudaStream_t st);
+template <typename T>
+void launch_frame_tangent(const DevFrame &fr, const double *c, const double *ef, const double *len,
+                          const double *lref, T *kel, long F, cudaStream_t st);
+// lumped mass contributions me[k*F + e] at the coordinates x; lt <- member lengths
+void launch_frame_mass(const DevFrame &fr, const double *x, double *lt, double *me, long F,
+                       cudaStream_t st);
 void launch_gather_f64(const int *ptr, const int *src, const double *in, double *out, long n,
                        cudaStream_t st);
 template <typename T>
@@ -196,5 +231,25 @@ void launch_psi(const double *ssd, const double *ssd_o, double *partial, MsalSca
 void launch_scale(const double *x, double alpha, double *y, long n, cudaStream_t st);
 // y += alpha * x
 void launch_axpy(const double *x, double alpha, double *y, long n, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Nonlinear Newmark vector algebra (vecops.cu)
+// ---------------------------------------------------------------------------
+// qtot (predictor modes 0, 1) and Reff = residual + M-weighted inertia terms
+void launch_nm_reff(int mode, double sub_dt, double lpf, double alpham, double alphaf, double a2, double a3,
+                    const double *pin_km1, const double *pin_k, const double *f_temp, const double *sm,
+                    const double *vc_i, const double *ac_i, double *qtot, double *reff, long n, cudaStream_t st);
+// band diagonal += c0 sm / den
+template <typename T>
+void launch_nm_keff(T *band, long ld, const double *sm, double c0, double den, long n, cudaStream_t st);
+// dd sign, d_temp, Newmark kinematics, x_temp
+void launch_nm_update(double *dd, int neg, double *d_temp, const double *um, const double *vm, const double *am,
+                      double *uc_i, double *vc_i, double *ac_i, double a0, double a2, double a3, double a6,
+                      double a7, const int *eq_x, double *x_t, long n, cudaStream_t st);
+// dyn = qtot - sm ac_i, the test sums -> sc->dots[0..6], intener1 on the first
+// iteration, convchk / test_err
+void launch_nm_test(const double *dd, const double *dt, const double *f, const double *fp, const double *fip,
+                    const double *qtot, const double *sm, const double *ac_i, double *dyn, double *partial,
+                    MsalScalars *sc, int first, long n, cudaStream_t st);
 
 }  // namespace cb

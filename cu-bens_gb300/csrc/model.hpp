@@ -1,0 +1,186 @@
+// The resident model handle (cb_model) and the driver steps that the
+// arc-length (msal.cu) and Newmark (newmark.cu) drivers share.
+//
+// State that the reference keeps as "converged" (x, c, ef, deffarea,
+// defllen) and "current/previous iteration" (x_temp, c_i, c_ip, ef_i, ef_ip,
+// defllen_i, defllen_ip) arrays is kept in the same three roles on the
+// device.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "cubens_gb300.h"
+#include "internal.hpp"
+
+#define CB_CUDA(x)                                                                         \
+    do {                                                                                   \
+        cudaError_t e_ = (x);                                                              \
+        if (e_ != cudaSuccess)                                                             \
+            throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + \
+                                     " at " __FILE__ ":" + std::to_string(__LINE__));      \
+    } while (0)
+
+struct cb_status_error : std::runtime_error {
+    int code;
+    cb_status_error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+struct cb_model {
+    cb::HostModel h;
+    cb_options opt{};
+    std::string err;
+    cudaStream_t st = nullptr;
+    size_t bytes = 0;
+    size_t h2d_bytes = 0;
+    std::vector<void *> allocs;
+
+    // nodes and equations
+    double *x0 = nullptr, *x_c = nullptr, *x_t = nullptr;
+    int *eq_x = nullptr;
+    // global vectors (NEQ)
+    double *q = nullptr, *d = nullptr, *dp = nullptr, *dpp = nullptr, *ddq = nullptr, *ddr = nullptr,
+           *dd = nullptr, *dt = nullptr, *r = nullptr, *f = nullptr, *zero = nullptr, *ssd_o = nullptr;
+    double *fcur = nullptr, *fprev = nullptr;  // f_temp and f_ip
+    // elements
+    cb::DevShell sh;
+    cb::DevTruss tr;
+    cb::DevFrame fr;
+    double *fr_lref = nullptr;  // lengths the frame elastic stiffness uses (llength / llength_temp)
+    double *fe = nullptr;       // element force contributions
+    void *kel = nullptr;        // element tangents
+    int *fmap_ptr = nullptr, *fmap_src = nullptr;
+    int *tmap_ptr = nullptr, *tmap_src = nullptr;
+    int64_t *tmap_dst = nullptr;
+    long tmap_n = 0;
+    cb::BandFactor bf;
+    cb::MsalScalars *sc = nullptr, *sc_h = nullptr;
+    double *partial = nullptr;
+
+    // MSAL host control state (main.c:2205-2230)
+    int phase = 0;  // 0 created, 1 first increment done
+    double lpf = 0, lpfp = 0, lpfpp = 0, beta = 0, psi = 1, dnormallow = 0, dnorm = 0, arc = 0, qq = 0;
+    double dkc = 0, lpfc = 0;
+    int errchk2 = 0, subcnt = 0, imagcnt = 0, negcnt = 0, itecnt = 0;
+
+    // Newmark (ALGFLAG 5): kinematics and per-step vectors (NEQ), frame
+    // mass contributions (14 F) and the per-step joint forces (ntin NEQ)
+    double *uc = nullptr, *vc = nullptr, *ac = nullptr, *uc_i = nullptr, *vc_i = nullptr, *ac_i = nullptr,
+           *um = nullptr, *vm = nullptr, *am = nullptr, *sm = nullptr, *qtot = nullptr, *dyn = nullptr,
+           *fp = nullptr;
+    double *me = nullptr;
+    double *pin = nullptr;
+    int nm_phase = 0;       // 0 not started, 1 running, 2 finished
+    long nm_k = 0;          // next time step
+    double nm_ddt = 1;      // time increment multiplier carried between steps (main.c:3452)
+
+    // timing
+    bool timing = false;
+    cb_timers tm{};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t marks[8] = {};
+
+    template <typename T>
+    T *alloc(size_t n)
+    {
+        void *p = nullptr;
+        size_t b = std::max<size_t>(1, n) * sizeof(T);
+        CB_CUDA(cudaMalloc(&p, b));
+        CB_CUDA(cudaMemsetAsync(p, 0, b, st));
+        allocs.push_back(p);
+        bytes += b;
+        return (T *)p;
+    }
+};
+
+template <typename T>
+inline void h2d(T *dst, const T *src, size_t n, cudaStream_t st)
+{
+    if (n) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+template <typename T>
+inline void d2h(T *dst, const T *src, size_t n, cudaStream_t st)
+{
+    if (n) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, st));
+}
+template <typename T>
+inline void d2d(T *dst, const T *src, size_t n, cudaStream_t st)
+{
+    if (n && dst != src) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+}
+
+// AoS (element-major, k fastest) <-> SoA (k-major) for per-element arrays
+inline std::vector<double> to_soa(const double *aos, long ne, int k)
+{
+    std::vector<double> s((size_t)ne * k);
+    for (long e = 0; e < ne; ++e)
+        for (int j = 0; j < k; ++j) s[(size_t)j * ne + e] = aos[(size_t)e * k + j];
+    return s;
+}
+inline void from_soa(const std::vector<double> &s, long ne, int k, double *aos)
+{
+    for (long e = 0; e < ne; ++e)
+        for (int j = 0; j < k; ++j) aos[(size_t)e * k + j] = s[(size_t)j * ne + e];
+}
+
+// Adds the GPU time of a driver phase to a timer when timing is on.
+struct PhaseTimer {
+    cb_model *m;
+    double *acc;
+    PhaseTimer(cb_model *m_, double *acc_) : m(m_), acc(acc_)
+    {
+        if (m->timing) CB_CUDA(cudaEventRecord(m->ev[0], m->st));
+    }
+    ~PhaseTimer()
+    {
+        if (!m->timing) return;
+        cudaEventRecord(m->ev[1], m->st);
+        cudaEventSynchronize(m->ev[1]);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, m->ev[0], m->ev[1]);
+        *acc += ms;
+    }
+};
+
+// Runs fn, turning exceptions into the handle's status code and message.
+template <typename F>
+int guarded(cb_model *m, F &&fn)
+{
+    try {
+        fn();
+        return CB_OK;
+    } catch (const cb_status_error &e) {
+        m->err = e.what();
+        return e.code;
+    } catch (const std::exception &e) {
+        m->err = e.what();
+        return CB_ERR_CUDA;
+    }
+}
+
+namespace drv {
+
+// Which element state the tangent is formed from: the converged one (MSAL,
+// main.c:2719-2727) or the previous iteration's (Newmark, main.c:3596-3620).
+enum class TangentState { converged, previous_iteration };
+
+void upload_model(cb_model *m);
+void reset_to_converged(cb_model *m);
+void advance_iteration(cb_model *m);
+void accept_state(cb_model *m, bool latest_in_ip = false);
+void internal_force(cb_model *m, const double *dd_vec, double *fout);
+void assemble_tangent(cb_model *m, TangentState which = TangentState::converged);
+void factor(cb_model *m);
+void solve(cb_model *m, const double *rhs, double *x);
+cb::MsalScalars &pull_scalars(cb_model *m);
+double device_dot(cb_model *m, const double *a, const double *b, bool diff = false);
+double device_elem(cb_model *m, const double *v, long i);
+
+}  // namespace drv

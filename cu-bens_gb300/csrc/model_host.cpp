@@ -2,9 +2,12 @@
 // that drive the deterministic (atomics-free) assembly on the GPU.
 //
 // Reading order follows main.c:340-433 (header), struc model.c:95-264
-// (incidences, constraints), main.c:1395 (coordinates), prop_tr truss.c:66,
-// prop_sh shell.c:61 (properties), load model.c:1313-1335 (joint loads) and
-// msal arc.c:48 / main.c:2240-2245 (MSAL controls).
+// (incidences, constraints), skylin model.c:1156-1201 (prescribed-motion
+// list of dynamic analyses), main.c:1395 (coordinates), prop_tr truss.c:66,
+// prop_fr frame.c:43-224, prop_sh shell.c:61 (properties), load
+// model.c:1313-1335 / 1492-1609 (joint loads, static or per time step) and
+// msal arc.c:48 / main.c:2240-2245 (MSAL controls) or main.c:3320-3326
+// (Newmark controls).
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -55,9 +58,18 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         status = CB_ERR_UNSUPPORTED;
         return "only ANAFLAG 2 (second-order elastic) is on the GPU path";
     }
-    if (alg != 3) {
+    if (alg != 3 && alg != 5) {
         status = CB_ERR_UNSUPPORTED;
-        return "only ALGFLAG 3 (modified spherical arc length) is on the GPU path";
+        return "only ALGFLAG 3 (modified spherical arc length) and 5 (nonlinear Newmark) are on the GPU path";
+    }
+    m.alg = alg;
+    if (alg == 5) {
+        (void)t.next();  // CHKPT
+        int rflag = (int)t.next();
+        if (rflag != 0) {
+            status = CB_ERR_UNSUPPORTED;
+            return "restart from a checkpoint (RFLAG 1) is not supported";
+        }
     }
     int slv = (int)t.next();
     int opt = (int)t.next();
@@ -75,18 +87,31 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
     m.ne_sh = (long)t.next();
     long nsbr = (long)t.next(), nfbr = (long)t.next();
     if (!t.ok || m.nj <= 0) return "bad control block";
-    if (m.ne_fr || nsbr || nfbr) {
+    if (nsbr || nfbr) {
         status = CB_ERR_UNSUPPORTED;
-        return "frame and brick elements are not on the GPU MSAL path";
+        return "brick elements are not on the GPU path";
     }
-    const long NJ = m.nj;
+    if (alg == 5 && (m.ne_tr || m.ne_sh)) {
+        status = CB_ERR_UNSUPPORTED;
+        return "the GPU Newmark path takes frame-only models (mass_fr indexes its properties without "
+               "the truss offset, frame.c:1357-1363)";
+    }
+    const long NJ = m.nj, F = m.ne_fr;
     std::vector<char> has_tr(NJ, 0), has_sh(NJ, 0);
+    std::vector<int> nfr(NJ, 0), wrp(NJ, 0);
     m.tr_conn.resize(2 * m.ne_tr);
     for (long i = 0; i < 2 * m.ne_tr; ++i) {
         long j = (long)t.next() - 1;
         if (j < 0 || j >= NJ) return "truss incidence out of range";
         m.tr_conn[i] = (int)j;
         has_tr[j] = 1;
+    }
+    m.fr_conn.resize(2 * F);
+    for (long i = 0; i < 2 * F; ++i) {
+        long j = (long)t.next() - 1;
+        if (j < 0 || j >= NJ) return "frame incidence out of range";
+        m.fr_conn[i] = (int)j;
+        nfr[j]++;
     }
     m.sh_conn.resize(3 * m.ne_sh);
     for (long i = 0; i < 3 * m.ne_sh; ++i) {
@@ -95,30 +120,71 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         m.sh_conn[i] = (int)j;
         has_sh[j] = 1;
     }
+    // constraints (struc, model.c:216-264); "j,7,r" also sets the warping
+    // restraint flag r: 1 gives every member end at the joint its own
+    // warping DOF
     m.jcode.assign(NJ * 7, -1);
     for (;;) {
         long j = (long)t.next(), k = (long)t.next();
         if (!t.ok) return "constraint list not terminated";
         if (j == 0) break;
         if (j < 0 || j > NJ || k < 1 || k > 7) return "joint constraint input not recognized";
-        if (k == 7) (void)t.next();
+        if (k == 7) wrp[j - 1] = (int)t.next();
         m.jcode[(j - 1) * 7 + k - 1] = 0;
     }
     // DOFs no element type uses (model.c:267-285): truss joints keep 1-3,
-    // shell joints keep 1-6, warping is fixed without frames.
+    // shell joints 1-6, frame joints all 7
     for (long i = 0; i < NJ; ++i) {
-        if (!has_sh[i]) {
-            int from = has_tr[i] ? 3 : 0;
-            for (int j = from; j < 7; ++j) m.jcode[i * 7 + j] = 0;
-        } else {
-            m.jcode[i * 7 + 6] = 0;
+        if (nfr[i] == 0) {
+            if (!has_sh[i]) {
+                int from = has_tr[i] ? 3 : 0;
+                for (int j = from; j < 7; ++j) m.jcode[i * 7 + j] = 0;
+            } else {
+                m.jcode[i * 7 + 6] = 0;
+            }
         }
     }
+    // equation numbers (codes, model.c:941-961)
     long neq = 0;
-    for (long i = 0; i < NJ * 7; ++i)
-        if (m.jcode[i] != 0) m.jcode[i] = ++neq;
+    for (long i = 0; i < NJ; ++i) {
+        for (int j = 0; j < 6; ++j)
+            if (m.jcode[i * 7 + j] != 0) m.jcode[i * 7 + j] = ++neq;
+        if (m.jcode[i * 7 + 6] != 0) {
+            m.jcode[i * 7 + 6] = ++neq;
+        } else if (wrp[i] == 1) {
+            m.jcode[i * 7 + 6] = ++neq;
+            neq += nfr[i] - 1;
+        }
+    }
     m.neq = neq;
     if (neq == 0) return "no free degrees of freedom";
+    // frame member codes; a joint with one warping DOF per member counts
+    // them up over its members in element order (model.c:1007-1032)
+    m.fr_mc.assign(14 * F, 0);
+    {
+        std::vector<int> cnt(nfr);
+        for (long e = 0; e < F; ++e)
+            for (int a = 0; a < 2; ++a) {
+                long j = m.fr_conn[e * 2 + a];
+                for (int d = 0; d < 6; ++d) m.fr_mc[e * 14 + a * 7 + d] = m.jcode[j * 7 + d];
+                if (wrp[j] == 1) {
+                    m.fr_mc[e * 14 + a * 7 + 6] = m.jcode[j * 7 + 6] + nfr[j] - cnt[j];
+                    cnt[j]--;
+                } else {
+                    m.fr_mc[e * 14 + a * 7 + 6] = m.jcode[j * 7 + 6];
+                }
+            }
+    }
+    if (alg == 5) {
+        // prescribed support motion list (skylin, model.c:1156-1201)
+        long j = (long)t.next();
+        (void)t.next();
+        if (!t.ok) return "model_def ended before the prescribed-motion list";
+        if (j != 0) {
+            status = CB_ERR_UNSUPPORTED;
+            return "prescribed support motion (NBC > 0) is not supported";
+        }
+    }
     // skyline column heights (skylin, model.c:1204-1277)
     std::vector<long> kht(neq, 0);
     auto profile = [&](const long *mc, int nd) {
@@ -134,6 +200,7 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
             for (int d = 0; d < 3; ++d) mc[a * 3 + d] = m.jcode[m.tr_conn[e * 2 + a] * 7 + d];
         profile(mc, 6);
     }
+    for (long e = 0; e < F; ++e) profile(&m.fr_mc[e * 14], 14);
     for (long e = 0; e < m.ne_sh; ++e) {
         long mc[18];
         for (int a = 0; a < 3; ++a)
@@ -158,6 +225,28 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         (void)t.next();  // density
         (void)t.next();  // yield stress (ANAFLAG 3 only)
     }
+    // frame properties (prop_fr, frame.c:43-224)
+    m.fr_prop.resize(8 * F);
+    m.fr_aux.resize(3 * F);
+    if (F > 0) {
+        for (long i = 0; i < F * 8; ++i) m.fr_prop[i] = t.next();
+        long j = (long)t.next();
+        for (int k = 0; k < 6; ++k) (void)t.next();
+        if (!t.ok) return "model_def ended inside the frame properties";
+        if (j != 0) {
+            status = CB_ERR_UNSUPPORTED;
+            return "frame member end offsets are not supported";
+        }
+        for (long i = 0; i < F * 3; ++i) m.fr_aux[i] = t.next();
+        for (long i = 0; i < F * 3; ++i) (void)t.next();  // yield stress, plastic moduli (ANAFLAG 3)
+        j = (long)t.next();
+        for (int k = 0; k < 4; ++k) (void)t.next();
+        if (!t.ok) return "model_def ended inside the frame properties";
+        if (j != 0) {
+            status = CB_ERR_UNSUPPORTED;
+            return "frame member end releases are not supported";
+        }
+    }
     m.sh_e.resize(m.ne_sh);
     m.sh_nu.resize(m.ne_sh);
     m.sh_t.resize(m.ne_sh);
@@ -170,6 +259,73 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
     }
     if (!t.ok) return "model_def ended inside the properties";
     m.q.assign(neq, 0.0);
+    if (alg == 5) {
+        // time points (main.c:1600-1607) and per-step joint forces (load,
+        // model.c:1516-1549): the lines of one DOF are consecutive time
+        // points; a zero force is stored as 1e-30
+        long ntsteps = (long)t.next();
+        m.ttot = t.next();
+        if (!t.ok || ntsteps <= 0) return "bad time-step line";
+        m.dt = m.ttot / (double)ntsteps;
+        m.ntin = ntsteps + 1;
+        m.nsteps = (long)(m.ttot / m.dt + 1);
+        if (m.nsteps != m.ntin) {
+            status = CB_ERR_UNSUPPORTED;
+            return "ttot/dt + 1 differs from the number of input time points";
+        }
+        m.pin.assign((size_t)m.ntin * neq, 0.0);
+        long kps = 0, i = 0;
+        for (;;) {
+            long jt = (long)t.next();
+            long dir = (long)t.next();
+            double mag = t.next();
+            if (!t.ok) return "joint load list not terminated";
+            if (jt == 0) break;
+            if (jt < 0 || jt > NJ || dir < 1 || dir > 7) return "joint load out of range";
+            if (mag == 0) mag = 1e-30;
+            long ks = m.jcode[(jt - 1) * 7 + dir - 1];
+            if (ks != kps) i = 0;
+            if (ks != 0) {
+                if (i >= m.ntin) return "more load lines for one DOF than input time points";
+                m.pin[(size_t)i * neq + (ks - 1)] = mag;
+            }
+            kps = ks;
+            ++i;
+        }
+        long jt = (long)t.next();
+        (void)t.next();
+        (void)t.next();
+        if (!t.ok) return "prescribed displacement list not terminated";
+        if (jt != 0) {
+            status = CB_ERR_UNSUPPORTED;
+            return "prescribed displacements are not supported";
+        }
+        // initial conditions: read and dropped, since the reference zeroes
+        // uc, vc and ac before the first step (main.c:3440-3443)
+        for (;;) {
+            jt = (long)t.next();
+            for (int k = 0; k < 4; ++k) (void)t.next();
+            if (!t.ok) return "initial condition list not terminated";
+            if (jt == 0) break;
+        }
+        m.numopt = t.next();
+        m.spectrds = t.next();
+        m.lpfmax = t.next();
+        m.lpf0 = t.next();
+        m.dlpf0 = t.next();
+        m.dlpfmax = t.next();
+        m.dlpfmin = t.next();
+        m.itemax = (int)t.next();
+        m.submax = (int)t.next();
+        m.solmin = (int)t.next();
+        m.toldisp = t.next();
+        m.tolforc = t.next();
+        m.tolener = t.next();
+        if (!t.ok) return "model_def ended inside the Newmark controls";
+        if (m.numopt == 0 && m.spectrds != 1) return "invalid spectral radius for Newmark without dissipation";
+        status = CB_OK;
+        return "";
+    }
     bool any_load = false;
     for (;;) {
         long jt = (long)t.next();
@@ -181,6 +337,16 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         long k = m.jcode[(jt - 1) * 7 + dir - 1];
         if (k != 0) m.q[k - 1] = mag;
         any_load = true;
+    }
+    if (F > 0) {
+        long fr = (long)t.next();
+        (void)t.next();
+        (void)t.next();
+        if (!t.ok) return "distributed load list not terminated";
+        if (fr != 0) {
+            status = CB_ERR_UNSUPPORTED;
+            return "frame distributed loads are not supported";
+        }
     }
     if (!any_load) return "no forces present in input file";
     long jt = (long)t.next();
@@ -206,13 +372,14 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
     return "";
 }
 
-// Force map. The reference accumulates forces_tr before forces_sh, elements
-// in order, so every equation's list is sorted by (type, element). The
-// contribution buffer holds the shell element forces at [k*E + e] (k < 18),
-// followed by the truss forces at 18E + [k*T + e] (k < 6).
+// Force map. The reference accumulates forces_tr, forces_fr, forces_sh in
+// that order, elements in order, so every equation's list is sorted by
+// (type, element). The contribution buffer holds the shell element forces at
+// [k*E + e] (k < 18), the truss forces at 18E + [k*T + e] (k < 6) and the
+// frame forces at 18E + 6T + [k*F + e] (k < 14).
 void build_force_map(const HostModel &m, GatherMap &g)
 {
-    const long E = m.ne_sh, T = m.ne_tr;
+    const long E = m.ne_sh, T = m.ne_tr, F = m.ne_fr;
     std::vector<std::vector<int>> lists(m.neq);
     for (long e = 0; e < T; ++e)
         for (int a = 0; a < 2; ++a)
@@ -220,6 +387,11 @@ void build_force_map(const HostModel &m, GatherMap &g)
                 long q = m.jcode[m.tr_conn[e * 2 + a] * 7 + d];
                 if (q) lists[q - 1].push_back((int)(18 * E + (a * 3 + d) * T + e));
             }
+    for (long e = 0; e < F; ++e)
+        for (int k = 0; k < 14; ++k) {
+            long q = m.fr_mc[e * 14 + k];
+            if (q) lists[q - 1].push_back((int)(18 * E + 6 * T + k * F + e));
+        }
     for (long e = 0; e < E; ++e)
         for (int a = 0; a < 3; ++a)
             for (int d = 0; d < 6; ++d) {
@@ -240,20 +412,22 @@ void build_force_map(const HostModel &m, GatherMap &g)
 static inline int packed(int ie, int je, int nd) { return ie * nd - ie * (ie - 1) / 2 + (je - ie); }
 
 // Tangent map. Element matrices are packed upper triangles, shells at
-// [p*E + e] (p < 171), trusses at 171E + [p*T + e] (p < 21). For a local pair
+// [p*E + e] (p < 171), trusses at 171E + [p*T + e] (p < 21), frames at
+// 171E + 21T + [p*F + e] (p < 105). For a local pair
 // (ie <= je) the global slot is (max(i,j), min(i,j)) of the lower band,
 // L[col*ld + (row-col)], and the value used is K[ie][je], as the reference
 // adds K[ie][je] for ie <= je into its skyline (truss.c:170-193,
-// shell.c:307-329). Lists are sorted by (slot, truss before shell, element).
+// frame.c:328-344, shell.c:307-329). Lists are sorted by (slot; truss,
+// frame, shell; element), the order stiff_tr, stiff_fr, stiff_sh add them.
 void build_tangent_map(const HostModel &m, long ld, GatherMap &g)
 {
-    const long E = m.ne_sh, T = m.ne_tr;
+    const long E = m.ne_sh, T = m.ne_tr, F = m.ne_fr;
     struct C {
         int64_t slot;
         int src;
     };
     std::vector<C> all;
-    all.reserve((size_t)(171 * E + 21 * T));
+    all.reserve((size_t)(171 * E + 21 * T + 105 * F));
     for (long e = 0; e < T; ++e) {
         long mc[6];
         for (int a = 0; a < 2; ++a)
@@ -263,6 +437,15 @@ void build_tangent_map(const HostModel &m, long ld, GatherMap &g)
                 if (!mc[ie] || !mc[je]) continue;
                 long r = std::max(mc[ie], mc[je]) - 1, c = std::min(mc[ie], mc[je]) - 1;
                 all.push_back({(int64_t)c * ld + (r - c), (int)(171 * E + packed(ie, je, 6) * T + e)});
+            }
+    }
+    for (long e = 0; e < F; ++e) {
+        const long *mc = &m.fr_mc[e * 14];
+        for (int je = 0; je < 14; ++je)
+            for (int ie = 0; ie <= je; ++ie) {
+                if (!mc[ie] || !mc[je]) continue;
+                long r = std::max(mc[ie], mc[je]) - 1, c = std::min(mc[ie], mc[je]) - 1;
+                all.push_back({(int64_t)c * ld + (r - c), (int)(171 * E + 21 * T + packed(ie, je, 14) * F + e)});
             }
     }
     for (long e = 0; e < E; ++e) {
@@ -276,7 +459,7 @@ void build_tangent_map(const HostModel &m, long ld, GatherMap &g)
                 all.push_back({(int64_t)c * ld + (r - c), (int)(packed(ie, je, 18) * E + e)});
             }
     }
-    // stable sort keeps (truss, then shell; element order) within a slot
+    // stable sort keeps (truss, frame, shell; element order) within a slot
     std::stable_sort(all.begin(), all.end(), [](const C &a, const C &b) { return a.slot < b.slot; });
     g.ptr.clear();
     g.src.clear();

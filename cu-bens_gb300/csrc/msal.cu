@@ -1,11 +1,10 @@
-// Resident model and the GPU-resident modified spherical arc-length driver.
+// Resident model setup, the driver steps shared with the Newmark driver, the
+// GPU-resident modified spherical arc-length driver and the C ABI.
 //
 // The host keeps the scalar control flow of main.c:2158-3141 (step-size
 // control, subdivision counters, acceptance); every vector and element
 // operation runs on the GPU, and the host reads one small scalar block back
-// per Newton iteration. State that the reference keeps as "converged" (x,
-// c, ef, deffarea, defllen) and "current/previous iteration" (x_temp, c_i,
-// c_ip, ef_i, ef_ip) arrays is kept in the same three roles on the device.
+// per Newton iteration.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -19,125 +18,11 @@
 
 #include "cubens_gb300.h"
 #include "internal.hpp"
-
-#define CB_CUDA(x)                                                                         \
-    do {                                                                                   \
-        cudaError_t e_ = (x);                                                              \
-        if (e_ != cudaSuccess)                                                             \
-            throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + \
-                                     " at " __FILE__ ":" + std::to_string(__LINE__));      \
-    } while (0)
-
-struct cb_status_error : std::runtime_error {
-    int code;
-    cb_status_error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
-};
-
-struct cb_model {
-    cb::HostModel h;
-    cb_options opt{};
-    std::string err;
-    cudaStream_t st = nullptr;
-    size_t bytes = 0;
-    size_t h2d_bytes = 0;
-    std::vector<void *> allocs;
-
-    // nodes and equations
-    double *x0 = nullptr, *x_c = nullptr, *x_t = nullptr;
-    int *eq_x = nullptr;
-    // global vectors (NEQ)
-    double *q = nullptr, *d = nullptr, *dp = nullptr, *dpp = nullptr, *ddq = nullptr, *ddr = nullptr,
-           *dd = nullptr, *dt = nullptr, *r = nullptr, *f = nullptr, *zero = nullptr, *ssd_o = nullptr;
-    double *fcur = nullptr, *fprev = nullptr;  // f_temp and f_ip
-    // elements
-    cb::DevShell sh;
-    cb::DevTruss tr;
-    double *fe = nullptr;   // element force contributions
-    void *kel = nullptr;    // element tangents
-    int *fmap_ptr = nullptr, *fmap_src = nullptr;
-    int *tmap_ptr = nullptr, *tmap_src = nullptr;
-    int64_t *tmap_dst = nullptr;
-    long tmap_n = 0;
-    cb::BandFactor bf;
-    cb::MsalScalars *sc = nullptr, *sc_h = nullptr;
-    double *partial = nullptr;
-
-    // host control state (main.c:2205-2230)
-    int phase = 0;  // 0 created, 1 first increment done
-    double lpf = 0, lpfp = 0, lpfpp = 0, beta = 0, psi = 1, dnormallow = 0, dnorm = 0, arc = 0, qq = 0;
-    double dkc = 0, lpfc = 0;
-    int errchk2 = 0, subcnt = 0, imagcnt = 0, negcnt = 0, itecnt = 0;
-
-    // timing
-    bool timing = false;
-    cb_timers tm{};
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-    cudaEvent_t marks[8] = {};
-
-    template <typename T>
-    T *alloc(size_t n)
-    {
-        void *p = nullptr;
-        size_t b = std::max<size_t>(1, n) * sizeof(T);
-        CB_CUDA(cudaMalloc(&p, b));
-        CB_CUDA(cudaMemsetAsync(p, 0, b, st));
-        allocs.push_back(p);
-        bytes += b;
-        return (T *)p;
-    }
-};
-
-namespace {
+#include "model.hpp"
 
 using cb::HostModel;
 
-template <typename T>
-void h2d(T *dst, const T *src, size_t n, cudaStream_t st)
-{
-    if (n) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
-}
-template <typename T>
-void d2h(T *dst, const T *src, size_t n, cudaStream_t st)
-{
-    if (n) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, st));
-}
-template <typename T>
-void d2d(T *dst, const T *src, size_t n, cudaStream_t st)
-{
-    if (n && dst != src) CB_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
-}
-
-// AoS (element-major, k fastest) <-> SoA (k-major) for per-element arrays
-std::vector<double> to_soa(const double *aos, long ne, int k)
-{
-    std::vector<double> s((size_t)ne * k);
-    for (long e = 0; e < ne; ++e)
-        for (int j = 0; j < k; ++j) s[(size_t)j * ne + e] = aos[(size_t)e * k + j];
-    return s;
-}
-void from_soa(const std::vector<double> &s, long ne, int k, double *aos)
-{
-    for (long e = 0; e < ne; ++e)
-        for (int j = 0; j < k; ++j) aos[(size_t)e * k + j] = s[(size_t)j * ne + e];
-}
-
-struct PhaseTimer {
-    cb_model *m;
-    double *acc;
-    PhaseTimer(cb_model *m_, double *acc_) : m(m_), acc(acc_)
-    {
-        if (m->timing) CB_CUDA(cudaEventRecord(m->ev[0], m->st));
-    }
-    ~PhaseTimer()
-    {
-        if (!m->timing) return;
-        cudaEventRecord(m->ev[1], m->st);
-        cudaEventSynchronize(m->ev[1]);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, m->ev[0], m->ev[1]);
-        *acc += ms;
-    }
-};
+namespace drv {
 
 void upload_model(cb_model *m)
 {
@@ -147,7 +32,7 @@ void upload_model(cb_model *m)
         m->h2d_bytes += n * sizeof(*src);
         ::h2d(dst, src, n, s);
     };
-    const long NJ = h.nj, N = h.neq, E = h.ne_sh, T = h.ne_tr;
+    const long NJ = h.nj, N = h.neq, E = h.ne_sh, T = h.ne_tr, F = h.ne_fr;
     m->x0 = m->alloc<double>(NJ * 3);
     m->x_c = m->alloc<double>(NJ * 3);
     m->x_t = m->alloc<double>(NJ * 3);
@@ -233,7 +118,45 @@ void upload_model(cb_model *m)
         d2d(t.len_c, t.len0, T, st);
         h2d(t.dir_c, dir0.data(), 3 * T, st);
     }
-    m->fe = m->alloc<double>(18 * E + 6 * T);
+    if (F > 0) {
+        cb::DevFrame &fr = m->fr;
+        fr.conn = m->alloc<int>(2 * F);
+        fr.eq = m->alloc<int>(14 * F);
+        fr.prop = m->alloc<double>(8 * F);
+        fr.aux = m->alloc<double>(3 * F);
+        fr.len0 = m->alloc<double>(F);
+        for (double **v : {&fr.c_c, &fr.c_ip, &fr.c_i}) *v = m->alloc<double>(9 * F);
+        for (double **v : {&fr.ef_c, &fr.ef_ip, &fr.ef_i}) *v = m->alloc<double>(14 * F);
+        for (double **v : {&fr.len_c, &fr.len_ip, &fr.len_i}) *v = m->alloc<double>(F);
+        m->fr_lref = m->alloc<double>(F);
+        std::vector<int> conn(2 * F), eq(14 * F);
+        std::vector<double> prop(8 * F), aux(3 * F);
+        for (long e = 0; e < F; ++e) {
+            conn[e] = h.fr_conn[e * 2];
+            conn[F + e] = h.fr_conn[e * 2 + 1];
+            for (int k = 0; k < 14; ++k) eq[k * F + e] = (int)h.fr_mc[e * 14 + k] - 1;
+            for (int k = 0; k < 8; ++k) prop[k * F + e] = h.fr_prop[e * 8 + k];
+            for (int k = 0; k < 3; ++k) aux[k * F + e] = h.fr_aux[e * 3 + k];
+        }
+        h2d(fr.conn, conn.data(), conn.size(), st);
+        h2d(fr.eq, eq.data(), eq.size(), st);
+        h2d(fr.prop, prop.data(), prop.size(), st);
+        h2d(fr.aux, aux.data(), aux.size(), st);
+        // initial triads and lengths (prop_fr, frame.c:130-160)
+        cb::launch_frame_geometry(fr, m->x0, fr.c_c, fr.len0, F, st);
+        CB_CUDA(cudaGetLastError());
+        d2d(fr.len_c, fr.len0, F, st);
+        d2d(m->fr_lref, fr.len0, F, st);
+    }
+    if (h.alg == 5) {
+        for (double **v : {&m->uc, &m->vc, &m->ac, &m->uc_i, &m->vc_i, &m->ac_i, &m->um, &m->vm, &m->am, &m->sm,
+                           &m->qtot, &m->dyn, &m->fp})
+            *v = m->alloc<double>(N);
+        m->me = m->alloc<double>(14 * F);
+        m->pin = m->alloc<double>(h.pin.size());
+        h2d(m->pin, h.pin.data(), h.pin.size(), st);
+    }
+    m->fe = m->alloc<double>(18 * E + 6 * T + 14 * F);
     // gather maps
     cb::GatherMap fm, tm;
     cb::build_force_map(h, fm);
@@ -252,8 +175,8 @@ void upload_model(cb_model *m)
     h2d(m->tmap_ptr, tm.ptr.data(), tm.ptr.size(), st);
     h2d(m->tmap_src, tm.src.data(), tm.src.size(), st);
     h2d(m->tmap_dst, tm.dst.data(), tm.dst.size(), st);
-    if (fp32) m->kel = m->alloc<float>(171 * E + 21 * T);
-    else m->kel = m->alloc<double>(171 * E + 21 * T);
+    if (fp32) m->kel = m->alloc<float>(171 * E + 21 * T + 105 * F);
+    else m->kel = m->alloc<double>(171 * E + 21 * T + 105 * F);
     m->sc = m->alloc<cb::MsalScalars>(1);
     m->partial = m->alloc<double>(16 * cb::kRedBlocks);
     CB_CUDA(cudaMallocHost(&m->sc_h, sizeof(cb::MsalScalars)));
@@ -281,19 +204,32 @@ void reset_to_converged(cb_model *m)
         d2d(m->tr.dir_i, m->tr.dir_c, 3 * T, st);
         d2d(m->tr.n_i, m->tr.n_c, T, st);
     }
+    const long F = m->h.ne_fr;
+    if (F) {
+        cb::DevFrame &fr = m->fr;
+        d2d(fr.c_i, fr.c_c, 9 * F, st);
+        d2d(fr.c_ip, fr.c_c, 9 * F, st);
+        d2d(fr.ef_i, fr.ef_c, 14 * F, st);
+        d2d(fr.ef_ip, fr.ef_c, 14 * F, st);
+        d2d(fr.len_i, fr.len_c, F, st);
+        d2d(fr.len_ip, fr.len_c, F, st);
+    }
 }
 
-// ip <- i after an iteration (main.c:2399-2428)
+// ip <- i after an iteration (main.c:2399-2428, 3712-3740)
 void advance_iteration(cb_model *m)
 {
     std::swap(m->sh.c_ip, m->sh.c_i);
     std::swap(m->sh.ef_ip, m->sh.ef_i);
+    std::swap(m->fr.c_ip, m->fr.c_i);
+    std::swap(m->fr.ef_ip, m->fr.ef_i);
+    std::swap(m->fr.len_ip, m->fr.len_i);
 }
 
 // converged <- i on acceptance (main.c:3060-3105); ip is left as it is.
 // latest_in_ip: the caller already advanced (ip <- i by pointer swap), so the
 // newest triads and element forces are in the ip buffers.
-void accept_state(cb_model *m, bool latest_in_ip = false)
+void accept_state(cb_model *m, bool latest_in_ip)
 {
     const long NJ = m->h.nj, E = m->h.ne_sh, T = m->h.ne_tr;
     cudaStream_t st = m->st;
@@ -308,42 +244,56 @@ void accept_state(cb_model *m, bool latest_in_ip = false)
         d2d(m->tr.dir_c, m->tr.dir_i, 3 * T, st);
         d2d(m->tr.n_c, m->tr.n_i, T, st);
     }
+    const long F = m->h.ne_fr;
+    if (F) {
+        cb::DevFrame &fr = m->fr;
+        d2d(fr.c_c, latest_in_ip ? fr.c_ip : fr.c_i, 9 * F, st);
+        d2d(fr.ef_c, latest_in_ip ? fr.ef_ip : fr.ef_i, 14 * F, st);
+        d2d(fr.len_c, latest_in_ip ? fr.len_ip : fr.len_i, F, st);
+    }
 }
 
-// updatc geometry + forces_tr + forces_sh + deterministic assembly into fout
+// updatc geometry + forces_tr + forces_fr + forces_sh + deterministic
+// assembly into fout
 void internal_force(cb_model *m, const double *dd_vec, double *fout)
 {
     PhaseTimer t(m, &m->tm.ms_force);
-    const long E = m->h.ne_sh, T = m->h.ne_tr;
+    const long E = m->h.ne_sh, T = m->h.ne_tr, F = m->h.ne_fr;
     if (T) cb::launch_truss_forces(m->tr, m->x_t, m->fe + 18 * E, T, m->st);
+    if (F) cb::launch_frame_forces(m->fr, m->x_t, dd_vec, m->fr_lref, m->fe + 18 * E + 6 * T, F, m->st);
     if (E) cb::launch_shell_forces(m->sh, m->x_t, dd_vec, m->fe, E, m->st);
     cb::launch_gather_f64(m->fmap_ptr, m->fmap_src, m->fe, fout, m->h.neq, m->st);
-    m->tm.launches += (T ? 1 : 0) + (E ? 1 : 0) + 1;
+    m->tm.launches += (T ? 1 : 0) + (F ? 1 : 0) + (E ? 1 : 0) + 1;
     m->tm.force_evals++;
 }
 
-// tangent of the converged state into the band (stiff_tr + stiff_sh)
-void assemble_tangent(cb_model *m)
+template <typename K>
+void assemble_tangent_t(cb_model *m, TangentState which)
+{
+    const long E = m->h.ne_sh, T = m->h.ne_tr, F = m->h.ne_fr;
+    cb::BandFactor &bf = m->bf;
+    K *k = (K *)m->kel;
+    if (E) cb::launch_shell_tangent<K>(m->sh, m->x_c, k, E, m->st);
+    if (T) cb::launch_truss_tangent<K>(m->tr, k + 171 * E, T, m->st);
+    if (F) {
+        const cb::DevFrame &fr = m->fr;
+        const bool conv = which == TangentState::converged;
+        cb::launch_frame_tangent<K>(fr, conv ? fr.c_c : fr.c_ip, conv ? fr.ef_c : fr.ef_ip,
+                                    conv ? fr.len_c : fr.len_ip, m->fr_lref, k + 171 * E + 21 * T, F, m->st);
+    }
+    cb::launch_gather_band<K>(m->tmap_ptr, m->tmap_src, m->tmap_dst, k, (K *)bf.band, m->tmap_n, m->st);
+    m->tm.launches += 1 + (E ? 1 : 0) + (T ? 1 : 0) + (F ? 1 : 0);
+}
+
+// tangent into the band (stiff_tr + stiff_fr + stiff_sh)
+void assemble_tangent(cb_model *m, TangentState which)
 {
     PhaseTimer t(m, &m->tm.ms_tangent);
-    const long E = m->h.ne_sh, T = m->h.ne_tr;
     cb::BandFactor &bf = m->bf;
     const size_t es = bf.fp32 ? 4 : 8;
     CB_CUDA(cudaMemsetAsync(bf.band, 0, es * (size_t)bf.ld * bf.nblk * bf.s, m->st));
-    if (bf.fp32) {
-        float *k = (float *)m->kel;
-        if (E) cb::launch_shell_tangent<float>(m->sh, m->x_c, k, E, m->st);
-        if (T) cb::launch_truss_tangent<float>(m->tr, k + 171 * E, T, m->st);
-        cb::launch_gather_band<float>(m->tmap_ptr, m->tmap_src, m->tmap_dst, k, (float *)bf.band, m->tmap_n,
-                                      m->st);
-    } else {
-        double *k = (double *)m->kel;
-        if (E) cb::launch_shell_tangent<double>(m->sh, m->x_c, k, E, m->st);
-        if (T) cb::launch_truss_tangent<double>(m->tr, k + 171 * E, T, m->st);
-        cb::launch_gather_band<double>(m->tmap_ptr, m->tmap_src, m->tmap_dst, k, (double *)bf.band,
-                                       m->tmap_n, m->st);
-    }
-    m->tm.launches += 1 + (E ? 1 : 0) + (T ? 1 : 0);
+    if (bf.fp32) assemble_tangent_t<float>(m, which);
+    else assemble_tangent_t<double>(m, which);
 }
 
 void factor(cb_model *m)
@@ -359,6 +309,42 @@ void solve(cb_model *m, const double *rhs, double *x)
     cb::band_solve(m->bf, rhs, x, m->st, m->opt.use_graphs != 0, &m->tm.launches);
     m->tm.solves++;
 }
+
+// Read the scalar block back (one synchronisation point).
+cb::MsalScalars &pull_scalars(cb_model *m)
+{
+    d2h(m->sc_h, m->sc, 1, m->st);
+    cb::GridBarrier bar{};
+    d2h(&bar, m->bf.bar, 1, m->st);
+    CB_CUDA(cudaStreamSynchronize(m->st));
+    if (bar.err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier of the solve timed out");
+    return *m->sc_h;
+}
+
+double device_dot(cb_model *m, const double *a, const double *b, bool diff)
+{
+    PhaseTimer t(m, &m->tm.ms_vector);
+    cb::launch_dot(a, b, m->partial, m->sc, 15, m->h.neq, m->st, diff);
+    m->tm.launches += 2;
+    double v = 0;
+    d2h(&v, &m->sc->dots[15], 1, m->st);
+    CB_CUDA(cudaStreamSynchronize(m->st));
+    return v;
+}
+
+double device_elem(cb_model *m, const double *v, long i)
+{
+    double x = 0;
+    d2h(&x, v + i, 1, m->st);
+    CB_CUDA(cudaStreamSynchronize(m->st));
+    return x;
+}
+
+}  // namespace drv
+
+namespace {
+
+using namespace drv;
 
 // Push the host-side scalars the device kernels read.
 void push_scalars(cb_model *m, double lam_t, double a, double intener1)
@@ -379,36 +365,6 @@ void push_scalars(cb_model *m, double lam_t, double a, double intener1)
     s.convchk = 1;
     s.test_err = 0;
     h2d(m->sc, m->sc_h, 1, m->st);
-}
-
-// Read the scalar block back (one synchronisation point).
-cb::MsalScalars &pull_scalars(cb_model *m)
-{
-    d2h(m->sc_h, m->sc, 1, m->st);
-    cb::GridBarrier bar{};
-    d2h(&bar, m->bf.bar, 1, m->st);
-    CB_CUDA(cudaStreamSynchronize(m->st));
-    if (bar.err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier of the solve timed out");
-    return *m->sc_h;
-}
-
-double device_dot(cb_model *m, const double *a, const double *b, bool diff = false)
-{
-    PhaseTimer t(m, &m->tm.ms_vector);
-    cb::launch_dot(a, b, m->partial, m->sc, 15, m->h.neq, m->st, diff);
-    m->tm.launches += 2;
-    double v = 0;
-    d2h(&v, &m->sc->dots[15], 1, m->st);
-    CB_CUDA(cudaStreamSynchronize(m->st));
-    return v;
-}
-
-double device_elem(cb_model *m, const double *v, long i)
-{
-    double x = 0;
-    d2h(&x, v + i, 1, m->st);
-    CB_CUDA(cudaStreamSynchronize(m->st));
-    return x;
 }
 
 double true_residual(cb_model *m, double lam, const double *fvec)
@@ -646,21 +602,6 @@ void msal_step(cb_model *m, cb_step *out)
     }
 }
 
-template <typename F>
-int guarded(cb_model *m, F &&fn)
-{
-    try {
-        fn();
-        return CB_OK;
-    } catch (const cb_status_error &e) {
-        m->err = e.what();
-        return e.code;
-    } catch (const std::exception &e) {
-        m->err = e.what();
-        return CB_ERR_CUDA;
-    }
-}
-
 }  // namespace
 
 extern "C" {
@@ -739,6 +680,9 @@ int cb_model_info(const cb_model *m, cb_info *info)
     info->dkdof = m->h.dkdof;
     info->device_bytes = m->bytes;
     info->h2d_bytes = m->h2d_bytes;
+    info->algflag = m->h.alg;
+    info->nsteps = m->h.nsteps;
+    info->dt = m->h.dt;
     return CB_OK;
 }
 
@@ -747,6 +691,7 @@ const char *cb_last_error(const cb_model *m) { return m ? m->err.c_str() : "null
 int cb_msal_begin(cb_model *m, cb_step *out)
 {
     if (!m || !out || !m->st) return CB_ERR_ARG;
+    if (m->h.alg != 3) return fail(m, CB_ERR_STATE, "cb_msal_begin needs an ALGFLAG 3 (MSAL) model");
     return guarded(m, [&] { msal_begin(m, out); });
 }
 

@@ -1,0 +1,377 @@
+// GPU-resident nonlinear Newmark driver (ALGFLAG 5) for frame models, and
+// the element-level C ABI of the frame kernels.
+//
+// The host keeps the scalar control flow of main.c:3305-3960: the time-step
+// loop, the load-factor loop inside a time step (lpf, dlpf, solmin, subcnt)
+// and the halving of the time increment (ddt, sub_dt, tsflag), including its
+// oddities. Every iteration is a full Newton iteration as in the reference:
+// the tangent is formed from the previous iteration's element state, the
+// lumped mass at the converged coordinates, Keff = K + a0 (1 - am)/(1 - af) M
+// is factored on the GPU and solved for the effective residual. The host
+// reads one small scalar block back per iteration.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cubens_gb300.h"
+#include "internal.hpp"
+#include "model.hpp"
+
+namespace {
+
+using namespace drv;
+
+struct NewmarkParams {
+    double alpham = 0, alphaf = 0, alpha = 0.25, delta = 0.5;
+};
+
+// main.c:3329-3343
+NewmarkParams newmark_params(const cb::HostModel &h)
+{
+    NewmarkParams p;
+    if (h.numopt == 1) {
+        p.alpham = (2 * h.spectrds - 1) / (h.spectrds + 1);
+        p.alphaf = h.spectrds / (h.spectrds + 1);
+    } else if (h.numopt == 2) {
+        p.alphaf = (1 - h.spectrds) / (1 + h.spectrds);
+    } else if (h.numopt == 3) {
+        p.alpham = (h.spectrds - 1) / (h.spectrds + 1);
+    }
+    p.alpha = std::pow(1 - p.alpham + p.alphaf, 2) / 4;
+    p.delta = 0.5 - p.alpham + p.alphaf;
+    return p;
+}
+
+void push_test_controls(cb_model *m)
+{
+    cb::MsalScalars &s = *m->sc_h;
+    std::memset(&s, 0, sizeof s);
+    s.toldisp = m->h.toldisp;
+    s.tolforc = m->h.tolforc;
+    s.tolener = m->h.tolener;
+    s.convchk = 1;
+    h2d(m->sc, m->sc_h, 1, m->st);
+}
+
+// initial state (main.c:3398-3447): zero displacements, forces, motion;
+// deformed lengths = undeformed; the frame lengths llength_temp = L0
+void newmark_begin(cb_model *m)
+{
+    const cb::HostModel &h = m->h;
+    const long N = h.neq, F = h.ne_fr, NJ = h.nj;
+    cudaStream_t st = m->st;
+    for (double *v : {m->d, m->f, m->uc, m->vc, m->ac, m->sm})
+        CB_CUDA(cudaMemsetAsync(v, 0, N * sizeof(double), st));
+    d2d(m->x_c, m->x0, NJ * 3, st);
+    if (F) {
+        cb::launch_frame_geometry(m->fr, m->x0, m->fr.c_c, m->fr.len_c, F, st);
+        CB_CUDA(cudaMemsetAsync(m->fr.ef_c, 0, 14 * F * sizeof(double), st));
+        d2d(m->fr_lref, m->fr.len0, F, st);
+    }
+    push_test_controls(m);
+    CB_CUDA(cudaStreamSynchronize(st));
+    m->nm_k = 0;
+    m->nm_ddt = 1;
+    m->nm_phase = 1;
+}
+
+// one Newton iteration of main.c:3543-3745; returns the scalar block
+cb::MsalScalars &newmark_iteration(cb_model *m, const NewmarkParams &p, long k, double sub_dt, double lpf,
+                                   int itecnt, double a0, double a2, double a3, double a6, double a7)
+{
+    const cb::HostModel &h = m->h;
+    const long N = h.neq, F = h.ne_fr;
+    cudaStream_t st = m->st;
+    // tangent of the previous iteration's state with llength_temp as it
+    // stands, then the mass at the converged coordinates, which rewrites
+    // llength_temp (mass_fr, frame.c:1339)
+    assemble_tangent(m, TangentState::previous_iteration);
+    {
+        PhaseTimer t(m, &m->tm.ms_tangent);
+        cb::launch_frame_mass(m->fr, m->x_c, m->fr_lref, m->me, F, st);
+        cb::launch_gather_f64(m->fmap_ptr, m->fmap_src, m->me, m->sm, N, st);
+        m->tm.launches += 2;
+    }
+    {
+        PhaseTimer t(m, &m->tm.ms_vector);
+        const int mode = itecnt > 0 ? 2 : (k == 0 ? 0 : 1);
+        const double *pin_k = m->pin + (size_t)k * N;
+        const double *pin_km1 = k > 0 ? m->pin + (size_t)(k - 1) * N : pin_k;
+        cb::launch_nm_reff(mode, sub_dt, lpf, p.alpham, p.alphaf, a2, a3, pin_km1, pin_k, m->fcur, m->sm, m->vc_i,
+                           m->ac_i, m->qtot, m->r, N, st);
+        const double c0 = a0 * (1 - p.alpham), den = 1 - p.alphaf;
+        if (m->bf.fp32) cb::launch_nm_keff<float>((float *)m->bf.band, m->bf.ld, m->sm, c0, den, N, st);
+        else cb::launch_nm_keff<double>((double *)m->bf.band, m->bf.ld, m->sm, c0, den, N, st);
+        m->tm.launches += 2;
+    }
+    factor(m);
+    solve(m, m->r, m->dd);
+    std::swap(m->fcur, m->fprev);  // f_ip = f_temp
+    {
+        PhaseTimer t(m, &m->tm.ms_vector);
+        cb::launch_nm_update(m->dd, itecnt > 0, m->dt, m->um, m->vm, m->am, m->uc_i, m->vc_i, m->ac_i, a0, a2, a3,
+                             a6, a7, m->eq_x, m->x_t, N, st);
+        m->tm.launches += 1;
+    }
+    internal_force(m, m->dd, m->fcur);
+    {
+        PhaseTimer t(m, &m->tm.ms_vector);
+        cb::launch_nm_test(m->dd, m->dt, m->fcur, m->fp, m->fprev, m->qtot, m->sm, m->ac_i, m->dyn, m->partial,
+                           m->sc, itecnt == 0, N, st);
+        m->tm.launches += 2;
+    }
+    return pull_scalars(m);
+}
+
+// one time step k of main.c:3449-3953
+void newmark_step(cb_model *m, cb_step *out)
+{
+    const cb::HostModel &h = m->h;
+    const long N = h.neq;
+    cudaStream_t st = m->st;
+    out->done = 0;
+    if (m->nm_k >= h.nsteps) {
+        out->done = 1;
+        out->lam = (double)(h.nsteps - 1) * h.dt;
+        out->iterations = 0;
+        out->attempts = 0;
+        out->residual = 0;
+        out->dk = 0;
+        return;
+    }
+    const long k = m->nm_k;
+    const NewmarkParams p = newmark_params(h);
+    const double dt = h.dt, lpfmax = h.lpfmax;
+    double ddt = m->nm_ddt;
+    double dt_temp = ddt * dt, sub_dt = ddt, tsflag = 0;
+    int convchk = 1, itecnt = 0, passes = 0;
+    double res_num = 0, res_den = 0;
+    do {
+        const double a0 = 1 / (p.alpha * std::pow(dt_temp, 2));
+        const double a2 = 1 / (p.alpha * dt_temp);
+        const double a3 = 1 / (2 * p.alpha) - 1;
+        const double a6 = (dt_temp) * (1 - p.delta);
+        const double a7 = p.delta * (dt_temp);
+        int solcnt = 0, subcnt = 0;
+        double lpf = h.lpf0, dlpf = h.dlpf0, dlpfp = dlpf;
+        do {
+            if (lpf > lpfmax) lpf = lpfmax;
+            d2d(m->fp, m->f, N, st);
+            d2d(m->dt, m->d, N, st);
+            d2d(m->fcur, m->f, N, st);
+            dlpfp = dlpf;
+            reset_to_converged(m);
+            d2d(m->um, m->uc, N, st);
+            d2d(m->uc_i, m->uc, N, st);
+            d2d(m->vm, m->vc, N, st);
+            d2d(m->vc_i, m->vc, N, st);
+            d2d(m->am, m->ac, N, st);
+            d2d(m->ac_i, m->ac, N, st);
+            ++passes;
+            itecnt = 0;
+            do {
+                cb::MsalScalars &s = newmark_iteration(m, p, k, sub_dt, lpf, itecnt, a0, a2, a3, a6, a7);
+                if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+                convchk = s.convchk;
+                res_num = s.dots[2];
+                res_den = s.dots[6];
+                advance_iteration(m);
+                itecnt++;
+            } while (convchk != 0 && itecnt <= h.itemax);
+            if (convchk != 0 && subcnt <= h.submax) {
+                if (lpf == lpfmax) break;            // main.c:3777-3782
+                else if (dlpfp == h.dlpfmin) break;  // main.c:3783-3787
+                dlpf = dlpfp / 2;
+                if (dlpf < h.dlpfmin) dlpf = h.dlpfmin;
+                lpf = lpf - dlpfp + dlpf;
+                subcnt++;
+                solcnt = 0;
+            } else if (subcnt > h.submax) {
+                break;
+            } else {
+                solcnt++;
+                subcnt = 0;
+                if (solcnt >= h.solmin) {
+                    dlpf *= 2;
+                    solcnt = 0;
+                }
+                lpf += dlpf;
+            }
+        } while (lpf <= lpfmax);
+        if (convchk != 0) {
+            // halve the time increment (main.c:3823-3843)
+            ddt = ddt / 2;
+            dt_temp = ddt * dt;
+            if (tsflag == 0) sub_dt = ddt;
+            else if (tsflag == 1) sub_dt = sub_dt - ddt;
+        } else {
+            // accept (main.c:3845-3917); the newest element state is in ip
+            d2d(m->d, m->dt, N, st);
+            d2d(m->f, m->fcur, N, st);
+            d2d(m->uc, m->uc_i, N, st);
+            d2d(m->vc, m->vc_i, N, st);
+            d2d(m->ac, m->ac_i, N, st);
+            accept_state(m, true);
+        }
+        if (ddt < 1) {
+            if (sub_dt <= 1) {
+                sub_dt = sub_dt + ddt;
+                tsflag = 1;
+            }
+            if (sub_dt > 1) {
+                ddt = ddt * 2;
+                tsflag = 2;
+            }
+        } else if (ddt == 1) {
+            tsflag = 2;
+        }
+    } while (ddt >= 0.0001 && tsflag != 2);
+    if (convchk != 0)
+        throw cb_status_error(CB_ERR_DIVERGED, "minimum time increment interval reached without convergence");
+    CB_CUDA(cudaStreamSynchronize(st));
+    m->nm_ddt = ddt;
+    out->lam = (double)k * dt;
+    out->iterations = itecnt;
+    out->attempts = passes;
+    out->residual = res_den > 0 ? std::sqrt(res_num / res_den) : 0.0;
+    out->dk = 0;
+    m->itecnt = itecnt;
+    m->nm_k = k + 1;
+    if (m->nm_k >= h.nsteps) m->nm_phase = 2;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cb_newmark_begin(cb_model *m)
+{
+    if (!m || !m->st) return CB_ERR_ARG;
+    if (m->h.alg != 5) {
+        m->err = "cb_newmark_begin needs an ALGFLAG 5 (nonlinear Newmark) model";
+        return CB_ERR_STATE;
+    }
+    return guarded(m, [&] { newmark_begin(m); });
+}
+
+int cb_newmark_step(cb_model *m, cb_step *out)
+{
+    if (!m || !out) return CB_ERR_ARG;
+    if (m->nm_phase == 0) {
+        m->err = "cb_newmark_begin has not completed";
+        return CB_ERR_STATE;
+    }
+    return guarded(m, [&] { newmark_step(m, out); });
+}
+
+int cb_newmark_state(const cb_model *m, double *u, double *v, double *a)
+{
+    if (!m || m->h.alg != 5) return CB_ERR_ARG;
+    cb_model *mm = const_cast<cb_model *>(m);
+    return guarded(mm, [&] {
+        const long N = m->h.neq;
+        if (u) d2h(u, m->uc, N, m->st);
+        if (v) d2h(v, m->vc, N, m->st);
+        if (a) d2h(a, m->ac, N, m->st);
+        CB_CUDA(cudaStreamSynchronize(m->st));
+    });
+}
+
+int cb_eval_frame_forces(cb_model *m, const double *x_temp, const double *dd, const double *c_ip,
+                         const double *ef_ip, const double *len_ip, const double *lref, double *c_i,
+                         double *len_i, double *ef_i, double *f)
+{
+    if (!m || !x_temp || !dd || !c_ip || !ef_ip || !len_ip || !lref || !f) return CB_ERR_ARG;
+    const long F = m->h.ne_fr, N = m->h.neq;
+    if (F == 0 || m->h.ne_tr || m->h.ne_sh) {
+        m->err = "cb_eval_frame_forces needs a frame-only model";
+        return CB_ERR_UNSUPPORTED;
+    }
+    return guarded(m, [&] {
+        cudaStream_t st = m->st;
+        cb::DevFrame &fr = m->fr;
+        h2d(m->x_t, x_temp, m->h.nj * 3, st);
+        h2d(m->dd, dd, N, st);
+        std::vector<double> cs = to_soa(c_ip, F, 9), es = to_soa(ef_ip, F, 14);
+        h2d(fr.c_ip, cs.data(), cs.size(), st);
+        h2d(fr.ef_ip, es.data(), es.size(), st);
+        h2d(fr.len_ip, len_ip, F, st);
+        h2d(m->fr_lref, lref, F, st);
+        internal_force(m, m->dd, m->fcur);
+        d2h(f, m->fcur, N, st);
+        std::vector<double> c(9 * F), e(14 * F), L(F);
+        d2h(c.data(), fr.c_i, 9 * F, st);
+        d2h(e.data(), fr.ef_i, 14 * F, st);
+        d2h(L.data(), fr.len_i, F, st);
+        CB_CUDA(cudaStreamSynchronize(st));
+        if (c_i) from_soa(c, F, 9, c_i);
+        if (ef_i) from_soa(e, F, 14, ef_i);
+        if (len_i) std::memcpy(len_i, L.data(), sizeof(double) * F);
+    });
+}
+
+int cb_eval_frame_tangent(cb_model *m, const double *c, const double *ef, const double *len, const double *lref,
+                          long *maxa, double *ss)
+{
+    if (!m || !c || !ef || !len || !lref || !ss) return CB_ERR_ARG;
+    const long F = m->h.ne_fr, N = m->h.neq;
+    if (F == 0 || m->h.ne_tr || m->h.ne_sh) {
+        m->err = "cb_eval_frame_tangent needs a frame-only model";
+        return CB_ERR_UNSUPPORTED;
+    }
+    return guarded(m, [&] {
+        cudaStream_t st = m->st;
+        cb::DevFrame &fr = m->fr;
+        std::vector<double> cs = to_soa(c, F, 9), es = to_soa(ef, F, 14);
+        h2d(fr.c_c, cs.data(), cs.size(), st);
+        h2d(fr.ef_c, es.data(), es.size(), st);
+        h2d(fr.len_c, len, F, st);
+        h2d(m->fr_lref, lref, F, st);
+        assemble_tangent(m, TangentState::converged);
+        cb::BandFactor &bf = m->bf;
+        const long npad = bf.nblk * bf.s;
+        std::vector<double> band((size_t)bf.ld * npad);
+        if (bf.fp32) {
+            std::vector<float> bfl((size_t)bf.ld * npad);
+            d2h(bfl.data(), (const float *)bf.band, bfl.size(), st);
+            CB_CUDA(cudaStreamSynchronize(st));
+            for (size_t i = 0; i < bfl.size(); ++i) band[i] = bfl[i];
+        } else {
+            d2h(band.data(), (const double *)bf.band, band.size(), st);
+            CB_CUDA(cudaStreamSynchronize(st));
+        }
+        if (maxa) std::memcpy(maxa, m->h.maxa.data(), sizeof(long) * (N + 1));
+        for (long j = 1; j <= N; ++j) {
+            long hgt = m->h.maxa[j] - m->h.maxa[j - 1] - 1;
+            for (long off = 0; off <= hgt; ++off) {
+                long i = j - off;
+                ss[m->h.maxa[j - 1] - 1 + off] = band[(size_t)(i - 1) * bf.ld + off];
+            }
+        }
+    });
+}
+
+int cb_eval_frame_mass(cb_model *m, const double *x, double *sm, double *len)
+{
+    if (!m || !x || !sm) return CB_ERR_ARG;
+    const long F = m->h.ne_fr, N = m->h.neq;
+    if (F == 0 || m->h.ne_tr || m->h.ne_sh) {
+        m->err = "cb_eval_frame_mass needs a frame-only model";
+        return CB_ERR_UNSUPPORTED;
+    }
+    return guarded(m, [&] {
+        cudaStream_t st = m->st;
+        h2d(m->x_t, x, m->h.nj * 3, st);
+        double *me = m->fe;  // frame-only: the contribution buffer holds 14 F entries
+        cb::launch_frame_mass(m->fr, m->x_t, m->fr_lref, me, F, st);
+        cb::launch_gather_f64(m->fmap_ptr, m->fmap_src, me, m->r, N, st);
+        d2h(sm, m->r, N, st);
+        if (len) d2h(len, m->fr_lref, F, st);
+        CB_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+}  // extern "C"

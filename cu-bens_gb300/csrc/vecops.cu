@@ -295,6 +295,143 @@ __global__ void axpy_kernel(const double *__restrict__ x, double alpha, double *
     if (i < n) y[i] += alpha * x[i];
 }
 
+// ---- nonlinear Newmark (main.c:3553-3588, 3639-3688; solve.c:203-210, 478-487) ----
+
+// Residual of main.c:3553-3588 and the effective right-hand side Reff of
+// solve.c:478-487 in one pass. mode 0: predictor of the first time step,
+// 1: predictor of a later step (HHT load interpolation), 2: corrector. The
+// reference passes uc_i, vc_i, ac_i as solve's "m" vectors, so Reff uses the
+// current iteration's velocity and acceleration.
+__global__ void nm_reff_kernel(int mode, double sub_dt, double lpf, double alpham, double alphaf, double a2,
+                               double a3, const double *__restrict__ pin_km1, const double *__restrict__ pin_k,
+                               const double *__restrict__ f_temp, const double *__restrict__ sm,
+                               const double *__restrict__ vc_i, const double *__restrict__ ac_i,
+                               double *__restrict__ qtot, double *__restrict__ reff, long n)
+{
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double f = f_temp[i], m = sm[i], v = vc_i[i], a = ac_i[i];
+    double r;
+    if (mode == 0) {
+        const double qt = pin_k[i] * sub_dt * lpf;
+        qtot[i] = qt;
+        r = qt - f;
+    } else if (mode == 1) {
+        const double pm = pin_km1[i];
+        const double qt = (pm + (pin_k[i] - pm) * (sub_dt)) * lpf;
+        qtot[i] = qt;
+        r = (qt - f) + alphaf / (1 - alphaf) * (pm - f);
+    } else {
+        r = f - qtot[i];
+        r = r + m * a - m * ((a2 * v + a3 * a) * (1 - alpham) - a * alpham) / (1 - alphaf);
+    }
+    reff[i] = r + m * ((1 - alpham) * (v * a2 + a * a3) - alpham * a) / (1 - alphaf);
+}
+
+// Keff = K + a0 (1 - alpha_m) / (1 - alpha_f) M on the band diagonal
+// (solve.c:203-210); c0 = a0 (1 - alpha_m), den = 1 - alpha_f.
+template <typename T>
+__global__ void nm_keff_kernel(T *__restrict__ band, long ld, const double *__restrict__ sm, double c0,
+                               double den, long n)
+{
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double add = c0 * sm[i] / den;
+    band[i * ld] = (T)((double)band[i * ld] + add);
+}
+
+// dd sign (correctors solve for -dd, main.c:3625-3631), d_temp += dd, the
+// Newmark kinematics of main.c:3634-3639 and x_temp += dd (updatc).
+__global__ void nm_update_kernel(double *__restrict__ dd, int neg, double *__restrict__ d_temp,
+                                 const double *__restrict__ um, const double *__restrict__ vm,
+                                 const double *__restrict__ am, double *__restrict__ uc_i,
+                                 double *__restrict__ vc_i, double *__restrict__ ac_i, double a0, double a2,
+                                 double a3, double a6, double a7, const int *__restrict__ eq_x,
+                                 double *__restrict__ x_t, long n)
+{
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x = dd[i];
+    if (neg) {
+        x = x * (-1);
+        dd[i] = x;
+    }
+    const double u = d_temp[i] + x;
+    d_temp[i] = u;
+    uc_i[i] = u;
+    const double acc = (u - um[i]) * a0 - a2 * vm[i] - a3 * am[i];
+    ac_i[i] = acc;
+    vc_i[i] = vm[i] + a6 * am[i] + a7 * acc;
+    const int xi = eq_x[i];
+    if (xi >= 0) x_t[xi] += x;
+}
+
+// dyn = qtot - M a (main.c:3684-3688) and the sums of the convergence test
+// with dyn as the external force: [0] dd.dd, [1] d.d, [2] |dyn - f|^2,
+// [3] |dyn - fp|^2, [4] dd.(dyn - f_ip), [5] dd.(dyn - fp) (intener1 of the
+// first iteration, main.c:3690-3696), [6] dyn.dyn
+__global__ void __launch_bounds__(kT) nm_test_dots_kernel(const double *__restrict__ dd,
+                                                          const double *__restrict__ dt,
+                                                          const double *__restrict__ f,
+                                                          const double *__restrict__ fp,
+                                                          const double *__restrict__ fip,
+                                                          const double *__restrict__ qtot,
+                                                          const double *__restrict__ sm,
+                                                          const double *__restrict__ ac_i,
+                                                          double *__restrict__ dyn, double *partial, long n)
+{
+    double acc[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) acc[k] = 0;
+    for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)kRedBlocks * kT) {
+        const double y = qtot[i] - sm[i] * ac_i[i];
+        dyn[i] = y;
+        const double x = dd[i], t = dt[i], r = y - f[i], rp = y - fp[i];
+        acc[0] += x * x;
+        acc[1] += t * t;
+        acc[2] += r * r;
+        acc[3] += rp * rp;
+        acc[4] += x * (y - fip[i]);
+        acc[5] += x * (y - fp[i]);
+        acc[6] += y * y;
+    }
+    block_partials<7>(acc, partial);
+}
+
+__global__ void nm_test_kernel(const double *partial, MsalScalars *sc, int first)
+{
+    __shared__ double d[7];
+    finalize_partials<7>(partial, d);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int k = 0; k < 7; ++k) sc->dots[k] = d[k];
+    if (first) sc->intener1 = d[5];
+    int conv = 0, err = 0;
+    if (sc->toldisp < 1) {
+        if (d[1] != 0) {
+            if (sqrt(d[0]) / sqrt(d[1]) > sc->toldisp) conv += 10;
+        } else {
+            err = 1;
+        }
+    }
+    if (!err && sc->tolforc < 1) {
+        if (d[3] != 0) {
+            if (sqrt(d[2]) / sqrt(d[3]) > sc->tolforc) conv += 100;
+        } else {
+            err = 1;
+        }
+    }
+    if (!err && sc->tolener < 1) {
+        if (sc->intener1 != 0) {
+            if (fabs(d[4] / sc->intener1) > sc->tolener) conv += 1000;
+        } else {
+            err = 1;
+        }
+    }
+    sc->convchk = conv;
+    sc->test_err = err;
+}
+
 inline unsigned nb(long n) { return (unsigned)((n + kT - 1) / kT); }
 
 }  // namespace
@@ -349,6 +486,35 @@ void launch_scale(const double *x, double alpha, double *y, long n, cudaStream_t
 void launch_axpy(const double *x, double alpha, double *y, long n, cudaStream_t st)
 {
     axpy_kernel<<<nb(n), kT, 0, st>>>(x, alpha, y, n);
+}
+
+void launch_nm_reff(int mode, double sub_dt, double lpf, double alpham, double alphaf, double a2, double a3,
+                    const double *pin_km1, const double *pin_k, const double *f_temp, const double *sm,
+                    const double *vc_i, const double *ac_i, double *qtot, double *reff, long n, cudaStream_t st)
+{
+    nm_reff_kernel<<<nb(n), kT, 0, st>>>(mode, sub_dt, lpf, alpham, alphaf, a2, a3, pin_km1, pin_k, f_temp, sm,
+                                         vc_i, ac_i, qtot, reff, n);
+}
+template <typename T>
+void launch_nm_keff(T *band, long ld, const double *sm, double c0, double den, long n, cudaStream_t st)
+{
+    nm_keff_kernel<T><<<nb(n), kT, 0, st>>>(band, ld, sm, c0, den, n);
+}
+template void launch_nm_keff<float>(float *, long, const double *, double, double, long, cudaStream_t);
+template void launch_nm_keff<double>(double *, long, const double *, double, double, long, cudaStream_t);
+void launch_nm_update(double *dd, int neg, double *d_temp, const double *um, const double *vm, const double *am,
+                      double *uc_i, double *vc_i, double *ac_i, double a0, double a2, double a3, double a6,
+                      double a7, const int *eq_x, double *x_t, long n, cudaStream_t st)
+{
+    nm_update_kernel<<<nb(n), kT, 0, st>>>(dd, neg, d_temp, um, vm, am, uc_i, vc_i, ac_i, a0, a2, a3, a6, a7,
+                                           eq_x, x_t, n);
+}
+void launch_nm_test(const double *dd, const double *dt, const double *f, const double *fp, const double *fip,
+                    const double *qtot, const double *sm, const double *ac_i, double *dyn, double *partial,
+                    MsalScalars *sc, int first, long n, cudaStream_t st)
+{
+    nm_test_dots_kernel<<<kRedBlocks, kT, 0, st>>>(dd, dt, f, fp, fip, qtot, sm, ac_i, dyn, partial, n);
+    nm_test_kernel<<<1, 7 * 32, 0, st>>>(partial, sc, first);
 }
 
 }  // namespace cb

@@ -43,7 +43,7 @@ class Info(C.Structure):
     _fields_ = [("nj", C.c_long), ("ne_tr", C.c_long), ("ne_fr", C.c_long), ("ne_sh", C.c_long),
                 ("neq", C.c_long), ("lss", C.c_long), ("bandwidth", C.c_long), ("block", C.c_long),
                 ("nblocks", C.c_long), ("dkdof", C.c_long), ("device_bytes", C.c_size_t),
-                ("h2d_bytes", C.c_size_t)]
+                ("h2d_bytes", C.c_size_t), ("algflag", C.c_int), ("nsteps", C.c_long), ("dt", C.c_double)]
 
 
 class Step(C.Structure):
@@ -93,6 +93,12 @@ def load(path: Path | None = None):
     L.cb_eval_tangent.argtypes = [vp, dp, dp, dp, dp, lp, dp]
     L.cb_factor_solve.argtypes = [vp, dp, dp, dp, ip]
     L.cb_solve_noalloc.argtypes = [vp, vp, vp]
+    L.cb_newmark_begin.argtypes = [vp]
+    L.cb_newmark_step.argtypes = [vp, C.POINTER(Step)]
+    L.cb_newmark_state.argtypes = [vp, dp, dp, dp]
+    L.cb_eval_frame_forces.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+    L.cb_eval_frame_tangent.argtypes = [vp, dp, dp, dp, dp, lp, dp]
+    L.cb_eval_frame_mass.argtypes = [vp, dp, dp, dp]
     _lib = L
     return L
 
@@ -137,7 +143,7 @@ class Model:
         L.cb_model_info(self.h, C.byref(inf))
         self.info = {k: getattr(inf, k) for k, _ in Info._fields_}
         self.neq = inf.neq
-        self.nj, self.ne_tr, self.ne_sh = inf.nj, inf.ne_tr, inf.ne_sh
+        self.nj, self.ne_tr, self.ne_fr, self.ne_sh = inf.nj, inf.ne_tr, inf.ne_fr, inf.ne_sh
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:
@@ -194,7 +200,56 @@ class Model:
         return dict(lam=np.array(lam), its=np.array(its), res=np.array(res),
                     d=np.array(ds) if with_d else None)
 
+    # ---- nonlinear Newmark (ALGFLAG 5) ----
+    def newmark_begin(self):
+        self._check(load().cb_newmark_begin(self.h))
+
+    def newmark_step(self) -> StepResult:
+        return self._step(load().cb_newmark_step)
+
+    def newmark_state(self):
+        u, v, a = np.zeros(self.neq), np.zeros(self.neq), np.zeros(self.neq)
+        self._check(load().cb_newmark_state(self.h, _d(u), _d(v), _d(a)))
+        return u, v, a
+
+    def run_newmark(self, steps: int, with_d: bool = True):
+        """The first ``steps`` time steps (k = 0 .. steps-1) from rest."""
+        t, its, res, att, ds = [], [], [], [], []
+        self.newmark_begin()
+        for _ in range(steps):
+            r = self.newmark_step()
+            if r.done:
+                break
+            t.append(r.lam)
+            its.append(r.iterations)
+            res.append(r.residual)
+            att.append(r.attempts)
+            if with_d:
+                ds.append(self.displacements()[0])
+        return dict(time=np.array(t), its=np.array(its), res=np.array(res), attempts=np.array(att),
+                    d=np.array(ds) if with_d else None)
+
     # ---- element-level entry points ----
+    def eval_frame_forces(self, x_temp, dd, c_ip, ef_ip, len_ip, lref):
+        F = self.ne_fr
+        c_i, len_i, ef_i, f = np.zeros(9 * F), np.zeros(F), np.zeros(14 * F), np.zeros(self.neq)
+        args = [_c64(v) for v in (x_temp, dd, c_ip, ef_ip, len_ip, lref)]
+        self._check(load().cb_eval_frame_forces(self.h, *[_d(a) for a in args], _d(c_i), _d(len_i), _d(ef_i),
+                                                _d(f)))
+        return c_i, len_i, ef_i, f
+
+    def eval_frame_tangent(self, c, ef, length, lref):
+        maxa = np.zeros(self.neq + 1, dtype=np.int64)
+        ss = np.zeros(self.info["lss"])
+        args = [_c64(v) for v in (c, ef, length, lref)]
+        self._check(load().cb_eval_frame_tangent(self.h, *[_d(a) for a in args],
+                                                 maxa.ctypes.data_as(C.POINTER(C.c_long)), _d(ss)))
+        return maxa, ss
+
+    def eval_frame_mass(self, x):
+        sm, L = np.zeros(self.neq), np.zeros(self.ne_fr)
+        self._check(load().cb_eval_frame_mass(self.h, _d(_c64(x)), _d(sm), _d(L)))
+        return sm, L
     def eval_forces(self, x_temp, dd, c_ip=None, ef_ip=None):
         E, T = self.ne_sh, self.ne_tr
         c_i, a_i, ef_i = np.zeros(9 * E), np.zeros(E), np.zeros(18 * E)

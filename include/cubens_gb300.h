@@ -5,8 +5,9 @@
  *
  *  1. Resident API (cb_*): the model, its state and the factorisation live in
  *     GPU memory; the host drives the modified spherical arc-length (MSAL)
- *     loop of main.c:2158-3141 one converged increment at a time. This is
- *     the fast path.
+ *     loop of main.c:2158-3141 one converged increment at a time, or the
+ *     nonlinear Newmark loop of main.c:3305-3960 one time step at a time.
+ *     This is the fast path.
  *
  *  2. Drop-in API: the prototypes.h entry points of the hot path with the
  *     reference's exact signatures (host pointers, sizes through the globals
@@ -66,16 +67,23 @@ typedef struct {
     long dkdof;                    /* 0-based DOF of the prescribed displacement */
     size_t device_bytes;           /* GPU memory held by the handle */
     size_t h2d_bytes;              /* bytes copied host -> device when the model was created */
+    int algflag;                   /* 3: MSAL model, 5: nonlinear Newmark model */
+    long nsteps;                   /* Newmark: time steps NTSTPS (main.c:3361) */
+    double dt;                     /* Newmark: time step */
 } cb_info;
 
-/* Result of one converged increment (what output() records, misc.c:402-417). */
+/* Result of one converged increment or time step (what output() records,
+ * misc.c:402-417). For Newmark steps lam is the time k dt, attempts the
+ * load-factor passes tried, residual |dyn - f| / |dyn| with dyn = qtot - M a,
+ * and dk 0. */
 typedef struct {
-    double lam;            /* load proportionality factor */
+    double lam;            /* load proportionality factor (Newmark: time) */
     int iterations;        /* itecnt at acceptance */
     int attempts;          /* increments tried (1 + arc-length cuts) */
     double residual;       /* |lam q - f| / |lam q| of the accepted state (FP64) */
     double dk;             /* displacement at the control DOF */
-    int done;              /* 1: |lam| > lpfmax or |d_k| > dkimax, no increment taken (main.c:2647) */
+    int done;              /* 1: |lam| > lpfmax or |d_k| > dkimax (main.c:2647), or the last
+                              time step was taken; no step was taken by this call */
 } cb_step;
 
 /* Per-kernel-class GPU time (ms, CUDA events on the handle's stream) and
@@ -90,10 +98,11 @@ typedef struct {
 
 int cb_default_options(cb_options *opt);
 
-/* Parse a model_def.txt text (ANAFLAG 2, ALGFLAG 3; truss and DKT shell
- * elements; SLVFLAG 0; OPTFLAG 1) and upload the model. Replaces the setup
- * part of main() (main.c:330-1648: struc, codes, skylin, prop_tr, prop_sh,
- * load, msal). */
+/* Parse a model_def.txt text and upload the model: ANAFLAG 2, SLVFLAG 0,
+ * OPTFLAG 1; ALGFLAG 3 (MSAL) with truss, frame and DKT shell elements, or
+ * ALGFLAG 5 (nonlinear Newmark) with frame elements. Replaces the setup part
+ * of main() (main.c:330-1648: struc, codes, skylin, prop_tr, prop_fr,
+ * prop_sh, load, msal). */
 int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb_model **out);
 int cb_model_destroy(cb_model *m);
 int cb_model_info(const cb_model *m, cb_info *info);
@@ -107,6 +116,16 @@ int cb_msal_begin(cb_model *m, cb_step *out);
 int cb_msal_step(cb_model *m, cb_step *out);
 /* Current converged displacements d (NEQ) and lambda. */
 int cb_get_displacements(const cb_model *m, double *d, double *lam);
+
+/* Nonlinear Newmark (ALGFLAG 5, frame models). cb_newmark_begin sets the
+ * initial state of main.c:3398-3447 (zero motion); each cb_newmark_step runs
+ * one time step k of main.c:3449-3953 (load-factor passes and time-increment
+ * halving included) and returns CB_OK with out->done = 1 once all NTSTPS
+ * steps are taken. cb_get_displacements then returns d; cb_newmark_state
+ * the displacement, velocity and acceleration (NEQ each; any may be NULL). */
+int cb_newmark_begin(cb_model *m);
+int cb_newmark_step(cb_model *m, cb_step *out);
+int cb_newmark_state(const cb_model *m, double *u, double *v, double *a);
 /* Reference load vector q (NEQ) and 1-based equation numbers jcode (NJ*7). */
 int cb_get_topology(const cb_model *m, long *jcode, double *q);
 
@@ -158,6 +177,25 @@ int cb_eval_forces(cb_model *m, const double *x_temp, const double *dd, const do
  * c_sh (NE_SH*9), area_sh (NE_SH), ef_tr (NE_TR*2). */
 int cb_eval_tangent(cb_model *m, const double *x, const double *c_sh, const double *area_sh,
                     const double *ef_tr, long *maxa, double *ss);
+
+/* Frame element entry points (frame-only models), arrays element-major:
+ *   cb_eval_frame_forces: forces_fr (frame.c:902-1312) with the frame part of
+ *     updatc (misc.c:108-147): x_temp (NJ*3), dd (NEQ), c_ip (NE_FR*9, rows
+ *     x^, y^, z^), ef_ip (NE_FR*14), len_ip and lref (NE_FR: deformed length
+ *     of the previous iteration, reference length) -> c_i, len_i, ef_i, and
+ *     f (NEQ, overwritten). Outputs other than f may be NULL.
+ *   cb_eval_frame_tangent: stiff_fr (frame.c:226-362) of the state (c, ef,
+ *     len, lref) into the reference's skyline layout (maxa, ss[lss]).
+ *   cb_eval_frame_mass: mass_fr (frame.c:1314-1391) lumped mass at the joint
+ *     coordinates x into sm (NEQ, overwritten); len (NE_FR, may be NULL) gets
+ *     the member lengths at x.
+ * They overwrite the handle's iteration state; call them between analyses. */
+int cb_eval_frame_forces(cb_model *m, const double *x_temp, const double *dd, const double *c_ip,
+                         const double *ef_ip, const double *len_ip, const double *lref, double *c_i,
+                         double *len_i, double *ef_i, double *f);
+int cb_eval_frame_tangent(cb_model *m, const double *c, const double *ef, const double *len,
+                          const double *lref, long *maxa, double *ss);
+int cb_eval_frame_mass(cb_model *m, const double *x, double *sm, double *len);
 
 /* Factor the tangent last assembled by cb_eval_tangent and solve K v = rhs
  * (skyfact/skysolve, solve.c:539-698). Outputs v (NEQ), the LDL^T pivots ssd

@@ -44,3 +44,35 @@ def test_parse_errors_need_no_gpu(lib):
     assert rc in (2, 4)
     assert lib.cb_last_error(h)
     lib.cb_model_destroy(h)
+
+
+def _create(lib, text: bytes):
+    opt = cubens.Options()
+    lib.cb_default_options(C.byref(opt))
+    h = C.c_void_p()
+    rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
+    msg = lib.cb_last_error(h).decode()
+    lib.cb_model_destroy(h)
+    return rc, msg
+
+
+def test_unsupported_frame_and_newmark_inputs_are_refused_before_upload(lib):
+    from cubens import models
+    spec = models.frame_building(1, 1, 1, steps=4)
+    lines = spec.text.splitlines()
+    # member end offsets (frame.c:85-108) are outside the GPU path
+    i = lines.index("0,0,0,0,0,0,0")
+    bad = "\n".join(lines[:i] + ["1,0.1,0,0,0,0,0", "0,0,0,0,0,0,0"] + lines[i + 1:]) + "\n"
+    rc, msg = _create(lib, bad.encode())
+    assert rc == 4 and "offsets" in msg
+    # prescribed support motion in a Newmark model
+    j = lines.index("0,0", 7 + spec.ne_fr) + 1  # the list after the constraints
+    bad = "\n".join(lines[:j] + ["2,1", "0,0"] + lines[j + 1:]) + "\n"
+    rc, msg = _create(lib, bad.encode())
+    assert rc == 4 and "prescribed" in msg
+    # a Newmark model with truss elements
+    truss = models.space_truss(bays=2).text.splitlines()
+    truss[1] = "5"
+    truss.insert(2, "0,0")
+    rc, msg = _create(lib, ("\n".join(truss) + "\n").encode())
+    assert rc == 4 and "frame-only" in msg
