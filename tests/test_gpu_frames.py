@@ -56,8 +56,8 @@ def test_frame_msal_path_matches_reference(golden_dir):
     z = np.load(golden_dir / "run_frame_msal.npz")
     steps = 16
     r = cubens.Model(str(z["model_def"])).run(steps)
-    np.testing.assert_array_equal(r["its"], z["iterations"])
-    assert _rel(r["lam"], z["lam"]) < 1e-6
+    np.testing.assert_array_equal(r["its"], z["iterations"][:steps])
+    assert _rel(r["lam"], z["lam"][:steps]) < 1e-6
     for k in range(steps):
         err = np.linalg.norm(r["d"][k] - z["d"][k]) / np.linalg.norm(z["d"][k])
         assert err < 1e-6, (k, err)
