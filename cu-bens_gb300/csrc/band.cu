@@ -11,9 +11,9 @@
 // rows; s (a multiple of 32, at least w = bw rounded up to 32) is the block
 // size of the solve.
 //
-// Factor: right-looking over 32-column panels, two launches per panel (the
-// 32x32 diagonal LDL^T in shared memory fused with the panel TRSM; then the
-// rank-32 update of the trailing band), replayed as a CUDA graph.
+// Factor: right-looking over 32-column panels in one persistent cooperative
+// kernel with bounded grid barriers between panels (factor_f32_kernel,
+// factor_f64_kernel); then the solve blocks below, replayed as a CUDA graph.
 //
 // Solve: with s >= bw, L is block lower-bidiagonal in s x s blocks and the
 // coupling block L_{i,i-1} has non-zeros only in its last w columns (L_{i+1,i}
@@ -64,128 +64,6 @@ __device__ __forceinline__ T lval(const T *band, long ld, long bw, long R, long 
 // -------------------------------------------------------------------------
 // Factor kernels
 // -------------------------------------------------------------------------
-
-// Panel p: every CTA (1024 threads, one per entry of the 32x32 diagonal
-// block) redundantly
-//   1. factors the diagonal block (LDL^T in shared memory, one elimination
-//      step per column) and
-//   2. inverts its unit-lower factor, Linv_pp = L_pp^-1 (one substitution
-//      step per column),
-// then takes up to kPanelRows of the panel rows r in [p+32, p+32+m), stages
-// them in shared memory and solves them as a small GEMM with no dependency
-// chain: W_r = A_r Linv_pp^T (= L_r D), L_rc = W_rc / d_c. W is kept for the
-// trailing update (wbuf, column-major in the panel column). CTA 0 writes 1/d,
-// the pivots, the flags and the factored diagonal block; the block goes to a
-// staging buffer because the other CTAs still read the unfactored one from
-// the band, and the trailing-update launch copies it into place.
-constexpr int kPanelThreads = 1024;
-constexpr int kPanelRows = 128;
-
-template <typename T>
-__global__ void __launch_bounds__(kPanelThreads) panel_kernel(T *band, long ld, long bw, long p, long m,
-                                                              T *dinv, double *ssd, int *flags, T *wbuf,
-                                                              long n, T *stage)
-{
-    __shared__ T a[NB][NB + 1];
-    __shared__ T x[NB][NB + 1];
-    __shared__ T ar[kPanelRows][NB + 1];
-    __shared__ T di[NB];
-    const int tid = threadIdx.x;
-    const int i = tid % NB, j = tid / NB;  // this thread's entry (i, j)
-    const long r_begin = (long)blockIdx.x * kPanelRows;
-    const long nrows = m - r_begin < kPanelRows ? m - r_begin : kPanelRows;
-    a[i][j] = (i >= j && i - j <= bw) ? band[(p + j) * ld + (i - j)] : T(0);
-    x[i][j] = (i == j) ? T(1) : T(0);
-    // stage this CTA's panel rows: ar[rr][k] = A(p+32+r_begin+rr, p+k)
-    for (int idx = tid; idx < kPanelRows * NB; idx += kPanelThreads) {
-        const int k = idx / kPanelRows, rr = idx % kPanelRows;
-        const long off = NB + r_begin + rr - k;
-        ar[rr][k] = (rr < nrows && off <= bw) ? band[(p + k) * ld + off] : T(0);
-    }
-    __syncthreads();
-    for (int k = 0; k < NB; ++k) {
-        const T d = a[k][k];
-        const bool live = i >= j && j >= k;
-        const T lik = (live && i > k) ? a[i][k] / d : T(0);
-        const T ljk = (live && j > k) ? a[j][k] / d : T(0);
-        __syncthreads();
-        if (live && j > k) a[i][j] -= lik * d * ljk;
-        if (j == k && i > k) a[i][k] = lik;
-        __syncthreads();
-    }
-    for (int k = 0; k < NB; ++k) {
-        if (i > k && j <= k) x[i][j] -= a[i][k] * x[k][j];
-        __syncthreads();
-    }
-    if (tid < NB) di[tid] = T(1) / a[tid][tid];
-    if (blockIdx.x == 0) {
-        stage[j * NB + i] = a[i][j];
-        if (tid < NB) {
-            const T dl = a[tid][tid];
-            dinv[p + tid] = T(1) / dl;
-            long g = p + tid;
-            if (g < n) {
-                ssd[g] = (double)dl;
-                if (!(dl > T(0))) atomicOr(&flags[0], 1);
-                if (dl == T(0)) atomicOr(&flags[1], 1);
-            }
-        }
-    }
-    __syncthreads();
-    for (int idx = tid; idx < kPanelRows * NB; idx += kPanelThreads) {
-        const int c = idx / kPanelRows, rr = idx % kPanelRows;
-        if (rr >= nrows) continue;
-        T acc = 0;
-#pragma unroll 8
-        for (int k = 0; k <= c; ++k) acc += ar[rr][k] * x[c][k];
-        const long row = r_begin + rr;
-        wbuf[c * m + row] = acc;
-        const long off = NB + row - c;
-        if (off <= bw) band[(p + c) * ld + off] = acc * di[c];
-    }
-}
-
-// Trailing update: A_rj -= sum_k W_rk L_jk over the panel, for the lower
-// triangle of rows/cols [p+32, p+32+m) (always inside the band since m <= bw);
-// CTA (0,0) also stores panel p's factored diagonal block from the stage.
-template <typename T, int TS>
-__global__ void __launch_bounds__(256) trailing_kernel(T *band, long ld, long bw, long p, long m, const T *wbuf,
-                                                       const T *dinv, const T *stage)
-{
-    int ti = blockIdx.y, tj = blockIdx.x;
-    if (tj > ti) return;
-    if (ti == 0 && tj == 0) {
-        // the factored 32x32 diagonal block of panel p, staged by panel_kernel
-        for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
-            int j = idx / NB, i = idx % NB;
-            if (i >= j && i - j <= bw) band[(p + j) * ld + (i - j)] = stage[idx];
-        }
-    }
-    __shared__ T wr[NB][TS + 1];
-    __shared__ T lc[NB][TS + 1];
-    const long base = p + NB;
-    const long r0 = (long)ti * TS, j0 = (long)tj * TS;
-    for (int idx = threadIdx.x; idx < NB * TS; idx += blockDim.x) {
-        int k = idx / TS, t = idx % TS;
-        long rr = r0 + t, jj = j0 + t;
-        wr[k][t] = rr < m ? wbuf[k * m + rr] : T(0);
-        lc[k][t] = jj < m ? wbuf[k * m + jj] * dinv[p + k] : T(0);
-    }
-    __syncthreads();
-    constexpr int PER = TS * TS / 256 > 0 ? TS * TS / 256 : 1;
-    for (int q = 0; q < PER; ++q) {
-        int idx = threadIdx.x + q * 256;
-        if (idx >= TS * TS) break;
-        int ri = idx / TS, ji = idx % TS;
-        long rr = r0 + ri, jj = j0 + ji;
-        if (rr >= m || jj >= m || jj > rr) continue;
-        T acc = 0;
-#pragma unroll 8
-        for (int k = 0; k < NB; ++k) acc += wr[k][ri] * lc[k][ji];
-        long col = base + jj;
-        band[col * ld + (rr - jj)] -= acc;
-    }
-}
 
 template <typename T>
 __global__ void pad_identity_kernel(T *band, long ld, long n, long npad)
@@ -349,34 +227,338 @@ __global__ void __launch_bounds__(256) rn_kernel(const T *band, long ld, long bw
 // -------------------------------------------------------------------------
 
 // Grid barrier for a cooperative launch. The wait is bounded: after 2^24
-// polls (well over a second) the CTA records a timeout in bar->err and goes
-// on, so a fault cannot hang the GPU; the host turns the flag into
-// CB_ERR_TIMEOUT.
-__device__ __forceinline__ void grid_barrier(GridBarrier *bar, unsigned nblocks)
+// polls (well over a second) the CTA records a timeout in bar->err; once the
+// flag is set no CTA waits any more. Returns false when the flag is set, and
+// the caller then leaves the kernel, so a fault cannot hang the GPU; the host
+// turns the flag into CB_ERR_TIMEOUT.
+__device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks)
 {
+    __shared__ int failed;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *vgen = &bar->gen;
-        unsigned gen = *vgen;
-        __threadfence();
-        unsigned arrived = atomicAdd(&bar->count, 1u) + 1u;
-        if (arrived == nblocks) {
-            bar->count = 0;
+        volatile int *verr = &bar->err;
+        failed = *verr;
+        if (!failed) {
+            volatile unsigned *vgen = &bar->gen;
+            unsigned gen = *vgen;
             __threadfence();
-            atomicAdd(&bar->gen, 1u);
-        } else {
-            unsigned long long polls = 0;
-            while (*vgen == gen) {
-                if (++polls > (1ull << 24)) {
-                    atomicExch(&bar->err, 1);
-                    break;
+            unsigned arrived = atomicAdd(&bar->count, 1u) + 1u;
+            if (arrived == nblocks) {
+                bar->count = 0;
+                __threadfence();
+                atomicAdd(&bar->gen, 1u);
+            } else {
+                unsigned long long polls = 0;
+                while (*vgen == gen) {
+                    if (*verr) {
+                        failed = 1;
+                        break;
+                    }
+                    if (++polls > (1ull << 24)) {
+                        atomicExch(&bar->err, 1);
+                        failed = 1;
+                        break;
+                    }
+                    __nanosleep(32);
                 }
-                __nanosleep(32);
             }
+            __threadfence();
         }
-        __threadfence();
     }
     __syncthreads();
+    return !failed;
+}
+
+// -------------------------------------------------------------------------
+// Persistent factorisation: one cooperative launch for the whole band
+// -------------------------------------------------------------------------
+
+template <typename T>
+struct FactorArgs {
+    T *band;
+    long ld, bw, npad, n;
+    T *dinv;
+    double *ssd;
+    int *flags;
+    T *wbuf;     // 32 * bw: W of the current panel (FP64) / staged L rows, two buffers (FP32)
+    T *dstage;   // 2 * 32 * 32: staged factored diagonal blocks (FP32)
+    GridBarrier *bar;
+};
+
+// Tile t of the lower triangle of an nt x nt tile grid: t = ti (ti + 1) / 2 + tj.
+__device__ __forceinline__ void tile_of(long t, long &ti, long &tj)
+{
+    ti = (long)((sqrt(8.0 * (double)t + 1.0) - 1.0) / 2.0);
+    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+    while (ti * (ti + 1) / 2 > t) --ti;
+    tj = t - ti * (ti + 1) / 2;
+}
+
+// 1, 1/d and the pivots of panel p, from the factored block A (D on the diagonal).
+template <typename T>
+__device__ __forceinline__ void record_pivots(const FactorArgs<T> &a, long p, T dl, T rd, int i)
+{
+    a.dinv[p + i] = rd;
+    const long g = p + i;
+    if (g < a.n) {
+        a.ssd[g] = (double)dl;
+        if (!(dl > T(0))) atomicOr(&a.flags[0], 1);
+        if (dl == T(0)) atomicOr(&a.flags[1], 1);
+    }
+}
+
+// LDL^T of a 32x32 block in shared memory and the inverse of its unit-lower
+// factor, by one warp in registers: lane i holds row i, l_jk and L_rk come by
+// shuffle, so the 32 dependent elimination steps cost no block-wide
+// synchronisation. On return A holds L below and D on the diagonal, Li the
+// inverse of the unit-lower L (row-major) and di = 1/D. A separate function
+// so that both loop nests unroll completely (the row stays in registers).
+template <typename T>
+__device__ __noinline__ void ldlt32_warp(T (*A)[NB + 1], T (*Li)[NB + 1], T *di)
+{
+    const int lane = threadIdx.x % 32;
+    T r[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) r[j] = A[lane][j];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+        const T d = __shfl_sync(0xffffffffu, r[k], k);
+        const T rd = T(1) / d;
+        const T l = lane > k ? r[k] * rd : T(0);
+        if (lane > k) r[k] = l;
+        const T ldk = l * d;
+#pragma unroll
+        for (int j = k + 1; j < NB; ++j) {
+            const T ljk = __shfl_sync(0xffffffffu, l, j);
+            if (j <= lane) r[j] -= ldk * ljk;
+        }
+    }
+    T x[NB];
+#pragma unroll
+    for (int rr = 0; rr < NB; ++rr) {
+        T acc = 0;
+#pragma unroll
+        for (int k = 0; k < rr; ++k) acc += __shfl_sync(0xffffffffu, r[k], rr) * x[k];
+        x[rr] = rr == lane ? T(1) : (rr < lane ? T(0) : -acc);
+    }
+    T dl = 0;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        A[lane][j] = j <= lane ? r[j] : T(0);
+        Li[j][lane] = x[j];
+        if (j == lane) dl = r[j];
+    }
+    di[lane] = T(1) / dl;
+}
+
+// FP32: one grid barrier per 32-column panel p (m = min(bw, npad - p - 32)).
+//   1. every CTA factors the diagonal block and inverts its unit-lower factor
+//      in the registers of warp 0 (ldlt32_warp);
+//   2. each CTA takes TS x TS tiles (ti, tj) of the trailing lower triangle,
+//      forms the panel rows it needs from the band, W = A Linv^T (= L D) for
+//      the tile's rows and L = W D^-1 for its columns, and applies
+//      A_rj -= sum_k W_rk L_jk. The owner of a diagonal tile stages its L
+//      rows, CTA 0 the factored diagonal block: other CTAs still read the
+//      panel's A values from the band during this phase;
+//   -- grid barrier --
+//   0. (next panel) all CTAs copy the staged L rows and block into the band.
+template <int TS>
+__global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
+{
+    using T = float;
+    __shared__ T A[NB][NB + 1];   // factored diagonal block: L below, D on the diagonal
+    __shared__ T Li[NB][NB + 1];  // Linv of the unit-lower L_pp
+    __shared__ T di[NB];
+    __shared__ T Ar[TS][NB + 1];  // raw panel rows of the tile's row block, then W
+    __shared__ T Ac[TS][NB + 1];  // raw panel rows of the tile's column block, then L
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    const long ld = a.ld, bw = a.bw;
+    long mprev = 0;
+    for (long p = 0; p <= a.npad; p += NB) {
+        // ---- 0. staged output of the previous panel into the band ----
+        if (p > 0) {
+            const long pp = p - NB;
+            const int buf = (int)((pp / NB) & 1);
+            const T *ls = a.wbuf + (long)buf * NB * bw;
+            const T *ds = a.dstage + buf * NB * NB;
+            const long total = NB * NB + NB * mprev;
+            for (long idx = blockIdx.x * 256L + tid; idx < total; idx += gridDim.x * 256L) {
+                if (idx < NB * NB) {
+                    const int j = (int)(idx / NB), i = (int)(idx % NB);
+                    if (i >= j && i - j <= bw) a.band[(pp + j) * ld + (i - j)] = ds[idx];
+                } else {
+                    const long q = idx - NB * NB;
+                    const int c = (int)(q / mprev);
+                    const long r = q % mprev;
+                    const long off = NB + r - c;
+                    if (off <= bw) a.band[(pp + c) * ld + off] = ls[c * mprev + r];
+                }
+            }
+        }
+        if (p == a.npad) break;
+        long m = a.npad - p - NB;
+        if (m > bw) m = bw;
+        if (m < 0) m = 0;
+        const int buf = (int)((p / NB) & 1);
+        // ---- 1. diagonal block: LDL^T and Linv by warp 0 in registers ----
+        for (int e = tid; e < NB * NB; e += 256) {
+            const int jj = e / NB, ii = e % NB;
+            A[ii][jj] = (ii >= jj && ii - jj <= bw) ? a.band[(p + jj) * ld + (ii - jj)] : T(0);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            ldlt32_warp<T>(A, Li, di);
+            if (blockIdx.x == 0) record_pivots(a, p, A[lane][lane], di[lane], lane);
+        }
+        __syncthreads();
+        if (blockIdx.x == 0) {
+            T *ds = a.dstage + buf * NB * NB;
+            for (int idx = tid; idx < NB * NB; idx += 256) ds[idx] = A[idx % NB][idx / NB];
+        }
+        // ---- 2. trailing tiles ----
+        T *ls = a.wbuf + (long)buf * NB * bw;
+        const long nt = (m + TS - 1) / TS;
+        const long ntiles = nt * (nt + 1) / 2;
+        for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            long ti, tj;
+            tile_of(t, ti, tj);
+            const long r0 = ti * TS, j0 = tj * TS;
+            // raw panel rows: X[q][k] = A(p+32+r0+q, p+k)
+            for (int idx = tid; idx < NB * TS; idx += 256) {
+                const int k = idx / TS, q = idx % TS;
+                const long o1 = NB + r0 + q - k, o2 = NB + j0 + q - k;
+                Ar[q][k] = (r0 + q < m && o1 <= bw) ? a.band[(p + k) * ld + o1] : T(0);
+                Ac[q][k] = (j0 + q < m && o2 <= bw) ? a.band[(p + k) * ld + o2] : T(0);
+            }
+            __syncthreads();
+            // W = X Linv^T for the row block, L = W D^-1 for the column block
+            T wv[TS * NB / 256], lv[TS * NB / 256];
+#pragma unroll
+            for (int u = 0; u < TS * NB / 256; ++u) {
+                const int idx = tid + 256 * u, c = idx / TS, q = idx % TS;
+                T w1 = 0, w2 = 0;
+                for (int k = 0; k <= c; ++k) {
+                    const T li = Li[c][k];
+                    w1 += Ar[q][k] * li;
+                    w2 += Ac[q][k] * li;
+                }
+                wv[u] = w1;
+                lv[u] = w2 * di[c];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < TS * NB / 256; ++u) {
+                const int idx = tid + 256 * u, c = idx / TS, q = idx % TS;
+                Ar[q][c] = wv[u];
+                Ac[q][c] = lv[u];
+                if (ti == tj && j0 + q < m) ls[c * m + j0 + q] = lv[u];
+            }
+            __syncthreads();
+            for (int idx = tid; idx < TS * TS; idx += 256) {
+                const int ji = idx / TS, ri = idx % TS;
+                const long rr = r0 + ri, jj = j0 + ji;
+                if (rr >= m || jj >= m || jj > rr) continue;
+                T acc = 0;
+#pragma unroll 8
+                for (int k = 0; k < NB; ++k) acc += Ar[ri][k] * Ac[ji][k];
+                a.band[(p + NB + jj) * ld + (rr - jj)] -= acc;
+            }
+            __syncthreads();
+        }
+        mprev = m;
+        if (!grid_barrier(a.bar, gridDim.x)) return;
+    }
+}
+
+// FP64 (the FP64 pipe is the bound): two grid barriers per panel.
+//   1. every CTA factors the diagonal block with all 256 threads (one
+//      elimination step per column, warp-uniform columns);
+//   2. one warp per panel row r forms W_r by forward substitution with the
+//      unit-lower L_pp (W_r L_pp^T = A_r), writes L_r = W_r D^-1 into the band
+//      and W_r into wbuf;
+//   -- grid barrier --
+//   3. CTA 0 writes the diagonal block and pivots; the CTAs share the TS x TS
+//      tiles of the trailing update from wbuf;
+//   -- grid barrier --
+template <int TS>
+__global__ void __launch_bounds__(256) factor_f64_kernel(FactorArgs<double> a)
+{
+    using T = double;
+    __shared__ T A[NB][NB + 1];
+    __shared__ T di[NB];
+    __shared__ T Wr[TS][NB + 1];
+    __shared__ T Lc[TS][NB + 1];
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    const long ld = a.ld, bw = a.bw;
+    const long gwarp = blockIdx.x * 8L + warp, nwarps = gridDim.x * 8L;
+    for (long p = 0; p < a.npad; p += NB) {
+        long m = a.npad - p - NB;
+        if (m > bw) m = bw;
+        if (m < 0) m = 0;
+        // ---- 1. diagonal block, all threads; entry e: column e / 32 (warp-uniform), row e % 32 ----
+        for (int e = tid; e < NB * NB; e += 256) {
+            const int j = e / NB, i = e % NB;
+            A[i][j] = (i >= j && i - j <= bw) ? a.band[(p + j) * ld + (i - j)] : T(0);
+        }
+        __syncthreads();
+        for (int k = 0; k < NB; ++k) {
+            const T d = A[k][k];
+            if (warp == 0 && lane > k) A[lane][k] = A[lane][k] / d;
+            __syncthreads();
+            for (int e = tid; e < NB * NB; e += 256) {
+                const int j = e / NB, i = e % NB;
+                if (j > k && j <= i) A[i][j] -= (A[i][k] * d) * A[j][k];
+            }
+            __syncthreads();
+        }
+        if (tid < NB) di[tid] = T(1) / A[tid][tid];
+        __syncthreads();
+        // ---- 2. panel rows by substitution, one warp per row ----
+        for (long r = gwarp; r < m; r += nwarps) {
+            const long off = NB + r - lane;
+            T w = off <= bw ? a.band[(p + lane) * ld + off] : T(0);
+            for (int k = 0; k < NB; ++k) {
+                const T wk = __shfl_sync(0xffffffffu, w, k);
+                if (lane > k) w -= wk * A[lane][k];
+            }
+            a.wbuf[lane * m + r] = w;
+            if (off <= bw) a.band[(p + lane) * ld + off] = w * di[lane];
+        }
+        if (!grid_barrier(a.bar, gridDim.x)) return;
+        // ---- 3. diagonal block out, trailing update ----
+        if (blockIdx.x == 0) {
+            for (int e = tid; e < NB * NB; e += 256) {
+                const int j = e / NB, i = e % NB;
+                if (i >= j && i - j <= bw) a.band[(p + j) * ld + (i - j)] = A[i][j];
+            }
+            if (tid < NB) record_pivots(a, p, A[tid][tid], di[tid], tid);
+        }
+        const long nt = (m + TS - 1) / TS;
+        const long ntiles = nt * (nt + 1) / 2;
+        for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            long ti, tj;
+            tile_of(t, ti, tj);
+            const long r0 = ti * TS, j0 = tj * TS;
+            for (int idx = tid; idx < NB * TS; idx += 256) {
+                const int k = idx / TS, q = idx % TS;
+                const long rr = r0 + q, jj = j0 + q;
+                Wr[q][k] = rr < m ? a.wbuf[k * m + rr] : T(0);
+                Lc[q][k] = jj < m ? a.wbuf[k * m + jj] * di[k] : T(0);
+            }
+            __syncthreads();
+            for (int idx = tid; idx < TS * TS; idx += 256) {
+                const int ji = idx / TS, ri = idx % TS;
+                const long rr = r0 + ri, jj = j0 + ji;
+                if (rr >= m || jj >= m || jj > rr) continue;
+                T acc = 0;
+#pragma unroll 8
+                for (int k = 0; k < NB; ++k) acc += Wr[ri][k] * Lc[ji][k];
+                a.band[(p + NB + jj) * ld + (rr - jj)] -= acc;
+            }
+            __syncthreads();
+        }
+        if (!grid_barrier(a.bar, gridDim.x)) return;
+    }
 }
 
 template <typename T>
@@ -424,13 +606,13 @@ __global__ void __launch_bounds__(256) solve_kernel(SolveArgs<T> a)
     const long nthr = gridDim.x * (long)blockDim.x;
     // A: y = blockdiag(Linv) b (b converted to T into w first)
     for (long g = gthr; g < npad; g += nthr) a.z[g] = g < a.n ? (T)a.rhs[g] : T(0);
-    grid_barrier(a.bar, gridDim.x);
+    if (!grid_barrier(a.bar, gridDim.x)) return;
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, r = row % s;
         T acc = warp_row_dot(a.linv + i * s * s + r * s, a.z + i * s, r + 1, lane);
         if (lane == 0) a.y[row] = acc;
     }
-    grid_barrier(a.bar, gridDim.x);
+    if (!grid_barrier(a.bar, gridDim.x)) return;
     // B: y_i -= Pn_i y_{i-1}[s-w:s]
     for (long i = 1; i < nb; ++i) {
         const T *yp = a.y + i * s - w;
@@ -438,17 +620,17 @@ __global__ void __launch_bounds__(256) solve_kernel(SolveArgs<T> a)
             T acc = warp_row_dot(a.pn + i * s * w + r * w, yp, w, lane);
             if (lane == 0) a.y[i * s + r] -= acc;
         }
-        grid_barrier(a.bar, gridDim.x);
+        if (!grid_barrier(a.bar, gridDim.x)) return;
     }
     // C: v = blockdiag(Linv^T) (y / D), warp per row of the stored transpose
     for (long g = gthr; g < npad; g += nthr) a.z[g] = a.y[g] * a.dinv[g];
-    grid_barrier(a.bar, gridDim.x);
+    if (!grid_barrier(a.bar, gridDim.x)) return;
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, c = row % s;
         T acc = warp_row_dot(a.linvt + i * s * s + c * s + c, a.z + i * s + c, s - c, lane);
         if (lane == 0) a.v[row] = acc;
     }
-    grid_barrier(a.bar, gridDim.x);
+    if (!grid_barrier(a.bar, gridDim.x)) return;
     // D: x_i -= Rn_i x_{i+1}[0:w]
     for (long i = nb - 2; i >= 0; --i) {
         const T *xn = a.v + (i + 1) * s;
@@ -456,7 +638,7 @@ __global__ void __launch_bounds__(256) solve_kernel(SolveArgs<T> a)
             T acc = warp_row_dot(a.rn + i * s * w + c * w, xn, w, lane);
             if (lane == 0) a.v[i * s + c] -= acc;
         }
-        grid_barrier(a.bar, gridDim.x);
+        if (!grid_barrier(a.bar, gridDim.x)) return;
     }
     for (long g = gthr; g < a.n; g += nthr) a.out[g] = (double)a.v[g];
 }
@@ -465,29 +647,36 @@ __global__ void __launch_bounds__(256) solve_kernel(SolveArgs<T> a)
 // Host sequences
 // -------------------------------------------------------------------------
 
+// The whole band LDL^T in one cooperative launch (plus the identity padding
+// and the flag reset).
 template <typename T>
-void factor_impl(BandFactor &f, cudaStream_t st, long *launches)
+void factor_band(BandFactor &f, cudaStream_t st, long *launches)
 {
+    constexpr int TS = sizeof(T) == 8 ? 16 : 32;
     T *band = (T *)f.band;
-    T *dinv = (T *)f.dinv;
-    T *wbuf = (T *)f.work;  // 32 * bw panel scratch (no solve is live during a factor)
     const long npad = f.nblk * f.s;
     if (npad > f.n) {
         pad_identity_kernel<T><<<(unsigned)((npad - f.n + 127) / 128), 128, 0, st>>>(band, f.ld, f.n, npad);
         ++*launches;
     }
     CB_CUDA(cudaMemsetAsync(f.flags, 0, 2 * sizeof(int), st));
-    for (long p = 0; p < npad; p += NB) {
-        long m = std::min(f.bw, npad - p - NB);
-        if (m < 0) m = 0;
-        unsigned nct = (unsigned)std::max(1L, (m + kPanelRows - 1) / kPanelRows);
-        panel_kernel<T><<<nct, kPanelThreads, 0, st>>>(band, f.ld, f.bw, p, m, dinv, f.ssd, f.flags, wbuf, f.n,
-                                                        (T *)f.stage);
-        constexpr int TS = sizeof(T) == 8 ? 16 : 32;
-        unsigned nt = (unsigned)std::max(1L, (m + TS - 1) / TS);
-        trailing_kernel<T, TS><<<dim3(nt, nt), 256, 0, st>>>(band, f.ld, f.bw, p, m, wbuf, dinv, (const T *)f.stage);
-        *launches += 2;
-    }
+    CB_CUDA(cudaMemsetAsync(f.fbar, 0, sizeof(GridBarrier), st));
+    const long nt = (f.bw + TS - 1) / TS;
+    const long ntiles = nt * (nt + 1) / 2;
+    const long need = std::max(ntiles, (f.bw + 7) / 8);
+    const int grid = (int)std::max(1L, std::min((long)f.factor_grid, need));
+    FactorArgs<T> a{band, f.ld, f.bw, npad, f.n, (T *)f.dinv, f.ssd, f.flags, (T *)f.work, (T *)f.stage, f.fbar};
+    void *args[] = {&a};
+    const void *fn = f.fp32 ? (const void *)factor_f32_kernel<32> : (const void *)factor_f64_kernel<16>;
+    CB_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(256), args, 0, st));
+    ++*launches;
+}
+
+// Solve blocks from the factored band: Linv_i, its transpose, Pn_i, Rn_i.
+template <typename T>
+void form_solve_blocks(BandFactor &f, cudaStream_t st, long *launches)
+{
+    T *band = (T *)f.band;
     const long nt = f.s / NB;
     const long kb = (f.bw + NB - 1) / NB + 1;
     inv_diag_kernel<T><<<dim3((unsigned)nt, (unsigned)f.nblk), 32, 0, st>>>(band, f.ld, f.bw, f.s, (T *)f.linv);
@@ -534,31 +723,22 @@ void solve_launch(const BandFactor &f, const double *rhs, double *x, void *work,
                                         args, 0, st));
 }
 
-template <typename T>
-int max_cooperative_grid()
+template <typename K>
+int max_cooperative_grid(K kernel)
 {
     int dev = 0, sms = 0, per = 0;
     CB_CUDA(cudaGetDevice(&dev));
     CB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, solve_kernel<T>, 256, 0));
+    CB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 256, 0));
     return std::max(1, sms * std::min(per, 4));
 }
 
 template <typename T>
 void profile_impl(BandFactor &f, int which, cudaStream_t st)
 {
-    long m = std::min(f.bw, f.nblk * f.s - NB);
-    if (m <= 0) return;
-    if (which == 3) {  // one trailing update of panel 0 (modifies the factor)
-        constexpr int TS = sizeof(T) == 8 ? 16 : 32;
-        unsigned nt = (unsigned)((m + TS - 1) / TS);
-        trailing_kernel<T, TS><<<dim3(nt, nt), 256, 0, st>>>((T *)f.band, f.ld, f.bw, 0, m, (const T *)f.work,
-                                                              (const T *)f.dinv, (const T *)f.stage);
-    } else if (which == 4) {  // one panel factor of panel 0 (modifies the factor)
-        unsigned nct = (unsigned)std::max(1L, (m + kPanelRows - 1) / kPanelRows);
-        panel_kernel<T><<<nct, kPanelThreads, 0, st>>>((T *)f.band, f.ld, f.bw, 0, m, (T *)f.dinv, f.ssd,
-                                                        f.flags, (T *)f.work, f.n, (T *)f.stage);
-    }
+    long dummy = 0;
+    if (which == 3) factor_band<T>(f, st, &dummy);             // the persistent LDL^T alone
+    else if (which == 4) form_solve_blocks<T>(f, st, &dummy);  // Linv, Pn, Rn from the factor
 }
 
 }  // namespace
@@ -611,18 +791,21 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32)
     CB_CUDA(cudaMalloc(&f.linvt, es * (size_t)f.nblk * f.s * f.s));
     CB_CUDA(cudaMalloc(&f.pmat, es * (size_t)f.nblk * f.s * f.w));
     CB_CUDA(cudaMalloc(&f.rmat, es * (size_t)f.nblk * f.s * f.w));
-    size_t work = std::max((size_t)3 * npad, (size_t)NB * f.bw + NB);
+    size_t work = std::max((size_t)3 * npad, (size_t)2 * NB * f.bw + NB);
     CB_CUDA(cudaMalloc(&f.work, es * work));
     CB_CUDA(cudaMalloc(&f.ssd, sizeof(double) * (size_t)n));
     CB_CUDA(cudaMalloc(&f.flags, 2 * sizeof(int)));
     CB_CUDA(cudaMalloc(&f.bar, sizeof(GridBarrier)));
-    CB_CUDA(cudaMalloc(&f.stage, es * NB * NB));
+    CB_CUDA(cudaMalloc(&f.stage, es * 2 * NB * NB));
     CB_CUDA(cudaMemset(f.linv, 0, es * (size_t)f.nblk * f.s * f.s));
     CB_CUDA(cudaMemset(f.linvt, 0, es * (size_t)f.nblk * f.s * f.s));
     CB_CUDA(cudaMemset(f.pmat, 0, es * (size_t)f.nblk * f.s * f.w));
     CB_CUDA(cudaMemset(f.rmat, 0, es * (size_t)f.nblk * f.s * f.w));
     CB_CUDA(cudaMemset(f.bar, 0, sizeof(GridBarrier)));
-    f.solve_grid = fp32 ? max_cooperative_grid<float>() : max_cooperative_grid<double>();
+    CB_CUDA(cudaMalloc(&f.fbar, sizeof(GridBarrier)));
+    CB_CUDA(cudaMemset(f.fbar, 0, sizeof(GridBarrier)));
+    f.solve_grid = fp32 ? max_cooperative_grid(solve_kernel<float>) : max_cooperative_grid(solve_kernel<double>);
+    f.factor_grid = fp32 ? max_cooperative_grid(factor_f32_kernel<32>) : max_cooperative_grid(factor_f64_kernel<16>);
     f.bytes = es * ((size_t)f.ld * npad + npad + (size_t)f.nblk * f.s * (2 * f.s + 2 * f.w) + work);
 }
 
@@ -630,7 +813,7 @@ void band_free(BandFactor &f)
 {
     if (f.factor_graph) cudaGraphExecDestroy(f.factor_graph);
     for (void *p : {f.band, f.dinv, f.linv, f.linvt, f.pmat, f.rmat, f.work, f.stage, (void *)f.ssd,
-                    (void *)f.flags, (void *)f.bar})
+                    (void *)f.flags, (void *)f.bar, (void *)f.fbar})
         if (p) cudaFree(p);
     f = BandFactor{};
 }
@@ -639,17 +822,19 @@ void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches)
 {
     long dummy = 0;
     long *cnt = launches ? launches : &dummy;
+    if (f.fp32) factor_band<float>(f, st, cnt);
+    else factor_band<double>(f, st, cnt);
     if (!use_graph) {
-        if (f.fp32) factor_impl<float>(f, st, cnt);
-        else factor_impl<double>(f, st, cnt);
+        if (f.fp32) form_solve_blocks<float>(f, st, cnt);
+        else form_solve_blocks<double>(f, st, cnt);
         return;
     }
     if (!f.factor_graph) {
         long per = 0;
         cudaGraph_t g;
         CB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        if (f.fp32) factor_impl<float>(f, st, &per);
-        else factor_impl<double>(f, st, &per);
+        if (f.fp32) form_solve_blocks<float>(f, st, &per);
+        else form_solve_blocks<double>(f, st, &per);
         CB_CUDA(cudaStreamEndCapture(st, &g));
         CB_CUDA(cudaGraphInstantiate(&f.factor_graph, g, 0));
         cudaGraphDestroy(g);

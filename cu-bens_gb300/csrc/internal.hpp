@@ -120,13 +120,15 @@ struct BandFactor {
     void *linvt = nullptr;       // nblk * s*s: its transpose (row-major)
     void *pmat = nullptr;        // nblk * s*w: Pn_i = Linv_i L_{i,i-1}[:, s-w:s] (row-major)
     void *rmat = nullptr;        // nblk * s*w: Rn_i = (L_{i+1,i}[0:w,:] Linv_i)^T (row-major)
-    void *work = nullptr;        // max(3*npad, 32*bw) work elements
+    void *work = nullptr;        // max(3*npad, 64*bw + 32) work elements
     double *ssd = nullptr;       // n pivots (FP64 copy)
     int *flags = nullptr;        // [0] det (any pivot <= 0), [1] zero pivot seen
     GridBarrier *bar = nullptr;  // persistent-solve barrier
-    void *stage = nullptr;       // 32x32 factored diagonal block handed from panel to trailing kernel
+    GridBarrier *fbar = nullptr; // persistent-factor barrier
+    void *stage = nullptr;       // 2 x 32x32: staged factored diagonal blocks (FP32 factor)
     bool fp32 = false;
     int solve_grid = 1;          // CTAs of the cooperative solve launch
+    int factor_grid = 1;         // most CTAs of the cooperative factor launch
     size_t bytes = 0;            // device memory held
     cudaGraphExec_t factor_graph = nullptr;
     long factor_launches = 0;
@@ -136,8 +138,8 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32);
 void band_free(BandFactor &f);
 // Factor the band in place: pivots to f.ssd, det/zero flags to f.flags.
 void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches);
-// One launch of a single band kernel for isolated timing: 3 = trailing update
-// of panel 0, 4 = fused panel factor of panel 0 (both modify the factor).
+// One launch sequence for isolated timing: 3 = the persistent LDL^T of the
+// band as it stands (overwrites it), 4 = the solve blocks from the factor.
 void band_profile_launch(BandFactor &f, int which, cudaStream_t st);
 // Bytes band_solve_with_work needs: 256 for the barrier + 3*npad work elements.
 size_t band_work_bytes(const BandFactor &f);

@@ -314,10 +314,12 @@ void solve(cb_model *m, const double *rhs, double *x)
 cb::MsalScalars &pull_scalars(cb_model *m)
 {
     d2h(m->sc_h, m->sc, 1, m->st);
-    cb::GridBarrier bar{};
-    d2h(&bar, m->bf.bar, 1, m->st);
+    cb::GridBarrier bar[2]{};
+    d2h(&bar[0], m->bf.bar, 1, m->st);
+    d2h(&bar[1], m->bf.fbar, 1, m->st);
     CB_CUDA(cudaStreamSynchronize(m->st));
-    if (bar.err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier of the solve timed out");
+    if (bar[0].err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier of the solve timed out");
+    if (bar[1].err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier of the factorisation timed out");
     return *m->sc_h;
 }
 
@@ -792,13 +794,16 @@ int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch, d
             case CB_K_SOLVE: cb::band_solve(m->bf, m->q, m->ddr, st, false, nullptr); break;
             case CB_K_SHELL_FORCE: cb::launch_shell_forces(m->sh, m->x_t, m->dd, m->fe, E, st); break;
             case CB_K_FACTOR: cb::band_factor(m->bf, st, m->opt.use_graphs != 0, nullptr); break;
-            case CB_K_TRAILING: cb::band_profile_launch(m->bf, 3, st); break;
-            case CB_K_PANEL: cb::band_profile_launch(m->bf, 4, st); break;
+            case CB_K_BAND_LDLT: cb::band_profile_launch(m->bf, 3, st); break;
+            case CB_K_SOLVE_BLOCKS: cb::band_profile_launch(m->bf, 4, st); break;
+            case CB_K_FRAME_FORCE:
+                cb::launch_frame_forces(m->fr, m->x_t, m->dd, m->fr_lref,
+                                        m->fe + 18 * E + 6 * m->h.ne_tr, m->h.ne_fr, st);
+                break;
             default: throw cb_status_error(CB_ERR_ARG, "unknown kernel id");
             }
         };
         const double w = (double)bf.w, n = (double)m->h.neq, b = (double)bf.bw;
-        const double mm = (double)std::min(bf.bw, bf.nblk * bf.s - 32);
         switch (which) {
         case CB_K_SOLVE:  // Linv lower halves twice, Pn and Rn once, vectors
             bytes = es * nb * (s * s + 2 * s * w) + 8.0 * 2 * n + es * 4 * nb * s;
@@ -815,13 +820,17 @@ int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch, d
             flops = 2 * (n * b * b / 2) + nb * 2 * (s * s * s / 6 + s * s * w);
             bytes = es * ((double)bf.ld * nb * s * 2 + nb * s * (s + 2 * w));
             break;
-        case CB_K_TRAILING:
-            flops = 2 * (mm * mm / 2) * 32;
-            bytes = es * (mm * mm / 2 * 2 + 2 * 32 * mm);
+        case CB_K_BAND_LDLT:  // n bw^2 / 2 FMA; the band read and written once from L2/HBM
+            flops = n * b * b;
+            bytes = es * (double)bf.ld * nb * s * 2;
             break;
-        case CB_K_PANEL:
-            flops = 2 * (32.0 * 32 * 32 / 6 + mm * 32 * 32 / 2);
-            bytes = es * (32.0 * 32 + 2 * mm * 32 * 2);
+        case CB_K_SOLVE_BLOCKS:
+            flops = nb * 2 * (s * s * s / 6 + s * s * w);
+            bytes = es * nb * s * (2 * s + 2 * w);
+            break;
+        case CB_K_FRAME_FORCE:  // per member ~500 B read, ~300 B written, ~1.2 kFLOP
+            bytes = (double)m->h.ne_fr * 800;
+            flops = (double)m->h.ne_fr * 1200;
             break;
         default: throw cb_status_error(CB_ERR_ARG, "unknown kernel id");
         }
@@ -949,7 +958,11 @@ int cb_factor_solve(cb_model *m, const double *rhs, double *v, double *ssd, int 
         if (ssd) d2h(ssd, m->bf.ssd, N, st);
         int fl[2] = {0, 0};
         d2h(fl, m->bf.flags, 2, st);
+        cb::GridBarrier bar[2]{};
+        d2h(&bar[0], m->bf.bar, 1, st);
+        d2h(&bar[1], m->bf.fbar, 1, st);
         CB_CUDA(cudaStreamSynchronize(st));
+        if (bar[0].err || bar[1].err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier timed out");
         if (det) *det = fl[0];
         if (fl[1]) throw cb_status_error(CB_ERR_NUMERIC, "zero pivot in the LDL^T factorisation");
     });

@@ -146,8 +146,9 @@ enum cb_kernel_id {
     CB_K_SOLVE = 0,        /* one solve: the persistent block-bidiagonal solve kernel */
     CB_K_SHELL_FORCE = 1,  /* the DKT internal-force kernel over all shell elements */
     CB_K_FACTOR = 2,       /* one whole band LDL^T + block inverses (graph replay) */
-    CB_K_TRAILING = 3,     /* one trailing rank-32 update of the band (modifies the factor) */
-    CB_K_PANEL = 4         /* one fused panel factor + TRSM (modifies the factor) */
+    CB_K_BAND_LDLT = 3,    /* the persistent band LDL^T kernel alone (refactors the band in place) */
+    CB_K_SOLVE_BLOCKS = 4, /* Linv, Pn, Rn of the solve from the current factor */
+    CB_K_FRAME_FORCE = 5   /* the frame internal-force kernel over all members */
 };
 /* Launch kernel `which` reps times back to back between two CUDA events and
  * report the mean milliseconds per launch and the algorithmic bytes and
