@@ -65,6 +65,14 @@ __device__ __forceinline__ T lval(const T *band, long ld, long bw, long R, long 
 // Factor kernels
 // -------------------------------------------------------------------------
 
+// 1/d from a band that already holds an LDL^T factor (D on the diagonal).
+template <typename T>
+__global__ void dinv_from_diag_kernel(const T *band, long ld, T *dinv, long npad)
+{
+    long j = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (j < npad) dinv[j] = T(1) / band[j * ld];
+}
+
 template <typename T>
 __global__ void pad_identity_kernel(T *band, long ld, long n, long npad)
 {
@@ -742,6 +750,27 @@ void profile_impl(BandFactor &f, int which, cudaStream_t st)
 }
 
 }  // namespace
+
+void band_use_factored(BandFactor &f, cudaStream_t st)
+{
+    const long npad = f.nblk * f.s;
+    const unsigned g = (unsigned)((npad + 255) / 256);
+    long dummy = 0;
+    if (f.fp32) {
+        if (npad > f.n)
+            pad_identity_kernel<float><<<(unsigned)((npad - f.n + 127) / 128), 128, 0, st>>>((float *)f.band, f.ld,
+                                                                                            f.n, npad);
+        dinv_from_diag_kernel<float><<<g, 256, 0, st>>>((const float *)f.band, f.ld, (float *)f.dinv, npad);
+        form_solve_blocks<float>(f, st, &dummy);
+    } else {
+        if (npad > f.n)
+            pad_identity_kernel<double><<<(unsigned)((npad - f.n + 127) / 128), 128, 0, st>>>((double *)f.band,
+                                                                                             f.ld, f.n, npad);
+        dinv_from_diag_kernel<double><<<g, 256, 0, st>>>((const double *)f.band, f.ld, (double *)f.dinv, npad);
+        form_solve_blocks<double>(f, st, &dummy);
+    }
+    CB_CUDA(cudaGetLastError());
+}
 
 size_t band_work_bytes(const BandFactor &f)
 {

@@ -25,6 +25,7 @@
 // triad products 4 x 2 x 9 FMA, kg entries ~ 150).
 #include <cuda_runtime.h>
 
+#include "frame.cuh"
 #include "internal.hpp"
 
 namespace cb {
@@ -32,37 +33,6 @@ namespace cb {
 namespace {
 
 constexpr int kFT = 128;
-
-__device__ __forceinline__ void cross_norm(const double *a, const double *b, double *c)
-{
-    c[0] = a[1] * b[2] - a[2] * b[1];
-    c[1] = a[2] * b[0] - a[0] * b[2];
-    c[2] = a[0] * b[1] - a[1] * b[0];
-    double l = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
-    c[0] /= l;
-    c[1] /= l;
-    c[2] /= l;
-}
-
-// rows x^, y^, z^ of c; x^ along the member, z^ = x^ x (aux - end 1)
-// normalised, y^ = z^ x x^ normalised
-__device__ __forceinline__ void frame_geometry(const double *pa, const double *pb, const double *aux,
-                                               double *c, double *len)
-{
-    double el[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
-    double L = sqrt(el[0] * el[0] + el[1] * el[1] + el[2] * el[2]);
-    double lx[3] = {el[0] / L, el[1] / L, el[2] / L};
-    double tmp[3] = {aux[0] - pa[0], aux[1] - pa[1], aux[2] - pa[2]};
-    double lz[3], ly[3];
-    cross_norm(lx, tmp, lz);
-    cross_norm(lz, lx, ly);
-    for (int m = 0; m < 3; ++m) {
-        c[m] = lx[m];
-        c[3 + m] = ly[m];
-        c[6 + m] = lz[m];
-    }
-    *len = L;
-}
 
 struct Section {
     double E, G, A, Iz, Iy, J, Iw;
@@ -208,19 +178,12 @@ __global__ void __launch_bounds__(kFT) frame_geometry_kernel(DevFrame fr, const 
     len[e] = L;
 }
 
-__global__ void __launch_bounds__(kFT) frame_forces_kernel(DevFrame fr, const double *__restrict__ x_t,
-                                                           const double *__restrict__ dd,
-                                                           const double *__restrict__ lref,
-                                                           double *__restrict__ fe, long F)
+// forces_fr for member e with the current triad ci given: ef_i, and the
+// element force in global axes T_i^T ef_i into fe.
+__device__ __forceinline__ void frame_force_member(const DevFrame &fr, long e, const double *ci,
+                                                   const double *__restrict__ dd, const double *__restrict__ lref,
+                                                   double *__restrict__ fe, long F)
 {
-    long e = blockIdx.x * (long)kFT + threadIdx.x;
-    if (e >= F) return;
-    const int na = fr.conn[e], nb = fr.conn[F + e];
-    double pa[3] = {x_t[na * 3], x_t[na * 3 + 1], x_t[na * 3 + 2]};
-    double pb[3] = {x_t[nb * 3], x_t[nb * 3 + 1], x_t[nb * 3 + 2]};
-    double aux[3] = {fr.aux[e], fr.aux[F + e], fr.aux[2 * F + e]};
-    double ci[9], Li;
-    frame_geometry(pa, pb, aux, ci, &Li);
     double cp[9], efp[14], DD[14];
     for (int k = 0; k < 9; ++k) cp[k] = fr.c_ip[k * F + e];
     for (int k = 0; k < 14; ++k) {
@@ -284,8 +247,37 @@ __global__ void __launch_bounds__(kFT) frame_forces_kernel(DevFrame fr, const do
         fe[(long)i * F + e] = v;
         fr.ef_i[(long)i * F + e] = efi[i];
     }
+}
+
+__global__ void __launch_bounds__(kFT) frame_forces_kernel(DevFrame fr, const double *__restrict__ x_t,
+                                                           const double *__restrict__ dd,
+                                                           const double *__restrict__ lref,
+                                                           double *__restrict__ fe, long F)
+{
+    long e = blockIdx.x * (long)kFT + threadIdx.x;
+    if (e >= F) return;
+    const int na = fr.conn[e], nb = fr.conn[F + e];
+    double pa[3] = {x_t[na * 3], x_t[na * 3 + 1], x_t[na * 3 + 2]};
+    double pb[3] = {x_t[nb * 3], x_t[nb * 3 + 1], x_t[nb * 3 + 2]};
+    double aux[3] = {fr.aux[e], fr.aux[F + e], fr.aux[2 * F + e]};
+    double ci[9], Li;
+    frame_geometry(pa, pb, aux, ci, &Li);
+    frame_force_member(fr, e, ci, dd, lref, fe, F);
     for (int q = 0; q < 9; ++q) fr.c_i[q * F + e] = ci[q];
     fr.len_i[e] = Li;
+}
+
+// The same with the current triads given (c_i[q*F + e], as updatc formed them).
+__global__ void __launch_bounds__(kFT) frame_forces_triads_kernel(DevFrame fr, const double *__restrict__ c_i,
+                                                                  const double *__restrict__ dd,
+                                                                  const double *__restrict__ lref,
+                                                                  double *__restrict__ fe, long F)
+{
+    long e = blockIdx.x * (long)kFT + threadIdx.x;
+    if (e >= F) return;
+    double ci[9];
+    for (int q = 0; q < 9; ++q) ci[q] = c_i[q * F + e];
+    frame_force_member(fr, e, ci, dd, lref, fe, F);
 }
 
 // Tangent from the state (c, ef, len) with reference lengths lref; writes
@@ -357,6 +349,12 @@ void launch_frame_forces(const DevFrame &fr, const double *x_t, const double *dd
                          long F, cudaStream_t st)
 {
     if (F) frame_forces_kernel<<<nblk(F), kFT, 0, st>>>(fr, x_t, dd, lref, fe, F);
+}
+
+void launch_frame_forces_given_triads(const DevFrame &fr, const double *c_i, const double *dd, const double *lref,
+                                      double *fe, long F, cudaStream_t st)
+{
+    if (F) frame_forces_triads_kernel<<<nblk(F), kFT, 0, st>>>(fr, c_i, dd, lref, fe, F);
 }
 
 template <typename T>

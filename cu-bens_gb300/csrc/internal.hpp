@@ -136,6 +136,9 @@ struct BandFactor {
 
 void band_alloc(BandFactor &f, long n, long bw, bool fp32);
 void band_free(BandFactor &f);
+// The band already holds an LDL^T factor (L below, D on the diagonal): form
+// 1/d and the solve blocks so that band_solve can use it.
+void band_use_factored(BandFactor &f, cudaStream_t st);
 // Factor the band in place: pivots to f.ssd, det/zero flags to f.flags.
 void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches);
 // One launch sequence for isolated timing: 3 = the persistent LDL^T of the
@@ -169,6 +172,9 @@ void launch_frame_geometry(const DevFrame &fr, const double *x, double *c, doubl
 // forces fe[k*F + e]; lref are the lengths the elastic stiffness uses
 void launch_frame_forces(const DevFrame &fr, const double *x_t, const double *dd, const double *lref,
                          double *fe, long F, cudaStream_t st);
+// the same with the current triads c_i[q*F + e] given instead of formed from x_t
+void launch_frame_forces_given_triads(const DevFrame &fr, const double *c_i, const double *dd, const double *lref,
+                                      double *fe, long F, cudaStream_t st);
 template <typename T>
 void launch_frame_tangent(const DevFrame &fr, const double *c, const double *ef, const double *len,
                           const double *lref, T *kel, long F, cudaStream_t st);

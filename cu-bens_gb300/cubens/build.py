@@ -1,8 +1,10 @@
-"""Build the CUDA library libcubens_gb300.so in-tree with nvcc for sm_103a.
+"""Build the CUDA libraries in-tree with nvcc for sm_103a.
 
-Every translation unit under csrc/ is compiled in parallel, then linked into
-one shared library exporting the C ABI of include/cubens_gb300.h (and the
-drop-in symbols of include/cubens_gb300_dropin.h).
+Every translation unit under csrc/ is compiled in parallel. All but
+dropin.cu are linked into libcubens_gb300.so, which exports the C ABI of
+include/cubens_gb300.h; dropin.cu becomes libcubens_dropin.so (the
+prototypes.h entry points of include/cubens_gb300_dropin.h), linked against
+the first with an $ORIGIN run path.
 """
 from __future__ import annotations
 
@@ -18,6 +20,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "lib" / "libcubens_gb300.so"
+DROPIN_LIB = PKG / "lib" / "libcubens_dropin.so"
+DROPIN_SRC = "dropin.cu"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
@@ -69,8 +73,14 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
             for err in ex.map(run, jobs):
                 if verbose and err:
                     print(err)
-    if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
+    main_objs = [o for o in objs if o.name != DROPIN_SRC + ".o"]
+    dropin_objs = [o for o in objs if o.name == DROPIN_SRC + ".o"]
+    if force or jobs or _stale(LIB, main_objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, main_objs)]
+        run(cmd)
+    if dropin_objs and (force or jobs or _stale(DROPIN_LIB, [*dropin_objs, LIB])):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(DROPIN_LIB), *map(str, dropin_objs), "-L", str(LIB.parent),
+               "-lcubens_gb300", "-Xlinker", "-rpath,$ORIGIN"]
         run(cmd)
     return LIB
 

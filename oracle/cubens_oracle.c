@@ -1166,6 +1166,12 @@ void orc_frame_forces(const orc_model *m, const double *x_temp, const double *dd
     }
 }
 
+void orc_shell_geometry0(const orc_model *m, double *xl, double *slen)
+{
+    memcpy(xl, m->sh_xl, sizeof(double) * 3 * (size_t)m->ne_sh);
+    memcpy(slen, m->sh_slen0, sizeof(double) * 3 * (size_t)m->ne_sh);
+}
+
 void orc_frame_mcode(const orc_model *m, long *mc)
 {
     memcpy(mc, m->fr_mc, sizeof(long) * 14 * (size_t)m->ne_fr);

@@ -107,6 +107,8 @@ void orc_skyline_solve(const orc_model *m, double *ss, double *rhs, double *ssd,
 
 /* Initial shell geometry from prop_sh (shell.c:43-108): c (NE_SH*9), area (NE_SH) */
 void orc_shell_initial(const orc_model *m, double *c, double *area);
+/* ... and the local coordinates xlocal (NE_SH*3) and side lengths slength (NE_SH*3) */
+void orc_shell_geometry0(const orc_model *m, double *xl, double *slen);
 
 /* Quadratic root selection of the arc-length constraint (arc.c:70-157). */
 int orc_quad(long neq, double a, double b, double c, double *dt, const double *dp,

@@ -54,6 +54,12 @@ def lib():
         L.orc_tangent_fr.argtypes = [P, dp, dp, dp, dp, lp, dp]
         L.orc_frame_mass.argtypes = [P, dp, dp]
         L.orc_frame_mcode.argtypes = [P, lp]
+        L.orc_shell_geometry0.argtypes = [P, dp, dp]
+        L.orc_quad.restype = C.c_int
+        L.orc_quad.argtypes = [C.c_long, C.c_double, C.c_double, C.c_double, dp, dp, dp, dp, dp, dp, dp]
+        L.orc_test.restype = C.c_int
+        L.orc_test.argtypes = [C.c_long, dp, dp, dp, dp, dp, dp, C.c_double, ip, C.c_double, C.c_double,
+                               C.c_double]
         _lib = L
     return _lib
 
@@ -163,6 +169,12 @@ class OracleModel:
         lib().orc_frame_mass(self.h, _d(np.ascontiguousarray(x, dtype=np.float64)), _d(sm))
         return sm
 
+    def shell_geometry0(self):
+        xl = np.zeros(self.ne_sh * 3)
+        sl = np.zeros(self.ne_sh * 3)
+        lib().orc_shell_geometry0(self.h, _d(xl), _d(sl))
+        return xl, sl
+
     def shell_initial(self):
         c = np.zeros(self.ne_sh * 9)
         a = np.zeros(self.ne_sh)
@@ -201,6 +213,26 @@ class OracleModel:
         det = np.zeros(1, dtype=np.int32)
         lib().orc_skyline_solve(self.h, _d(ss), _d(v), _d(ssd), _i(det), fact)
         return v, ssd, int(det[0]), ss
+
+
+def quad(a, b, c, dt, dp, ddr, ddq):
+    """arc.c quad on copies: returns (status, dt, dd, dlpf, lpft increment)."""
+    dt = np.array(dt, dtype=np.float64)
+    dd = np.zeros_like(dt)
+    dl = np.zeros(1)
+    lp = np.zeros(1)
+    rc = lib().orc_quad(len(dt), a, b, c, _d(dt), _d(np.ascontiguousarray(dp, dtype=np.float64)),
+                        _d(np.ascontiguousarray(ddr, dtype=np.float64)),
+                        _d(np.ascontiguousarray(ddq, dtype=np.float64)), _d(dd), _d(dl), _d(lp))
+    return rc, dt, dd, float(dl[0]), float(lp[0])
+
+
+def test_criteria(d_temp, dd, f_temp, fp, qtot, f_ip, intener1, toldisp, tolforc, tolener):
+    """misc.c test: returns (status, convchk)."""
+    cc = np.zeros(1, dtype=np.int32)
+    args = [np.ascontiguousarray(v, dtype=np.float64) for v in (d_temp, dd, f_temp, fp, qtot, f_ip)]
+    rc = lib().orc_test(len(args[0]), *[_d(v) for v in args], intener1, _i(cc), toldisp, tolforc, tolener)
+    return rc, int(cc[0])
 
 
 def skyline_to_dense(maxa, ss, neq):

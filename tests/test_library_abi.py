@@ -11,9 +11,9 @@ import cubens
 ROOT = Path(__file__).resolve().parents[1]
 
 
-def declared_functions():
+def declared_functions(header: str = "cubens_gb300.h"):
     names = []
-    for h in sorted((ROOT / "include").glob("*.h")):
+    for h in [ROOT / "include" / header]:
         text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
         names += re.findall(r"\b([a-z_][a-z0-9_]*)\s*\([^;{]*\)\s*;", text)
     return sorted(set(n for n in names if n not in ("if", "while", "for", "sizeof", "return")))
@@ -32,6 +32,15 @@ def test_headers_declare_functions():
 
 def test_every_declared_symbol_is_exported(lib):
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_dropin_library_exports_the_prototypes_symbols():
+    from dropin import loader
+    _, d = loader.load()
+    names = declared_functions("cubens_gb300_dropin.h")
+    assert {"forces_sh", "stiff_sh", "forces_fr", "updatc", "solve", "skyfact", "quad", "test"} <= set(names)
+    missing = [n for n in names if not hasattr(d, n)]
     assert not missing, missing
 
 
