@@ -291,6 +291,7 @@ struct FactorArgs {
     T *wbuf;     // 32 * bw: W of the current panel (FP64) / staged L rows, two buffers (FP32)
     T *dstage;   // 2 * 32 * 32: staged factored diagonal blocks (FP32)
     GridBarrier *bar;
+    int dist;    // FP32: panel rows formed once per panel (wide bands) instead of per tile
 };
 
 // Tile t of the lower triangle of an nt x nt tile grid: t = ti (ti + 1) / 2 + tj.
@@ -384,7 +385,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
     long mprev = 0;
     for (long p = 0; p <= a.npad; p += NB) {
         // ---- 0. staged output of the previous panel into the band ----
-        if (p > 0) {
+        if (p > 0 && !a.dist) {
             const long pp = p - NB;
             const int buf = (int)((pp / NB) & 1);
             const T *ls = a.wbuf + (long)buf * NB * bw;
@@ -419,9 +420,57 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
             if (blockIdx.x == 0) record_pivots(a, p, A[lane][lane], di[lane], lane);
         }
         __syncthreads();
-        if (blockIdx.x == 0) {
+        if (blockIdx.x == 0 && !a.dist) {
             T *ds = a.dstage + buf * NB * NB;
             for (int idx = tid; idx < NB * NB; idx += 256) ds[idx] = A[idx % NB][idx / NB];
+        }
+        if (a.dist) {
+            // ---- 2'. wide band: panel rows once, one warp per row; W to wbuf,
+            //          L into the band (no other CTA reads this panel's A) ----
+            const long gwarp = blockIdx.x * 8L + warp, nwarps = gridDim.x * 8L;
+            for (long r = gwarp; r < m; r += nwarps) {
+                const long off = NB + r - lane;
+                const T ar = off <= bw ? a.band[(p + lane) * ld + off] : T(0);
+                T w = 0;
+                for (int k = 0; k < NB; ++k) {
+                    const T v = __shfl_sync(0xffffffffu, ar, k);
+                    if (k <= lane) w += v * Li[lane][k];
+                }
+                a.wbuf[lane * m + r] = w;
+                if (off <= bw) a.band[(p + lane) * ld + off] = w * di[lane];
+            }
+            if (!grid_barrier(a.bar, gridDim.x)) return;
+            if (blockIdx.x == 0)
+                for (int idx = tid; idx < NB * NB; idx += 256) {
+                    const int j = idx / NB, i = idx % NB;
+                    if (i >= j && i - j <= bw) a.band[(p + j) * ld + (i - j)] = A[i][j];
+                }
+            const long nt = (m + TS - 1) / TS;
+            const long ntiles = nt * (nt + 1) / 2;
+            for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+                long ti, tj;
+                tile_of(t, ti, tj);
+                const long r0 = ti * TS, j0 = tj * TS;
+                for (int idx = tid; idx < NB * TS; idx += 256) {
+                    const int k = idx / TS, q = idx % TS;
+                    const long rr = r0 + q, jj = j0 + q;
+                    Ar[q][k] = rr < m ? a.wbuf[k * m + rr] : T(0);
+                    Ac[q][k] = jj < m ? a.wbuf[k * m + jj] * di[k] : T(0);
+                }
+                __syncthreads();
+                for (int idx = tid; idx < TS * TS; idx += 256) {
+                    const int ji = idx / TS, ri = idx % TS;
+                    const long rr = r0 + ri, jj = j0 + ji;
+                    if (rr >= m || jj >= m || jj > rr) continue;
+                    T acc = 0;
+#pragma unroll 8
+                    for (int k = 0; k < NB; ++k) acc += Ar[ri][k] * Ac[ji][k];
+                    a.band[(p + NB + jj) * ld + (rr - jj)] -= acc;
+                }
+                __syncthreads();
+            }
+            if (!grid_barrier(a.bar, gridDim.x)) return;
+            continue;
         }
         // ---- 2. trailing tiles ----
         T *ls = a.wbuf + (long)buf * NB * bw;
@@ -569,6 +618,94 @@ __global__ void __launch_bounds__(256) factor_f64_kernel(FactorArgs<double> a)
     }
 }
 
+// Direct substitution with the band factor, for a factorisation that serves
+// one solve (no block inverses): L y = b right-looking over 32-row panels
+// (the panel's unit-lower block solved by warp 0 of every CTA, then the
+// rows below updated), z = D^-1 y, then L^T x = z right-looking from the
+// last panel (the block solved, then the bw rows above updated). One grid
+// barrier per panel each way.
+template <typename T>
+struct DirectArgs {
+    const T *band, *dinv;
+    long ld, bw, npad, n;
+    const double *rhs;
+    double *out;
+    T *y;
+    GridBarrier *bar;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) solve_direct_kernel(DirectArgs<T> a)
+{
+    __shared__ T yp[NB];
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    const long ld = a.ld, bw = a.bw, npad = a.npad;
+    const long gthr = blockIdx.x * 256L + tid, nthr = gridDim.x * 256L;
+    for (long g = gthr; g < npad; g += nthr) a.y[g] = g < a.n ? (T)a.rhs[g] : T(0);
+    if (!grid_barrier(a.bar, gridDim.x)) return;
+    // forward: y_p = L_pp^-1 y_p; y_r -= L(r, p..p+31) y_p for the rows below
+    for (long p = 0; p < npad; p += NB) {
+        long m = npad - p - NB;
+        if (m > bw) m = bw;
+        if (m < 0) m = 0;
+        if (warp == 0) {
+            T l[NB];
+#pragma unroll
+            for (int k = 0; k < NB; ++k) l[k] = (k < lane && lane - k <= bw) ? a.band[(p + k) * ld + (lane - k)] : T(0);
+            T v = a.y[p + lane];
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                const T vk = __shfl_sync(0xffffffffu, v, k);
+                if (lane > k) v -= l[k] * vk;
+            }
+            yp[lane] = v;
+        }
+        __syncthreads();
+        if (blockIdx.x == 0 && tid < NB) a.y[p + tid] = yp[tid];
+        for (long r = gthr; r < m; r += nthr) {
+            T acc = 0;
+#pragma unroll 8
+            for (int k = 0; k < NB; ++k) {
+                const long off = NB + r - k;
+                if (off <= bw) acc += a.band[(p + k) * ld + off] * yp[k];
+            }
+            a.y[p + NB + r] -= acc;
+        }
+        if (!grid_barrier(a.bar, gridDim.x)) return;
+    }
+    for (long g = gthr; g < npad; g += nthr) a.y[g] *= a.dinv[g];
+    if (!grid_barrier(a.bar, gridDim.x)) return;
+    // backward: x_p = L_pp^-T z_p; z_j -= sum_i L(p+i, j) x_i for j in [p-bw, p)
+    for (long p = npad - NB; p >= 0; p -= NB) {
+        if (warp == 0) {
+            // lane k holds z_k; column k of the block: L(p+i, p+k), i > k
+            T l[NB];
+#pragma unroll
+            for (int i = 0; i < NB; ++i) l[i] = (i > lane && i - lane <= bw) ? a.band[(p + lane) * ld + (i - lane)] : T(0);
+            T v = a.y[p + lane];
+#pragma unroll
+            for (int i = NB - 1; i >= 0; --i) {
+                const T xi = __shfl_sync(0xffffffffu, v, i);
+                if (lane < i) v -= l[i] * xi;
+            }
+            yp[lane] = v;
+        }
+        __syncthreads();
+        if (blockIdx.x == 0 && tid < NB) a.y[p + tid] = yp[tid];
+        const long jlo = p - bw > 0 ? p - bw : 0;
+        for (long j = jlo + gthr; j < p; j += nthr) {
+            T acc = 0;
+            const long base = p - j;  // band offset of L(p, j)
+#pragma unroll 8
+            for (int i = 0; i < NB; ++i)
+                if (base + i <= bw) acc += a.band[j * ld + base + i] * yp[i];
+            a.y[j] -= acc;
+        }
+        if (!grid_barrier(a.bar, gridDim.x)) return;
+    }
+    for (long g = gthr; g < a.n; g += nthr) a.out[g] = (double)a.y[g];
+}
+
 template <typename T>
 struct SolveArgs {
     const T *linv, *linvt, *pn, *rn, *dinv;
@@ -673,7 +810,11 @@ void factor_band(BandFactor &f, cudaStream_t st, long *launches)
     const long ntiles = nt * (nt + 1) / 2;
     const long need = std::max(ntiles, (f.bw + 7) / 8);
     const int grid = (int)std::max(1L, std::min((long)f.factor_grid, need));
-    FactorArgs<T> a{band, f.ld, f.bw, npad, f.n, (T *)f.dinv, f.ssd, f.flags, (T *)f.work, (T *)f.stage, f.fbar};
+    // FP32: form each panel's rows once (two barriers per panel) when the
+    // trailing triangle has many more tiles than CTAs; otherwise per tile
+    const int dist = (f.fp32 && ntiles > 2L * grid) ? 1 : 0;
+    FactorArgs<T> a{band, f.ld, f.bw, npad, f.n, (T *)f.dinv, f.ssd, f.flags, (T *)f.work, (T *)f.stage, f.fbar,
+                    dist};
     void *args[] = {&a};
     const void *fn = f.fp32 ? (const void *)factor_f32_kernel<32> : (const void *)factor_f64_kernel<16>;
     CB_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(256), args, 0, st));
@@ -705,9 +846,24 @@ void form_solve_blocks(BandFactor &f, cudaStream_t st, long *launches)
 }
 
 template <typename T>
+void solve_direct_launch(const BandFactor &f, const double *rhs, double *x, void *work, GridBarrier *bar,
+                         cudaStream_t st)
+{
+    DirectArgs<T> a{(const T *)f.band, (const T *)f.dinv, f.ld, f.bw, f.nblk * f.s, f.n, rhs, x, (T *)work, bar};
+    CB_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), st));
+    void *args[] = {&a};
+    CB_CUDA(cudaLaunchCooperativeKernel((const void *)solve_direct_kernel<T>, dim3((unsigned)f.solve_grid),
+                                        dim3(256), args, 0, st));
+}
+
+template <typename T>
 void solve_launch(const BandFactor &f, const double *rhs, double *x, void *work, GridBarrier *bar,
                   cudaStream_t st)
 {
+    if (f.direct) {
+        solve_direct_launch<T>(f, rhs, x, work, bar, st);
+        return;
+    }
     const long npad = f.nblk * f.s;
     SolveArgs<T> a;
     a.linv = (const T *)f.linv;
@@ -746,7 +902,7 @@ void profile_impl(BandFactor &f, int which, cudaStream_t st)
 {
     long dummy = 0;
     if (which == 3) factor_band<T>(f, st, &dummy);             // the persistent LDL^T alone
-    else if (which == 4) form_solve_blocks<T>(f, st, &dummy);  // Linv, Pn, Rn from the factor
+    else if (which == 4 && !f.direct) form_solve_blocks<T>(f, st, &dummy);  // Linv, Pn, Rn from the factor
 }
 
 }  // namespace
@@ -761,13 +917,13 @@ void band_use_factored(BandFactor &f, cudaStream_t st)
             pad_identity_kernel<float><<<(unsigned)((npad - f.n + 127) / 128), 128, 0, st>>>((float *)f.band, f.ld,
                                                                                             f.n, npad);
         dinv_from_diag_kernel<float><<<g, 256, 0, st>>>((const float *)f.band, f.ld, (float *)f.dinv, npad);
-        form_solve_blocks<float>(f, st, &dummy);
+        if (!f.direct) form_solve_blocks<float>(f, st, &dummy);
     } else {
         if (npad > f.n)
             pad_identity_kernel<double><<<(unsigned)((npad - f.n + 127) / 128), 128, 0, st>>>((double *)f.band,
                                                                                              f.ld, f.n, npad);
         dinv_from_diag_kernel<double><<<g, 256, 0, st>>>((const double *)f.band, f.ld, (double *)f.dinv, npad);
-        form_solve_blocks<double>(f, st, &dummy);
+        if (!f.direct) form_solve_blocks<double>(f, st, &dummy);
     }
     CB_CUDA(cudaGetLastError());
 }
@@ -794,19 +950,23 @@ void band_profile_launch(BandFactor &f, int which, cudaStream_t st)
     CB_CUDA(cudaGetLastError());
 }
 
-void band_alloc(BandFactor &f, long n, long bw, bool fp32)
+void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct)
 {
     f.n = n;
     f.bw = std::max(1L, bw);
     f.fp32 = fp32;
+    f.direct = direct;
     f.ld = ((f.bw + 1 + 7) / 8) * 8;
     f.w = std::max(32L, ((f.bw + 31) / 32) * 32);
     const size_t es = fp32 ? 4 : 8;
     // Block size of the solve: FP32 uses up to 4 w (fewer sequential steps,
     // bounded by the inverse blocks' memory of n*s elements); FP64 keeps
-    // s = w because the FP64 inversion work grows with s^2.
+    // s = w because the FP64 inversion work grows with s^2. The direct solve
+    // needs no blocks: the matrix is padded to a multiple of 32 only.
     long s = f.w;
-    if (fp32) {
+    if (direct) {
+        s = NB;
+    } else if (fp32) {
         const double budget = 4.0e9;
         long cap = (long)(budget / ((double)es * (double)std::max(1L, n)));
         s = std::max(f.w, std::min(4 * f.w, (cap / 32) * 32));
@@ -814,28 +974,35 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32)
     f.s = s;
     f.nblk = (n + f.s - 1) / f.s;
     const long npad = f.nblk * f.s;
+    const size_t blocks = direct ? 0 : (size_t)f.nblk * f.s;
     CB_CUDA(cudaMalloc(&f.band, es * (size_t)f.ld * npad));
     CB_CUDA(cudaMalloc(&f.dinv, es * (size_t)npad));
-    CB_CUDA(cudaMalloc(&f.linv, es * (size_t)f.nblk * f.s * f.s));
-    CB_CUDA(cudaMalloc(&f.linvt, es * (size_t)f.nblk * f.s * f.s));
-    CB_CUDA(cudaMalloc(&f.pmat, es * (size_t)f.nblk * f.s * f.w));
-    CB_CUDA(cudaMalloc(&f.rmat, es * (size_t)f.nblk * f.s * f.w));
+    if (!direct) {
+        CB_CUDA(cudaMalloc(&f.linv, es * blocks * f.s));
+        CB_CUDA(cudaMalloc(&f.linvt, es * blocks * f.s));
+        CB_CUDA(cudaMalloc(&f.pmat, es * blocks * f.w));
+        CB_CUDA(cudaMalloc(&f.rmat, es * blocks * f.w));
+        CB_CUDA(cudaMemset(f.linv, 0, es * blocks * f.s));
+        CB_CUDA(cudaMemset(f.linvt, 0, es * blocks * f.s));
+        CB_CUDA(cudaMemset(f.pmat, 0, es * blocks * f.w));
+        CB_CUDA(cudaMemset(f.rmat, 0, es * blocks * f.w));
+    }
     size_t work = std::max((size_t)3 * npad, (size_t)2 * NB * f.bw + NB);
     CB_CUDA(cudaMalloc(&f.work, es * work));
     CB_CUDA(cudaMalloc(&f.ssd, sizeof(double) * (size_t)n));
     CB_CUDA(cudaMalloc(&f.flags, 2 * sizeof(int)));
     CB_CUDA(cudaMalloc(&f.bar, sizeof(GridBarrier)));
     CB_CUDA(cudaMalloc(&f.stage, es * 2 * NB * NB));
-    CB_CUDA(cudaMemset(f.linv, 0, es * (size_t)f.nblk * f.s * f.s));
-    CB_CUDA(cudaMemset(f.linvt, 0, es * (size_t)f.nblk * f.s * f.s));
-    CB_CUDA(cudaMemset(f.pmat, 0, es * (size_t)f.nblk * f.s * f.w));
-    CB_CUDA(cudaMemset(f.rmat, 0, es * (size_t)f.nblk * f.s * f.w));
     CB_CUDA(cudaMemset(f.bar, 0, sizeof(GridBarrier)));
     CB_CUDA(cudaMalloc(&f.fbar, sizeof(GridBarrier)));
     CB_CUDA(cudaMemset(f.fbar, 0, sizeof(GridBarrier)));
-    f.solve_grid = fp32 ? max_cooperative_grid(solve_kernel<float>) : max_cooperative_grid(solve_kernel<double>);
+    if (direct)
+        f.solve_grid = fp32 ? max_cooperative_grid(solve_direct_kernel<float>)
+                            : max_cooperative_grid(solve_direct_kernel<double>);
+    else
+        f.solve_grid = fp32 ? max_cooperative_grid(solve_kernel<float>) : max_cooperative_grid(solve_kernel<double>);
     f.factor_grid = fp32 ? max_cooperative_grid(factor_f32_kernel<32>) : max_cooperative_grid(factor_f64_kernel<16>);
-    f.bytes = es * ((size_t)f.ld * npad + npad + (size_t)f.nblk * f.s * (2 * f.s + 2 * f.w) + work);
+    f.bytes = es * ((size_t)f.ld * npad + npad + blocks * (2 * f.s + 2 * f.w) + work);
 }
 
 void band_free(BandFactor &f)
@@ -853,6 +1020,7 @@ void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches)
     long *cnt = launches ? launches : &dummy;
     if (f.fp32) factor_band<float>(f, st, cnt);
     else factor_band<double>(f, st, cnt);
+    if (f.direct) return;
     if (!use_graph) {
         if (f.fp32) form_solve_blocks<float>(f, st, cnt);
         else form_solve_blocks<double>(f, st, cnt);

@@ -127,6 +127,7 @@ struct BandFactor {
     GridBarrier *fbar = nullptr; // persistent-factor barrier
     void *stage = nullptr;       // 2 x 32x32: staged factored diagonal blocks (FP32 factor)
     bool fp32 = false;
+    bool direct = false;         // no solve blocks: substitution with the band (one solve per factor)
     int solve_grid = 1;          // CTAs of the cooperative solve launch
     int factor_grid = 1;         // most CTAs of the cooperative factor launch
     size_t bytes = 0;            // device memory held
@@ -134,7 +135,9 @@ struct BandFactor {
     long factor_launches = 0;
 };
 
-void band_alloc(BandFactor &f, long n, long bw, bool fp32);
+// direct: the factor serves one solve (Newmark's full Newton): the solve
+// substitutes with the band itself and no solve blocks are formed
+void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct = false);
 void band_free(BandFactor &f);
 // The band already holds an LDL^T factor (L below, D on the diagonal): form
 // 1/d and the solve blocks so that band_solve can use it.

@@ -165,7 +165,9 @@ void upload_model(cb_model *m)
     h2d(m->fmap_ptr, fm.ptr.data(), fm.ptr.size(), st);
     h2d(m->fmap_src, fm.src.data(), fm.src.size(), st);
     const bool fp32 = m->opt.precision == CB_MIXED;
-    cb::band_alloc(m->bf, N, h.bw, fp32);
+    // Newmark refactors every iteration and solves once per factorisation:
+    // direct substitution, no solve blocks
+    cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5);
     m->bytes += m->bf.bytes;
     cb::build_tangent_map(h, m->bf.ld, tm);
     m->tmap_n = (long)tm.dst.size();
