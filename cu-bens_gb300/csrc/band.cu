@@ -380,6 +380,8 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
     __shared__ T di[NB];
     __shared__ T Ar[TS][NB + 1];  // raw panel rows of the tile's row block, then W
     __shared__ T Ac[TS][NB + 1];  // raw panel rows of the tile's column block, then L
+    __shared__ T Wd[NB][64];      // wide bands: W of a 64-row block (k-major)
+    __shared__ T Ld[NB][64];      // wide bands: L of a 64-column block
     const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
     const long ld = a.ld, bw = a.bw;
     long mprev = 0;
@@ -445,27 +447,50 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                     const int j = idx / NB, i = idx % NB;
                     if (i >= j && i - j <= bw) a.band[(p + j) * ld + (i - j)] = A[i][j];
                 }
-            const long nt = (m + TS - 1) / TS;
+            // 64 x 64 tiles, a 4 x 4 register block per thread: rows
+            // r0 + tx + 16 i (consecutive threads, consecutive rows of a
+            // column), columns j0 + ty + 16 j
+            constexpr int WT = 64;
+            const int tx = tid % 16, ty = tid / 16;
+            const long nt = (m + WT - 1) / WT;
             const long ntiles = nt * (nt + 1) / 2;
             for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
                 long ti, tj;
                 tile_of(t, ti, tj);
-                const long r0 = ti * TS, j0 = tj * TS;
-                for (int idx = tid; idx < NB * TS; idx += 256) {
-                    const int k = idx / TS, q = idx % TS;
+                const long r0 = ti * WT, j0 = tj * WT;
+                for (int idx = tid; idx < NB * WT; idx += 256) {
+                    const int k = idx / WT, q = idx % WT;
                     const long rr = r0 + q, jj = j0 + q;
-                    Ar[q][k] = rr < m ? a.wbuf[k * m + rr] : T(0);
-                    Ac[q][k] = jj < m ? a.wbuf[k * m + jj] * di[k] : T(0);
+                    Wd[k][q] = rr < m ? a.wbuf[k * m + rr] : T(0);
+                    Ld[k][q] = jj < m ? a.wbuf[k * m + jj] * di[k] : T(0);
                 }
                 __syncthreads();
-                for (int idx = tid; idx < TS * TS; idx += 256) {
-                    const int ji = idx / TS, ri = idx % TS;
-                    const long rr = r0 + ri, jj = j0 + ji;
-                    if (rr >= m || jj >= m || jj > rr) continue;
-                    T acc = 0;
+                T acc[4][4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = 0;
 #pragma unroll 8
-                    for (int k = 0; k < NB; ++k) acc += Ar[ri][k] * Ac[ji][k];
-                    a.band[(p + NB + jj) * ld + (rr - jj)] -= acc;
+                for (int k = 0; k < NB; ++k) {
+                    T wv[4], lv[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        wv[i] = Wd[k][tx + 16 * i];
+                        lv[i] = Ld[k][ty + 16 * i];
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] += wv[i] * lv[j];
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const long jj = j0 + ty + 16 * j;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const long rr = r0 + tx + 16 * i;
+                        if (rr < m && jj < m && jj <= rr) a.band[(p + NB + jj) * ld + (rr - jj)] -= acc[i][j];
+                    }
                 }
                 __syncthreads();
             }
