@@ -9,6 +9,14 @@ LDL^T, predictor and the modified-Newton corrector iterations to the
 reference's own convergence test.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload panel|frame]
+
+--workload frame measures the nonlinear Newmark workload instead: the
+20 x 20 bay, 30 storey steel frame building (13,671 joints, 38,430
+co-rotational 14-DOF members, warping fixed: NEQ 79,380), seeded
+band-limited lateral floor forces, dt 0.005 s; a step is one time step
+(main.c:3449-3953: full Newton, the effective stiffness factored every
+iteration).
 
 Under torchrun with N > 1 every rank runs an independent replica of the
 analysis on its own GPU (the analysis does not shard); value is the total
@@ -25,6 +33,8 @@ import sys
 import threading
 import time
 from pathlib import Path
+
+import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "cu-bens_gb300"))
@@ -194,6 +204,276 @@ def run_reference(args, world, rank, pg):
     print(json.dumps(line), flush=True)
 
 
+FRAME_WORKLOAD = ("frame building 20x20 bays x 30 storeys (13,671 joints, 38,430 frame members, "
+                  "NEQ 79,380), nonlinear Newmark dt 0.005")
+
+
+def frame_text(steps: int, bays=(20, 20, 30)):
+    from cubens import models
+    return models.frame_building(*bays, steps=steps, dt=0.005, seed=4).text
+
+
+def frame_cpu_sample(target_s: float = 20.0):
+    """The oracle port on a reduced building with the same members, loads and
+    controls (10 x 10 bays x 15 storeys, NEQ 10,890, bandwidth 731): whole
+    time steps for about target_s, then scaled to the full building by the
+    skyline factorisation work n bw^2 of one full-Newton iteration."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    import time as _t
+    steps = 3
+    o = oracle.OracleModel(frame_text(steps + 1, (10, 10, 15)))
+    t0 = _t.perf_counter()
+    r = o.newmark(steps)
+    secs = _t.perf_counter() - t0
+    if r["rc"] < steps:
+        raise RuntimeError(f"oracle stopped early: {r['error']}")
+    n_s, bw_s = o.neq, 0
+    full = oracle.OracleModel(frame_text(2))
+    # skyline column heights give the bandwidth of both models
+    for mod in (o, full):
+        maxa, _ = mod.tangent_fr(*([np.zeros(9 * mod.ne_fr), np.zeros(14 * mod.ne_fr), np.ones(mod.ne_fr),
+                                     np.ones(mod.ne_fr)]))
+        bw = int(np.max(np.diff(maxa)) - 1)
+        if mod is o:
+            bw_s = bw
+        else:
+            bw_f = bw
+    scale = (full.neq * bw_f ** 2) / (n_s * bw_s ** 2)
+    value = steps / secs / scale
+    return {"value": value, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"oracle port (gcc -O2, 1 thread): {steps} time steps of the 10x10x15 building "
+                      f"(NEQ {n_s}, bandwidth {bw_s}) in {secs:.1f} s, {np.mean(r['its']):.1f} iterations per step, "
+                      f"scaled by n bw^2 to NEQ {full.neq}, bandwidth {bw_f} (x{scale:.1f})"}
+
+
+def run_frame(args, world, rank, local, pg):
+    import cubens
+    device = local if world > 1 else 0
+    hbm_peak, peak_kind = peaks()
+    text = frame_text(args.warmup + args.steps + 2)
+
+    def analysis(precision):
+        m = cubens.Model(text, precision=precision, device=device)
+        m.newmark_begin()
+        for _ in range(args.warmup):
+            m.newmark_step()
+        return m
+
+    def timed(m, k):
+        m.mark(0)
+        w0 = time.perf_counter()
+        its, res = [], []
+        for _ in range(k):
+            r = m.newmark_step()
+            its.append(r.iterations)
+            res.append(r.residual)
+        m.mark(1)
+        dev = m.elapsed_ms(0, 1)
+        return dev, (time.perf_counter() - w0) * 1e3, its, res
+
+    m = analysis(cubens.MIXED)
+    info = m.info
+    clocks = ClockSampler(device)
+    barrier(pg)
+    l0 = m.timers()["launches"]
+    clocks.start()
+    dev_ms, wall_ms, its, res = timed(m, args.steps)
+    clk = clocks.stop()
+    launches = m.timers()["launches"] - l0
+    barrier(pg)
+    t_max = allmax(pg, wall_ms)
+    value = world * args.steps / (t_max / 1e3)
+    ms_ldlt, bytes_ldlt, flops_ldlt = m.profile_kernel(cubens.K_BAND_LDLT, reps=2)
+    ms_solve, _, _ = m.profile_kernel(cubens.K_SOLVE, reps=2)
+    ms_ff, bytes_ff, _ = m.profile_kernel(cubens.K_FRAME_FORCE, reps=5)
+    m.close()
+    p = analysis(cubens.FP64)
+    dev64, wall64, its64, res64 = timed(p, max(1, args.steps // 3))
+    n64 = max(1, args.steps // 3)
+    p.close()
+    e2e = None
+    if not args.skip_e2e:
+        barrier(pg)
+        w0 = time.perf_counter()
+        e = cubens.Model(text, precision=cubens.MIXED, device=device)
+        e.newmark_begin()
+        d2h = 0
+        nst = args.warmup + args.steps
+        for _ in range(nst):
+            e.newmark_step()
+            d, _ = e.displacements()
+            d2h += d.nbytes
+        e2e_s = time.perf_counter() - w0
+        h2d = e.info["h2d_bytes"]
+        e.close()
+        e2e = {"value": world * nst / allmax(pg, e2e_s), "unit": "steps/s", "h2d_bytes_per_step": h2d / nst,
+               "d2h_bytes_per_step": d2h / nst,
+               "includes": "model_def parse + upload, all time steps from rest, d read back after every step"}
+    if rank != 0:
+        return None
+    cpu = frame_cpu_sample() if world == 1 and not args.skip_cpu else None
+    achieved = bytes_ldlt / (ms_ldlt * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 effective stiffness/LDLT + f64 residual", "data": "synthetic",
+        "config": {"workload": FRAME_WORKLOAD, "neq": info["neq"], "bandwidth": info["bandwidth"],
+                   "controls": "numopt 0 (beta 0.25, gamma 0.5), lpf 1, toldisp 1e-8, tolener 1e-8",
+                   "parallelism": f"replicas x{world}", "l2": "working set > L2 (band "
+                   f"{info['device_bytes'] / 1e9:.2f} GB)", "iterations_per_step": its,
+                   "max_rel_residual": max(res), "device_ms_timed": dev_ms,
+                   "fp64_plain": {"value": n64 / (wall64 / 1e3), "ms_per_step": wall64 / n64,
+                                  "iterations_per_step": its64, "max_rel_residual": max(res64)},
+                   "band_ldlt_ms": ms_ldlt, "band_ldlt_GFLOPs": flops_ldlt / (ms_ldlt * 1e-3) / 1e9,
+                   "direct_solve_ms": ms_solve, "frame_force_ms": ms_ff},
+        "roofline": {"kernel": "factor_f32_kernel (persistent band LDL^T, wide-band mode, FP32)", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "peak_kind": peak_kind, "traffic": None, "bytes_per_launch": bytes_ldlt,
+                     "ms_per_launch": ms_ldlt,
+                     "note": "latency/FMA-bound: 2,481 dependent panels, n bw^2/2 FMA per launch"},
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_reference_frame(args, world, rank, pg):
+    if rank != 0:
+        return
+    cpu = frame_cpu_sample()
+    line = {"metric": METRIC, "value": cpu["value"], "unit": "steps/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cpu["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": FRAME_WORKLOAD},
+            "cpu_baseline": cpu, "e2e": {"value": cpu["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+BATCH_WORKLOAD = ("batched imperfection sweep: DKT panels n x n, n drawn from {16,24,...,96} (seeded), "
+                  "4-mode imperfection 0.1 t, MSAL dk -0.2, toldisp 1e-4, FP32 tangent/LDL^T + FP64 residual")
+
+
+def batch_specs(count: int, seed: int = 2024):
+    from cubens import models
+    out = []
+    for i, n in enumerate(models.batch_sizes(count, seed)):
+        # the imperfect panels need the displacement tolerance 1e-4: at 1e-5 the
+        # reference's own first increment does not converge on most of them
+        c = models.MsalControls(joint=n // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.2, toldisp=1e-4,
+                                tolforc=1.0, tolener=1.0, itemax=100)
+        out.append(models.cylindrical_panel(n, seed=seed + i, imperfection=0.1, controls=c))
+    return out
+
+
+def _oracle_batch_item(args):
+    text, steps = args
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    r = oracle.OracleModel(text).msal_timed(steps)
+    return len(r["t"]), (r["t"][-1] - r["t"][0]) if len(r["t"]) > 1 else 0.0, r["t"][0] if len(r["t"]) else 0.0
+
+
+def batch_cpu_sample(specs, steps: int):
+    """The oracle port on the host cores, one process per analysis (the
+    reference is single-threaded): a pool of all cores over the first
+    instances, each for `steps` arc-length steps; aggregate steps/s."""
+    import multiprocessing as mp
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    sample = specs[:cores]
+    ctx = mp.get_context("spawn")
+    w0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        rs = pool.map(_oracle_batch_item, [(s.text, steps + 1) for s in sample])
+    wall = time.perf_counter() - w0
+    nsteps = sum(max(0, k - 1) for k, _, _ in rs)
+    busy = sum(t for _, t, _ in rs)
+    return {"value": nsteps / wall, "unit": "steps/s", "cores": cores, "kind": "port",
+            "sample": f"oracle port (gcc -O2), {len(sample)} instances of the sweep in a pool of {cores} "
+                      f"processes, {steps} arc-length steps each after the first increment; {nsteps} steps in "
+                      f"{wall:.1f} s wall ({busy:.1f} s of step time)"}
+
+
+def run_batch(args, world, rank, local, pg):
+    import cubens
+    device = local if world > 1 else 0
+    count = args.batch
+    specs = batch_specs(count)
+    steps = args.steps + 1
+    cpu = batch_cpu_sample(specs, min(3, args.steps)) if (rank == 0 and world == 1 and not args.skip_cpu) else None
+    c0 = time.perf_counter()
+    batch = [cubens.Model(s.text, precision=cubens.MIXED, device=device) for s in specs]
+    create_s = time.perf_counter() - c0
+    h2d = sum(b.info["h2d_bytes"] for b in batch)
+    threads = min(16, os.cpu_count() or 4)
+    # warm-up: a separate small batch (first increments of 4 instances)
+    warm = [cubens.Model(s.text, precision=cubens.MIXED, device=device) for s in specs[:4]]
+    cubens.batch_msal(warm, 1 + args.warmup, threads=threads)
+    for w in warm:
+        w.close()
+    clocks = ClockSampler(device)
+    barrier(pg)
+    clocks.start()
+    w0 = time.perf_counter()
+    rc, res = cubens.batch_msal(batch, steps, threads=threads)
+    wall = time.perf_counter() - w0
+    clk = clocks.stop()
+    barrier(pg)
+    nconv = sum(len(r["its"]) for r in res)
+    t_max = allmax(pg, wall)
+    value = world * nconv / t_max
+    neqs = [b.info["neq"] for b in batch]
+    mem = sum(b.info["device_bytes"] for b in batch)
+    launches = sum(b.timers()["launches"] for b in batch)
+    for b in batch:
+        b.close()
+    # the same analyses one after another on one thread
+    seq = [cubens.Model(s.text, precision=cubens.MIXED, device=device) for s in specs[:8]]
+    w0 = time.perf_counter()
+    _, rs = cubens.batch_msal(seq, steps, threads=1)
+    seq_wall = time.perf_counter() - w0
+    seq_rate = sum(len(r["its"]) for r in rs) / seq_wall
+    for b in seq:
+        b.close()
+    if rank != 0:
+        return None
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / max(1, nconv), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 tangent/LDLT + f64 residual",
+            "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD, "instances": count, "steps_per_instance": steps,
+                       "neq_min": min(neqs), "neq_max": max(neqs), "host_threads": threads,
+                       "device_bytes_total": mem, "status": rc,
+                       "sequential_one_thread_steps_per_s": seq_rate,
+                       "l2": "working set > L2", "parallelism": f"replicas x{world}"},
+            "roofline": None, "cpu_baseline": cpu,
+            "e2e": {"value": world * nconv / allmax(pg, create_s + wall), "unit": "steps/s",
+                    "h2d_bytes_per_step": h2d / max(1, nconv), "d2h_bytes_per_step": 48,
+                    "includes": "model_def parse + upload of every instance, then the batch call (each step's "
+                                "record read back)"},
+            "clocks": clk, "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_reference_batch(args, world, rank, pg):
+    if rank != 0:
+        return
+    cpu = batch_cpu_sample(batch_specs(args.batch), min(3, args.steps))
+    line = {"metric": METRIC, "value": cpu["value"], "unit": "steps/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cpu["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": BATCH_WORKLOAD, "instances": args.batch},
+            "cpu_baseline": cpu, "e2e": {"value": cpu["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, world, rank, local, pg):
     import cubens
     text, ctrl = panel_text()
@@ -326,9 +606,23 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample (profiling runs)")
     ap.add_argument("--skip-e2e", action="store_true", help="omit the end-to-end leg (profiling runs)")
+    ap.add_argument("--workload", choices=["panel", "frame", "batch"], default="panel",
+                    help="panel: MSAL DKT panel 64x64 (default); frame: nonlinear Newmark frame building; "
+                         "batch: the batched imperfection sweep")
+    ap.add_argument("--batch", type=int, default=48, help="instances of the batch workload")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup(args.gpus)
-    if args.impl == "reference":
+    if args.workload == "batch":
+        if args.impl == "reference":
+            run_reference_batch(args, world, rank, pg)
+        else:
+            run_batch(args, world, rank, local, pg)
+    elif args.workload == "frame":
+        if args.impl == "reference":
+            run_reference_frame(args, world, rank, pg)
+        else:
+            run_frame(args, world, rank, local, pg)
+    elif args.impl == "reference":
         run_reference(args, world, rank, pg)
     else:
         run_ours(args, world, rank, local, pg)

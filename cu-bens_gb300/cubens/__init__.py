@@ -93,6 +93,7 @@ def load(path: Path | None = None):
     L.cb_eval_tangent.argtypes = [vp, dp, dp, dp, dp, lp, dp]
     L.cb_factor_solve.argtypes = [vp, dp, dp, dp, ip]
     L.cb_solve_noalloc.argtypes = [vp, vp, vp]
+    L.cb_batch_msal.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.POINTER(Step), ip]
     L.cb_newmark_begin.argtypes = [vp]
     L.cb_newmark_step.argtypes = [vp, C.POINTER(Step)]
     L.cb_newmark_state.argtypes = [vp, dp, dp, dp]
@@ -109,6 +110,24 @@ def _d(a):
 
 def _c64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def batch_msal(models, steps: int, threads: int = 16):
+    """Run the arc-length loop of several Models concurrently (cb_batch_msal):
+    returns per model dict(lam, its, res, status)."""
+    L = load()
+    n = len(models)
+    hs = (C.c_void_p * n)(*[m.h for m in models])
+    out = (Step * (n * steps))()
+    st = (C.c_int * n)()
+    rc = L.cb_batch_msal(hs, n, steps, threads, out, st)
+    res = []
+    for i in range(n):
+        recs = [out[i * steps + k] for k in range(steps)]
+        recs = [r for r in recs if not r.done]
+        res.append(dict(lam=np.array([r.lam for r in recs]), its=np.array([r.iterations for r in recs]),
+                        res=np.array([r.residual for r in recs]), status=int(st[i])))
+    return rc, res
 
 
 @dataclass

@@ -117,6 +117,16 @@ int cb_msal_step(cb_model *m, cb_step *out);
 /* Current converged displacements d (NEQ) and lambda. */
 int cb_get_displacements(const cb_model *m, double *d, double *lam);
 
+/* Batched analyses: runs cb_msal_begin and steps - 1 cb_msal_step on each
+ * of n independent handles (each created on its own, e.g. the panels of an
+ * imperfection sweep) from a pool of `threads` host threads; the handles'
+ * streams overlap on the GPU. out holds n * steps records (handle i's step k
+ * at out[i * steps + k]; records after a stop have done = 1); status (may be
+ * NULL) gets each handle's return code. Returns CB_OK or the first failing
+ * handle's code. The handles must be distinct and not used by others
+ * meanwhile. */
+int cb_batch_msal(cb_model **models, int n, int steps, int threads, cb_step *out, int *status);
+
 /* Nonlinear Newmark (ALGFLAG 5, frame models). cb_newmark_begin sets the
  * initial state of main.c:3398-3447 (zero motion); each cb_newmark_step runs
  * one time step k of main.c:3449-3953 (load-factor passes and time-increment

@@ -120,3 +120,24 @@ def test_newmark_call_order_and_model_kind(golden_dir):
     with pytest.raises(cubens.CubensError) as e:
         cubens.Model(str(zs["model_def"])).newmark_begin()
     assert e.value.code == 7
+
+
+def test_batched_msal_matches_single_runs():
+    """cb_batch_msal runs independent panels of different sizes concurrently;
+    every handle's path equals its run alone (and the oracle's)."""
+    specs = []
+    for i, n in enumerate((8, 16, 24, 8, 16)):
+        c = models.MsalControls(joint=n // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.2, toldisp=1e-4,
+                                tolforc=1.0, tolener=1.0, itemax=100)
+        specs.append(models.cylindrical_panel(n, seed=100 + i, imperfection=0.1, controls=c))
+    steps = 4
+    batch = [cubens.Model(s.text, precision=cubens.MIXED) for s in specs]
+    rc, res = cubens.batch_msal(batch, steps, threads=3)
+    assert rc == 0
+    for s, r in zip(specs, res):
+        alone = cubens.Model(s.text, precision=cubens.MIXED).run(steps, with_d=False)
+        np.testing.assert_array_equal(r["its"], alone["its"])
+        np.testing.assert_array_equal(r["lam"], alone["lam"])
+    o = oracle.OracleModel(specs[2].text).msal(steps)
+    np.testing.assert_array_equal(res[2]["its"], o["its"])
+    assert np.max(np.abs(res[2]["lam"] - o["lam"]) / np.abs(o["lam"])) < 1e-5
