@@ -930,7 +930,64 @@ void profile_impl(BandFactor &f, int which, cudaStream_t st)
     else if (which == 4 && !f.direct) form_solve_blocks<T>(f, st, &dummy);  // Linv, Pn, Rn from the factor
 }
 
+// ---- FP64 effective stiffness beside an FP32 factor (iterative refinement) ----
+
+// band32 = (float) band64 over the stored part of the band
+__global__ void band_to_f32_kernel(const double *__restrict__ b64, float *__restrict__ b32, long total)
+{
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q < total) b32[q] = (float)b64[q];
+}
+
+// w_j = K_jj x_j + sum_{i > j} K_ij x_i: one warp per column, coalesced
+// along the column's band entries
+__global__ void band_upper_dot_kernel(const double *__restrict__ band, long ld, long bw, long n,
+                                      const double *__restrict__ x, double *__restrict__ w)
+{
+    const long j = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x % 32;
+    if (j >= n) return;
+    double acc = 0;
+    for (long off = lane; off <= bw && j + off < n; off += 32) acc += band[j * ld + off] * x[j + off];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) w[j] = acc;
+}
+
+// r_i = b_i - (w_i + sum_{j < i} K_ij x_j): one thread per row
+__global__ void band_residual_kernel(const double *__restrict__ band, long ld, long bw, long n,
+                                     const double *__restrict__ b, const double *__restrict__ x,
+                                     const double *__restrict__ w, double *__restrict__ r)
+{
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = w[i];
+    const long lo = i - bw > 0 ? i - bw : 0;
+    for (long j = lo; j < i; ++j) acc += band[j * ld + (i - j)] * x[j];
+    r[i] = b[i] - acc;
+}
+
 }  // namespace
+
+void band_share_gpu(BandFactor &f, bool shared)
+{
+    if (f.direct) return;
+    f.solve_grid = shared ? (int)std::min<long>(f.solve_grid_full, std::max(32L, f.s / 8)) : f.solve_grid_full;
+}
+
+void band_copy_to_f32(const double *band64, BandFactor &f, cudaStream_t st)
+{
+    const long total = f.ld * f.nblk * f.s;
+    band_to_f32_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(band64, (float *)f.band, total);
+    CB_CUDA(cudaGetLastError());
+}
+
+void band_residual64(const double *band64, long ld, long bw, long n, const double *b, const double *x, double *r,
+                     double *w, cudaStream_t st)
+{
+    band_upper_dot_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(band64, ld, bw, n, x, w);
+    band_residual_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(band64, ld, bw, n, b, x, w, r);
+    CB_CUDA(cudaGetLastError());
+}
 
 void band_use_factored(BandFactor &f, cudaStream_t st)
 {
@@ -1021,11 +1078,17 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct)
     CB_CUDA(cudaMemset(f.bar, 0, sizeof(GridBarrier)));
     CB_CUDA(cudaMalloc(&f.fbar, sizeof(GridBarrier)));
     CB_CUDA(cudaMemset(f.fbar, 0, sizeof(GridBarrier)));
-    if (direct)
+    // The direct solve's grid is sized to the work of one panel step (at most
+    // bw rows), which also keeps its grid barriers cheap; the block solve
+    // takes every SM unless band_share_gpu narrows it.
+    if (direct) {
         f.solve_grid = fp32 ? max_cooperative_grid(solve_direct_kernel<float>)
                             : max_cooperative_grid(solve_direct_kernel<double>);
-    else
+        f.solve_grid = (int)std::min<long>(f.solve_grid, std::max(16L, f.bw / 64));
+    } else {
         f.solve_grid = fp32 ? max_cooperative_grid(solve_kernel<float>) : max_cooperative_grid(solve_kernel<double>);
+    }
+    f.solve_grid_full = f.solve_grid;
     f.factor_grid = fp32 ? max_cooperative_grid(factor_f32_kernel<32>) : max_cooperative_grid(factor_f64_kernel<16>);
     f.bytes = es * ((size_t)f.ld * npad + npad + blocks * (2 * f.s + 2 * f.w) + work);
 }

@@ -12,6 +12,8 @@
 
 #include "cubens_gb300.h"
 
+extern "C" void cb_internal_share_gpu(cb_model *m, int shared);
+
 namespace {
 
 int run_one(cb_model *m, int steps, cb_step *out)
@@ -50,10 +52,12 @@ extern "C" int cb_batch_msal(cb_model **models, int n, int steps, int threads, c
             if (status) status[i] = rc;
         }
     };
+    for (int i = 0; i < n; ++i) cb_internal_share_gpu(models[i], threads > 1);
     std::vector<std::thread> pool;
     pool.reserve(threads);
     for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
     for (auto &t : pool) t.join();
+    for (int i = 0; i < n; ++i) cb_internal_share_gpu(models[i], 0);
     if (status)
         for (int i = 0; i < n; ++i)
             if (status[i] != CB_OK) return status[i];

@@ -129,6 +129,7 @@ struct BandFactor {
     bool fp32 = false;
     bool direct = false;         // no solve blocks: substitution with the band (one solve per factor)
     int solve_grid = 1;          // CTAs of the cooperative solve launch
+    int solve_grid_full = 1;     // ... when the handle has the GPU to itself
     int factor_grid = 1;         // most CTAs of the cooperative factor launch
     size_t bytes = 0;            // device memory held
     cudaGraphExec_t factor_graph = nullptr;
@@ -147,6 +148,16 @@ void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches)
 // One launch sequence for isolated timing: 3 = the persistent LDL^T of the
 // band as it stands (overwrites it), 4 = the solve blocks from the factor.
 void band_profile_launch(BandFactor &f, int which, cudaStream_t st);
+// Handles that run concurrently (cb_batch_msal) give the block solve one warp
+// per row of a block step (s/8 CTAs) instead of every SM, so that several
+// handles' kernels fit at once; false restores the full grid.
+void band_share_gpu(BandFactor &f, bool shared);
+// FP64 effective stiffness kept beside an FP32 factor (same band layout):
+// copy it into the factor's band as FP32, and r = b - K x with it (w: n
+// scratch values).
+void band_copy_to_f32(const double *band64, BandFactor &f, cudaStream_t st);
+void band_residual64(const double *band64, long ld, long bw, long n, const double *b, const double *x, double *r,
+                     double *w, cudaStream_t st);
 // Bytes band_solve_with_work needs: 256 for the barrier + 3*npad work elements.
 size_t band_work_bytes(const BandFactor &f);
 // The solve with caller-provided work memory (band_work_bytes(f): the grid

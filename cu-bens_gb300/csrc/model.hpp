@@ -77,6 +77,9 @@ struct cb_model {
            *fp = nullptr;
     double *me = nullptr;
     double *pin = nullptr;
+    // mixed Newmark: the effective stiffness in FP64 beside the FP32 factor,
+    // FP64 element tangents and the refinement vectors (r, correction, scratch)
+    double *band64 = nullptr, *kel64 = nullptr, *ref_r = nullptr, *ref_x = nullptr, *ref_w = nullptr;
     int nm_phase = 0;       // 0 not started, 1 running, 2 finished
     long nm_k = 0;          // next time step
     double nm_ddt = 1;      // time increment multiplier carried between steps (main.c:3452)

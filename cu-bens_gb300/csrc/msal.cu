@@ -179,6 +179,11 @@ void upload_model(cb_model *m)
     h2d(m->tmap_dst, tm.dst.data(), tm.dst.size(), st);
     if (fp32) m->kel = m->alloc<float>(171 * E + 21 * T + 105 * F);
     else m->kel = m->alloc<double>(171 * E + 21 * T + 105 * F);
+    if (fp32 && h.alg == 5) {
+        m->band64 = m->alloc<double>((size_t)m->bf.ld * m->bf.nblk * m->bf.s);
+        m->kel64 = m->alloc<double>(105 * F);
+        for (double **v : {&m->ref_r, &m->ref_x, &m->ref_w}) *v = m->alloc<double>(N);
+    }
     m->sc = m->alloc<cb::MsalScalars>(1);
     m->partial = m->alloc<double>(16 * cb::kRedBlocks);
     CB_CUDA(cudaMallocHost(&m->sc_h, sizeof(cb::MsalScalars)));
@@ -753,6 +758,11 @@ cb::BandFactor *cb_internal_factor(cb_model *m, cudaStream_t *st, int *device)
     *st = m->st;
     *device = m->opt.device;
     return &m->bf;
+}
+
+void cb_internal_share_gpu(cb_model *m, int shared)
+{
+    if (m) cb::band_share_gpu(m->bf, shared != 0);
 }
 
 void cb_internal_set_error(cb_model *m, const char *msg)

@@ -24,6 +24,12 @@ namespace {
 
 using namespace drv;
 
+// Most refinement steps of a mixed-precision Newmark solve. Each FP32 solve
+// of the frame building's effective stiffness gains one to two digits, so a
+// solve needs several corrections to reach the FP64 solution that keeps the
+// full Newton iteration counts of the FP64 path.
+constexpr int kRefineSteps = 12;
+
 struct NewmarkParams {
     double alpham = 0, alphaf = 0, alpha = 0.25, delta = 0.5;
 };
@@ -88,7 +94,19 @@ cb::MsalScalars &newmark_iteration(cb_model *m, const NewmarkParams &p, long k, 
     // tangent of the previous iteration's state with llength_temp as it
     // stands, then the mass at the converged coordinates, which rewrites
     // llength_temp (mass_fr, frame.c:1339)
-    assemble_tangent(m, TangentState::previous_iteration);
+    const bool refine = m->bf.fp32;
+    if (refine) {
+        // mixed: the effective stiffness is assembled in FP64 and kept; its
+        // FP32 copy is factored and the solve refined against it
+        PhaseTimer t(m, &m->tm.ms_tangent);
+        const cb::DevFrame &fr = m->fr;
+        CB_CUDA(cudaMemsetAsync(m->band64, 0, sizeof(double) * (size_t)m->bf.ld * m->bf.nblk * m->bf.s, st));
+        cb::launch_frame_tangent<double>(fr, fr.c_ip, fr.ef_ip, fr.len_ip, m->fr_lref, m->kel64, F, st);
+        cb::launch_gather_band<double>(m->tmap_ptr, m->tmap_src, m->tmap_dst, m->kel64, m->band64, m->tmap_n, st);
+        m->tm.launches += 3;
+    } else {
+        assemble_tangent(m, TangentState::previous_iteration);
+    }
     {
         PhaseTimer t(m, &m->tm.ms_tangent);
         cb::launch_frame_mass(m->fr, m->x_c, m->fr_lref, m->me, F, st);
@@ -103,12 +121,38 @@ cb::MsalScalars &newmark_iteration(cb_model *m, const NewmarkParams &p, long k, 
         cb::launch_nm_reff(mode, sub_dt, lpf, p.alpham, p.alphaf, a2, a3, pin_km1, pin_k, m->fcur, m->sm, m->vc_i,
                            m->ac_i, m->qtot, m->r, N, st);
         const double c0 = a0 * (1 - p.alpham), den = 1 - p.alphaf;
-        if (m->bf.fp32) cb::launch_nm_keff<float>((float *)m->bf.band, m->bf.ld, m->sm, c0, den, N, st);
-        else cb::launch_nm_keff<double>((double *)m->bf.band, m->bf.ld, m->sm, c0, den, N, st);
+        if (refine) {
+            cb::launch_nm_keff<double>(m->band64, m->bf.ld, m->sm, c0, den, N, st);
+            cb::band_copy_to_f32(m->band64, m->bf, st);
+            m->tm.launches += 1;
+        } else if (m->bf.fp32) {
+            cb::launch_nm_keff<float>((float *)m->bf.band, m->bf.ld, m->sm, c0, den, N, st);
+        } else {
+            cb::launch_nm_keff<double>((double *)m->bf.band, m->bf.ld, m->sm, c0, den, N, st);
+        }
         m->tm.launches += 2;
     }
     factor(m);
     solve(m, m->r, m->dd);
+    if (refine) {
+        // iterative refinement: dd += K32^-1 (Reff - K64 dd) until the
+        // correction is below 1e-12 of dd (at most kRefineSteps corrections)
+        for (int it = 0; it < kRefineSteps; ++it) {
+            {
+                PhaseTimer t(m, &m->tm.ms_vector);
+                cb::band_residual64(m->band64, m->bf.ld, m->bf.bw, N, m->r, m->dd, m->ref_r, m->ref_w, st);
+                m->tm.launches += 2;
+            }
+            solve(m, m->ref_r, m->ref_x);
+            {
+                PhaseTimer t(m, &m->tm.ms_vector);
+                cb::launch_axpy(m->ref_x, 1.0, m->dd, N, st);
+                m->tm.launches += 1;
+            }
+            const double cx = device_dot(m, m->ref_x, nullptr), xx = device_dot(m, m->dd, nullptr);
+            if (!(cx > 1e-24 * xx)) break;
+        }
+    }
     std::swap(m->fcur, m->fprev);  // f_ip = f_temp
     {
         PhaseTimer t(m, &m->tm.ms_vector);

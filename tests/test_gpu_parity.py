@@ -119,3 +119,23 @@ def test_status_codes_and_errors():
     with pytest.raises(cubens.CubensError) as e:
         cubens.Model("2\n1\n0\n1\n2\n1,0,0,0,0\n")
     assert e.value.code in (2, 4)
+
+
+def test_benchmark_panel64_matches_oracle():
+    """The benchmark workload itself (64x64 panel, NEQ 24,960): the FP64 path
+    against the oracle for the first increment and four arc-length steps,
+    and the mixed path's curve against it (1e-5 on lambda at the same
+    control displacement is the mixed path's tolerance)."""
+    import bench
+    text, _ = bench.panel_text(64)
+    steps = 5
+    o = oracle.OracleModel(text).msal(steps)
+    assert o["rc"] == steps, o["error"]
+    g = cubens.Model(text, precision=cubens.FP64).run(steps)
+    np.testing.assert_array_equal(g["its"], o["its"])
+    assert _rel(g["lam"], o["lam"]) < 1e-6
+    for k in range(steps):
+        assert np.linalg.norm(g["d"][k] - o["d"][k]) / np.linalg.norm(o["d"][k]) < 1e-6
+    mx = cubens.Model(text, precision=cubens.MIXED).run(steps)
+    np.testing.assert_array_equal(mx["its"], o["its"])
+    assert _rel(mx["lam"], o["lam"]) < 1e-5
