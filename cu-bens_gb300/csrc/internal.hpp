@@ -57,6 +57,21 @@ struct GatherMap {
 void build_force_map(const HostModel &m, GatherMap &g);
 void build_tangent_map(const HostModel &m, long ld, GatherMap &g);
 
+// Compressed sparse rows of the symmetric tangent, both triangles.
+struct CsrPattern {
+    std::vector<int> rowptr;  // n+1
+    std::vector<int> col;     // nnz, ascending within a row
+    std::vector<int> diag;    // n: slot of (i, i)
+};
+// Pattern of the assembled tangent and its gather map: g lists each lower
+// pair's contributions (same order as the band map, so the sums are the
+// band's values bit for bit) and writes them to g.dst (the pair) and dst2
+// (its mirror, -1 on the diagonal).
+void build_csr_tangent(const HostModel &m, CsrPattern &p, GatherMap &g, std::vector<int64_t> &dst2);
+// Block-Jacobi blocks: start[b] .. start[b+1] are the equations of block b
+// (one joint's equations, at most 8).
+void build_node_blocks(const HostModel &m, std::vector<int> &start);
+
 // ---------------------------------------------------------------------------
 // Device buffers
 // ---------------------------------------------------------------------------
@@ -167,6 +182,85 @@ void band_solve_with_work(const BandFactor &f, const double *rhs, double *x, voi
 // Solve K x = rhs with the factor (rhs, x: FP64 device vectors of length n).
 void band_solve(BandFactor &f, const double *rhs, double *x, cudaStream_t st, bool use_graph,
                 long *launches);
+
+// ---------------------------------------------------------------------------
+// Krylov solve (krylov.cu): restarted flexible GMRES, right-preconditioned,
+// classical Gram-Schmidt applied twice, with a nodal block-Jacobi
+// preconditioner over a CSR sparse matrix-vector product. The Arnoldi
+// process, the Givens rotations and the restarts run on the device; the
+// host replays a captured chunk of Arnoldi steps and reads a status word.
+// ---------------------------------------------------------------------------
+constexpr int kMaxRestart = 64;
+
+struct KrylovCtl {
+    int j;        // current Arnoldi column
+    int done;     // the solve has ended (converged or gave up)
+    int finish;   // the current cycle ends with this step
+    int conv;     // the residual estimate met the tolerance
+    int iters;    // Arnoldi steps of this solve
+    int restarts;
+    int status;   // 0 converged, 1 iteration limit, 2 breakdown to a non-finite value
+    int ncols;    // columns of the finished cycle
+    int m, maxit;
+    double rtol, tol_abs, bnorm, beta, scale, resid;
+    double hp[kMaxRestart + 1];    // coefficients of the current Gram-Schmidt pass
+    double hcol[kMaxRestart + 1];  // Hessenberg column being formed
+    double H[kMaxRestart * (kMaxRestart + 1)];  // rotated Hessenberg, column j at H[j*(m+1)]
+    double cs[kMaxRestart], sn[kMaxRestart], g[kMaxRestart + 1], y[kMaxRestart];
+};
+
+// Preconditioner applied inside the Arnoldi step: z = P(w * scale), with
+// v_j = w * scale stored as the basis vector.
+enum class KrylovPrecond { block_jacobi, learned };
+
+struct KrylovSolver {
+    long n = 0, nnz = 0;
+    int m = 50, maxit = 2000;
+    double rtol = 1e-12;
+    bool fp32_precond = false;   // block inverses in FP32 (mixed precision)
+    int nred = 148;              // reduction blocks (fixed: bit-reproducible sums)
+    int rows_per_red = 0;
+    // matrix (FP64, both triangles)
+    int *rowptr = nullptr, *col = nullptr, *diag = nullptr;
+    double *val = nullptr;
+    // assembly map (lower pairs -> CSR slots)
+    int *amap_ptr = nullptr, *amap_src = nullptr;
+    int64_t *amap_dst = nullptr, *amap_dst2 = nullptr;
+    long amap_n = 0;
+    // block-Jacobi
+    long nblk = 0;
+    int *blk_start = nullptr, *blk_off = nullptr, *row_blk = nullptr;
+    void *binv = nullptr;        // per block its bs x bs inverse, row-major
+    long binv_n = 0;
+    // Krylov work
+    double *V = nullptr, *Z = nullptr, *w = nullptr, *b = nullptr, *x = nullptr, *partial = nullptr;
+    KrylovCtl *ctl = nullptr;
+    KrylovCtl *ctl_h = nullptr;  // pinned host copy (the header up to hp is read per chunk)
+    int chunk = 8;               // Arnoldi steps per graph replay
+    cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+    size_t bytes = 0;
+    // learned preconditioner hook (filled by the MPNN module)
+    void *mpnn = nullptr;
+    // statistics
+    long iterations_total = 0, solves = 0, unconverged = 0;
+    int last_iters = 0;
+    double last_resid = 0;
+};
+
+void krylov_alloc(KrylovSolver &ks, const HostModel &h, int restart, int maxit, bool fp32_precond,
+                  cudaStream_t st);
+void krylov_free(KrylovSolver &ks);
+// tangent values from the element matrices (FP64) into the CSR matrix
+void krylov_assemble(KrylovSolver &ks, const double *kel, cudaStream_t st);
+// Keff diagonal: val[diag[i]] += c0 sm[i] / den (the band's nm_keff arithmetic)
+void krylov_shift_diag(KrylovSolver &ks, const double *sm, double c0, double den, cudaStream_t st);
+// invert the nodal blocks of the current matrix
+void krylov_setup_block_jacobi(KrylovSolver &ks, cudaStream_t st);
+// Solve A x = b to rtol (relative to |b|); returns the Arnoldi steps taken.
+int krylov_solve(KrylovSolver &ks, const double *b, double *x, cudaStream_t st, bool use_graph,
+                 KrylovPrecond pc, long *launches);
+// y = A x (one CSR product; isolated timing)
+void krylov_spmv(const KrylovSolver &ks, const double *x, double *y, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Kernel entry points (host wrappers)

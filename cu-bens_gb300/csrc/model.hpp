@@ -60,7 +60,8 @@ struct cb_model {
     int *tmap_ptr = nullptr, *tmap_src = nullptr;
     int64_t *tmap_dst = nullptr;
     long tmap_n = 0;
-    cb::BandFactor bf;
+    cb::BandFactor bf;           // band LDL^T (CB_SOLVER_BAND)
+    cb::KrylovSolver *ks = nullptr;  // FGMRES (CB_SOLVER_FGMRES)
     cb::MsalScalars *sc = nullptr, *sc_h = nullptr;
     double *partial = nullptr;
 

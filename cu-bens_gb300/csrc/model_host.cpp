@@ -411,68 +411,135 @@ void build_force_map(const HostModel &m, GatherMap &g)
 // packed upper triangle (row-major).
 static inline int packed(int ie, int je, int nd) { return ie * nd - ie * (ie - 1) / 2 + (je - ie); }
 
-// Tangent map. Element matrices are packed upper triangles, shells at
-// [p*E + e] (p < 171), trusses at 171E + [p*T + e] (p < 21), frames at
-// 171E + 21T + [p*F + e] (p < 105). For a local pair
-// (ie <= je) the global slot is (max(i,j), min(i,j)) of the lower band,
-// L[col*ld + (row-col)], and the value used is K[ie][je], as the reference
-// adds K[ie][je] for ie <= je into its skyline (truss.c:170-193,
-// frame.c:328-344, shell.c:307-329). Lists are sorted by (slot; truss,
-// frame, shell; element), the order stiff_tr, stiff_fr, stiff_sh add them.
-void build_tangent_map(const HostModel &m, long ld, GatherMap &g)
+// Tangent contributions. Element matrices are packed upper triangles,
+// shells at [p*E + e] (p < 171), trusses at 171E + [p*T + e] (p < 21),
+// frames at 171E + 21T + [p*F + e] (p < 105). A local pair (ie <= je) adds
+// K[ie][je] to the global pair (max(i,j), min(i,j)) of the lower triangle,
+// as the reference adds K[ie][je] for ie <= je into its skyline
+// (truss.c:170-193, frame.c:328-344, shell.c:307-329). Pairs come out in the
+// order stiff_tr, stiff_fr, stiff_sh add them (truss, frame, shell; element).
+namespace {
+struct TangentPair {
+    long r, c;  // 0-based, r >= c
+    int src;
+};
+
+void collect_tangent_pairs(const HostModel &m, std::vector<TangentPair> &all)
 {
     const long E = m.ne_sh, T = m.ne_tr, F = m.ne_fr;
-    struct C {
-        int64_t slot;
-        int src;
-    };
-    std::vector<C> all;
+    all.clear();
     all.reserve((size_t)(171 * E + 21 * T + 105 * F));
+    auto add = [&](const long *mc, int ie, int je, int src) {
+        if (!mc[ie] || !mc[je]) return;
+        all.push_back({std::max(mc[ie], mc[je]) - 1, std::min(mc[ie], mc[je]) - 1, src});
+    };
     for (long e = 0; e < T; ++e) {
         long mc[6];
         for (int a = 0; a < 2; ++a)
             for (int d = 0; d < 3; ++d) mc[a * 3 + d] = m.jcode[m.tr_conn[e * 2 + a] * 7 + d];
         for (int je = 0; je < 6; ++je)
-            for (int ie = 0; ie <= je; ++ie) {
-                if (!mc[ie] || !mc[je]) continue;
-                long r = std::max(mc[ie], mc[je]) - 1, c = std::min(mc[ie], mc[je]) - 1;
-                all.push_back({(int64_t)c * ld + (r - c), (int)(171 * E + packed(ie, je, 6) * T + e)});
-            }
+            for (int ie = 0; ie <= je; ++ie) add(mc, ie, je, (int)(171 * E + packed(ie, je, 6) * T + e));
     }
     for (long e = 0; e < F; ++e) {
         const long *mc = &m.fr_mc[e * 14];
         for (int je = 0; je < 14; ++je)
-            for (int ie = 0; ie <= je; ++ie) {
-                if (!mc[ie] || !mc[je]) continue;
-                long r = std::max(mc[ie], mc[je]) - 1, c = std::min(mc[ie], mc[je]) - 1;
-                all.push_back({(int64_t)c * ld + (r - c), (int)(171 * E + 21 * T + packed(ie, je, 14) * F + e)});
-            }
+            for (int ie = 0; ie <= je; ++ie)
+                add(mc, ie, je, (int)(171 * E + 21 * T + packed(ie, je, 14) * F + e));
     }
     for (long e = 0; e < E; ++e) {
         long mc[18];
         for (int a = 0; a < 3; ++a)
             for (int d = 0; d < 6; ++d) mc[a * 6 + d] = m.jcode[m.sh_conn[e * 3 + a] * 7 + d];
         for (int je = 0; je < 18; ++je)
-            for (int ie = 0; ie <= je; ++ie) {
-                if (!mc[ie] || !mc[je]) continue;
-                long r = std::max(mc[ie], mc[je]) - 1, c = std::min(mc[ie], mc[je]) - 1;
-                all.push_back({(int64_t)c * ld + (r - c), (int)(packed(ie, je, 18) * E + e)});
-            }
+            for (int ie = 0; ie <= je; ++ie) add(mc, ie, je, (int)(packed(ie, je, 18) * E + e));
     }
-    // stable sort keeps (truss, frame, shell; element order) within a slot
-    std::stable_sort(all.begin(), all.end(), [](const C &a, const C &b) { return a.slot < b.slot; });
+}
+
+// Groups contributions by key (stable, so each list keeps the order above).
+template <typename Key>
+void group_pairs(std::vector<TangentPair> &all, Key key, GatherMap &g, std::vector<int64_t> &keys)
+{
+    std::stable_sort(all.begin(), all.end(),
+                     [&](const TangentPair &a, const TangentPair &b) { return key(a) < key(b); });
     g.ptr.clear();
     g.src.clear();
-    g.dst.clear();
+    keys.clear();
     g.ptr.push_back(0);
     for (size_t k = 0; k < all.size(); ++k) {
-        if (k == 0 || all[k].slot != all[k - 1].slot) {
+        if (k == 0 || key(all[k]) != key(all[k - 1])) {
             if (k) g.ptr.push_back((int)g.src.size());
-            g.dst.push_back(all[k].slot);
+            keys.push_back(key(all[k]));
         }
         g.src.push_back(all[k].src);
     }
     g.ptr.push_back((int)g.src.size());
+}
+}  // namespace
+
+// Band map: one list per lower-band slot L[col*ld + (row-col)].
+void build_tangent_map(const HostModel &m, long ld, GatherMap &g)
+{
+    std::vector<TangentPair> all;
+    collect_tangent_pairs(m, all);
+    group_pairs(all, [ld](const TangentPair &p) { return (int64_t)p.c * ld + (p.r - p.c); }, g, g.dst);
+}
+
+// CSR map: one list per lower pair (r >= c), written to the CSR slot of
+// (r, c) (dst) and of its mirror (c, r) (dst2, -1 on the diagonal). The
+// pattern holds both triangles, columns ascending in each row.
+void build_csr_tangent(const HostModel &m, CsrPattern &p, GatherMap &g, std::vector<int64_t> &dst2)
+{
+    const long n = m.neq;
+    std::vector<TangentPair> all;
+    collect_tangent_pairs(m, all);
+    std::vector<int64_t> keys;
+    group_pairs(all, [n](const TangentPair &q) { return (int64_t)q.r * n + q.c; }, g, keys);
+    // row lists: lower columns from the pairs, upper columns from the mirrors
+    std::vector<std::vector<int>> cols(n);
+    for (int64_t k : keys) {
+        long r = (long)(k / n), c = (long)(k % n);
+        cols[r].push_back((int)c);
+        if (r != c) cols[c].push_back((int)r);
+    }
+    p.rowptr.assign(n + 1, 0);
+    p.col.clear();
+    p.diag.assign(n, -1);
+    for (long i = 0; i < n; ++i) {
+        std::sort(cols[i].begin(), cols[i].end());
+        for (int c : cols[i]) {
+            if (c == i) p.diag[i] = (int)p.col.size();
+            p.col.push_back(c);
+        }
+        p.rowptr[i + 1] = (int)p.col.size();
+    }
+    auto slot = [&](long r, long c) -> int64_t {
+        auto b = p.col.begin() + p.rowptr[r], e = p.col.begin() + p.rowptr[r + 1];
+        return (int64_t)(std::lower_bound(b, e, (int)c) - p.col.begin());
+    };
+    g.dst.resize(keys.size());
+    dst2.resize(keys.size());
+    for (size_t k = 0; k < keys.size(); ++k) {
+        long r = (long)(keys[k] / n), c = (long)(keys[k] % n);
+        g.dst[k] = slot(r, c);
+        dst2[k] = r == c ? -1 : slot(c, r);
+    }
+}
+
+// Nodal blocks of consecutive equations for block-Jacobi: the equations of
+// one joint (jcode, at most 7) form a block; an equation no joint owns (a
+// member-end warping DOF) is a block of its own.
+void build_node_blocks(const HostModel &m, std::vector<int> &start)
+{
+    std::vector<long> owner(m.neq, -1);
+    for (long i = 0; i < m.nj; ++i)
+        for (int d = 0; d < 7; ++d)
+            if (m.jcode[i * 7 + d] > 0) owner[m.jcode[i * 7 + d] - 1] = i;
+    start.clear();
+    for (long q = 0; q < m.neq; ++q) {
+        bool fresh = q == 0 || owner[q] < 0 || owner[q] != owner[q - 1] || q - start.back() >= 8;
+        if (fresh) start.push_back((int)q);
+    }
+    start.push_back((int)m.neq);
 }
 
 }  // namespace cb

@@ -165,6 +165,20 @@ void upload_model(cb_model *m)
     h2d(m->fmap_ptr, fm.ptr.data(), fm.ptr.size(), st);
     h2d(m->fmap_src, fm.src.data(), fm.src.size(), st);
     const bool fp32 = m->opt.precision == CB_MIXED;
+    if (m->opt.solver == CB_SOLVER_FGMRES) {
+        // FP64 matrix and Krylov vectors; mixed precision stores the
+        // preconditioner in FP32
+        m->ks = new cb::KrylovSolver();
+        cb::krylov_alloc(*m->ks, h, m->opt.krylov_restart, m->opt.krylov_maxit, fp32, st);
+        m->bytes += m->ks->bytes;
+        m->kel = m->alloc<double>(171 * E + 21 * T + 105 * F);
+        m->sc = m->alloc<cb::MsalScalars>(1);
+        m->partial = m->alloc<double>(16 * cb::kRedBlocks);
+        CB_CUDA(cudaMallocHost(&m->sc_h, sizeof(cb::MsalScalars)));
+        std::memset(m->sc_h, 0, sizeof(cb::MsalScalars));
+        CB_CUDA(cudaStreamSynchronize(st));
+        return;
+    }
     // Newmark refactors every iteration and solves once per factorisation:
     // direct substitution, no solve blocks
     cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5);
@@ -322,8 +336,8 @@ cb::MsalScalars &pull_scalars(cb_model *m)
 {
     d2h(m->sc_h, m->sc, 1, m->st);
     cb::GridBarrier bar[2]{};
-    d2h(&bar[0], m->bf.bar, 1, m->st);
-    d2h(&bar[1], m->bf.fbar, 1, m->st);
+    if (m->bf.bar) d2h(&bar[0], m->bf.bar, 1, m->st);
+    if (m->bf.fbar) d2h(&bar[1], m->bf.fbar, 1, m->st);
     CB_CUDA(cudaStreamSynchronize(m->st));
     if (bar[0].err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier of the solve timed out");
     if (bar[1].err) throw cb_status_error(CB_ERR_TIMEOUT, "a grid barrier of the factorisation timed out");
@@ -644,6 +658,22 @@ int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb
         *out = m;
         return CB_ERR_UNSUPPORTED;
     }
+    if (m->opt.solver != CB_SOLVER_BAND && m->opt.solver != CB_SOLVER_FGMRES) {
+        m->err = "unknown solver";
+        *out = m;
+        return CB_ERR_ARG;
+    }
+    if (m->opt.solver == CB_SOLVER_FGMRES && m->h.alg != 5) {
+        m->err = "the FGMRES solver serves the nonlinear Newmark driver; MSAL needs the pivots of a "
+                 "factorisation (det, ssd)";
+        *out = m;
+        return CB_ERR_UNSUPPORTED;
+    }
+    if (m->opt.precond != CB_PRECOND_BLOCK_JACOBI && m->opt.precond != CB_PRECOND_LEARNED) {
+        m->err = "unknown preconditioner";
+        *out = m;
+        return CB_ERR_ARG;
+    }
     int rc = guarded(m, [&] {
         int ndev = 0;
         CB_CUDA(cudaGetDeviceCount(&ndev));
@@ -663,6 +693,10 @@ int cb_model_destroy(cb_model *m)
     if (!m) return CB_ERR_ARG;
     if (m->st) cudaStreamSynchronize(m->st);
     cb::band_free(m->bf);
+    if (m->ks) {
+        cb::krylov_free(*m->ks);
+        delete m->ks;
+    }
     for (void *p : m->allocs) cudaFree(p);
     if (m->sc_h) cudaFreeHost(m->sc_h);
     for (auto &e : m->ev)
@@ -692,6 +726,9 @@ int cb_model_info(const cb_model *m, cb_info *info)
     info->algflag = m->h.alg;
     info->nsteps = m->h.nsteps;
     info->dt = m->h.dt;
+    info->solver = m->ks ? CB_SOLVER_FGMRES : CB_SOLVER_BAND;
+    info->nnz = m->ks ? m->ks->nnz : 0;
+    info->node_blocks = m->ks ? m->ks->nblk : 0;
     return CB_OK;
 }
 
@@ -794,6 +831,12 @@ int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch, d
                       double *flops_per_launch)
 {
     if (!m || reps <= 0 || !ms_per_launch) return CB_ERR_ARG;
+    const bool band_kernel = which == CB_K_SOLVE || which == CB_K_FACTOR || which == CB_K_BAND_LDLT ||
+                             which == CB_K_SOLVE_BLOCKS;
+    if ((band_kernel && !m->bf.band) || (which == CB_K_SPMV && !m->ks)) {
+        m->err = "the kernel belongs to the other solver";
+        return CB_ERR_UNSUPPORTED;
+    }
     return guarded(m, [&] {
         cudaStream_t st = m->st;
         const cb::BandFactor &bf = m->bf;
@@ -812,6 +855,7 @@ int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch, d
                 cb::launch_frame_forces(m->fr, m->x_t, m->dd, m->fr_lref,
                                         m->fe + 18 * E + 6 * m->h.ne_tr, m->h.ne_fr, st);
                 break;
+            case CB_K_SPMV: cb::krylov_spmv(*m->ks, m->q, m->ddr, st); break;
             default: throw cb_status_error(CB_ERR_ARG, "unknown kernel id");
             }
         };
@@ -843,6 +887,10 @@ int cb_profile_kernel(cb_model *m, int which, int reps, double *ms_per_launch, d
         case CB_K_FRAME_FORCE:  // per member ~500 B read, ~300 B written, ~1.2 kFLOP
             bytes = (double)m->h.ne_fr * 800;
             flops = (double)m->h.ne_fr * 1200;
+            break;
+        case CB_K_SPMV:  // values 8 B + column 4 B per entry, row pointers, x once, y written
+            bytes = 12.0 * (double)m->ks->nnz + 4.0 * (n + 1) + 16.0 * n;
+            flops = 2.0 * (double)m->ks->nnz;
             break;
         default: throw cb_status_error(CB_ERR_ARG, "unknown kernel id");
         }
@@ -909,6 +957,10 @@ int cb_eval_tangent(cb_model *m, const double *x, const double *c_sh, const doub
     if (!m || !x || !ss) return CB_ERR_ARG;
     const long E = m->h.ne_sh, T = m->h.ne_tr, N = m->h.neq;
     if ((E && (!c_sh || !area_sh)) || (T && !ef_tr)) return CB_ERR_ARG;
+    if (!m->bf.band) {
+        m->err = "this entry point works on the band LDL^T; the handle uses the FGMRES solver";
+        return CB_ERR_UNSUPPORTED;
+    }
     return guarded(m, [&] {
         cudaStream_t st = m->st;
         h2d(m->x_c, x, m->h.nj * 3, st);
@@ -961,6 +1013,10 @@ int cb_factor_solve(cb_model *m, const double *rhs, double *v, double *ssd, int 
 {
     if (!m || !rhs || !v) return CB_ERR_ARG;
     const long N = m->h.neq;
+    if (!m->bf.band) {
+        m->err = "this entry point works on the band LDL^T; the handle uses the FGMRES solver";
+        return CB_ERR_UNSUPPORTED;
+    }
     return guarded(m, [&] {
         cudaStream_t st = m->st;
         factor(m);

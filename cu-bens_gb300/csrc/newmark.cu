@@ -84,6 +84,23 @@ void newmark_begin(cb_model *m)
     m->nm_phase = 1;
 }
 
+// Keff dd = Reff with FGMRES: the preconditioner from the current matrix,
+// then the solve (m->r -> m->dd).
+void krylov_newmark_solve(cb_model *m)
+{
+    cb::KrylovSolver &ks = *m->ks;
+    {
+        PhaseTimer t(m, &m->tm.ms_factor);
+        cb::krylov_setup_block_jacobi(ks, m->st);
+        m->tm.launches += 1;
+        m->tm.factorizations++;
+    }
+    PhaseTimer t(m, &m->tm.ms_solve);
+    cb::krylov_solve(ks, m->r, m->dd, m->st, m->opt.use_graphs != 0, cb::KrylovPrecond::block_jacobi,
+                     &m->tm.launches);
+    m->tm.solves++;
+}
+
 // one Newton iteration of main.c:3543-3745; returns the scalar block
 cb::MsalScalars &newmark_iteration(cb_model *m, const NewmarkParams &p, long k, double sub_dt, double lpf,
                                    int itecnt, double a0, double a2, double a3, double a6, double a7)
@@ -94,8 +111,16 @@ cb::MsalScalars &newmark_iteration(cb_model *m, const NewmarkParams &p, long k, 
     // tangent of the previous iteration's state with llength_temp as it
     // stands, then the mass at the converged coordinates, which rewrites
     // llength_temp (mass_fr, frame.c:1339)
-    const bool refine = m->bf.fp32;
-    if (refine) {
+    cb::KrylovSolver *ks = m->ks;
+    const bool refine = !ks && m->bf.fp32;
+    if (ks) {
+        // FGMRES: FP64 tangent into the CSR matrix
+        PhaseTimer t(m, &m->tm.ms_tangent);
+        const cb::DevFrame &fr = m->fr;
+        cb::launch_frame_tangent<double>(fr, fr.c_ip, fr.ef_ip, fr.len_ip, m->fr_lref, (double *)m->kel, F, st);
+        cb::krylov_assemble(*ks, (const double *)m->kel, st);
+        m->tm.launches += 2;
+    } else if (refine) {
         // mixed: the effective stiffness is assembled in FP64 and kept; its
         // FP32 copy is factored and the solve refined against it
         PhaseTimer t(m, &m->tm.ms_tangent);
@@ -121,7 +146,9 @@ cb::MsalScalars &newmark_iteration(cb_model *m, const NewmarkParams &p, long k, 
         cb::launch_nm_reff(mode, sub_dt, lpf, p.alpham, p.alphaf, a2, a3, pin_km1, pin_k, m->fcur, m->sm, m->vc_i,
                            m->ac_i, m->qtot, m->r, N, st);
         const double c0 = a0 * (1 - p.alpham), den = 1 - p.alphaf;
-        if (refine) {
+        if (ks) {
+            cb::krylov_shift_diag(*ks, m->sm, c0, den, st);
+        } else if (refine) {
             cb::launch_nm_keff<double>(m->band64, m->bf.ld, m->sm, c0, den, N, st);
             cb::band_copy_to_f32(m->band64, m->bf, st);
             m->tm.launches += 1;
@@ -132,8 +159,12 @@ cb::MsalScalars &newmark_iteration(cb_model *m, const NewmarkParams &p, long k, 
         }
         m->tm.launches += 2;
     }
-    factor(m);
-    solve(m, m->r, m->dd);
+    if (ks) {
+        krylov_newmark_solve(m);
+    } else {
+        factor(m);
+        solve(m, m->r, m->dd);
+    }
     if (refine) {
         // iterative refinement: dd += K32^-1 (Reff - K64 dd) until the
         // correction is below 1e-12 of dd (at most kRefineSteps corrections)
@@ -311,6 +342,31 @@ int cb_newmark_step(cb_model *m, cb_step *out)
     return guarded(m, [&] { newmark_step(m, out); });
 }
 
+int cb_set_krylov_tolerance(cb_model *m, double rtol)
+{
+    if (!m || !(rtol > 0) || !(rtol < 1)) return CB_ERR_ARG;
+    if (!m->ks) {
+        m->err = "the handle does not use the FGMRES solver";
+        return CB_ERR_STATE;
+    }
+    m->ks->rtol = rtol;
+    return CB_OK;
+}
+
+int cb_get_krylov_stats(const cb_model *m, cb_krylov_stats *s)
+{
+    if (!m || !s) return CB_ERR_ARG;
+    std::memset(s, 0, sizeof *s);
+    if (!m->ks) return CB_OK;
+    const cb::KrylovSolver &ks = *m->ks;
+    s->solves = ks.solves;
+    s->iterations = ks.iterations_total;
+    s->unconverged = ks.unconverged;
+    s->last_iterations = ks.last_iters;
+    s->last_residual = ks.last_resid;
+    return CB_OK;
+}
+
 int cb_newmark_state(const cb_model *m, double *u, double *v, double *a)
 {
     if (!m || m->h.alg != 5) return CB_ERR_ARG;
@@ -361,6 +417,10 @@ int cb_eval_frame_tangent(cb_model *m, const double *c, const double *ef, const 
                           long *maxa, double *ss)
 {
     if (!m || !c || !ef || !len || !lref || !ss) return CB_ERR_ARG;
+    if (!m->bf.band) {
+        m->err = "this entry point works on the band LDL^T; the handle uses the FGMRES solver";
+        return CB_ERR_UNSUPPORTED;
+    }
     const long F = m->h.ne_fr, N = m->h.neq;
     if (F == 0 || m->h.ne_tr || m->h.ne_sh) {
         m->err = "cb_eval_frame_tangent needs a frame-only model";

@@ -25,7 +25,10 @@ STATUS = {0: "ok", 1: "bad argument", 2: "parse error", 3: "CUDA error", 4: "uns
 FP64 = 0
 MIXED = 1
 
-K_SOLVE, K_SHELL_FORCE, K_FACTOR, K_BAND_LDLT, K_SOLVE_BLOCKS, K_FRAME_FORCE = range(6)
+K_SOLVE, K_SHELL_FORCE, K_FACTOR, K_BAND_LDLT, K_SOLVE_BLOCKS, K_FRAME_FORCE, K_SPMV = range(7)
+
+SOLVER_BAND, SOLVER_FGMRES = 0, 1
+PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
 
 
 class CubensError(RuntimeError):
@@ -36,14 +39,16 @@ class CubensError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("use_graphs", C.c_int),
-                ("reserved", C.c_int * 5)]
+                ("solver", C.c_int), ("krylov_restart", C.c_int), ("krylov_maxit", C.c_int),
+                ("precond", C.c_int), ("reserved", C.c_int * 1)]
 
 
 class Info(C.Structure):
     _fields_ = [("nj", C.c_long), ("ne_tr", C.c_long), ("ne_fr", C.c_long), ("ne_sh", C.c_long),
                 ("neq", C.c_long), ("lss", C.c_long), ("bandwidth", C.c_long), ("block", C.c_long),
                 ("nblocks", C.c_long), ("dkdof", C.c_long), ("device_bytes", C.c_size_t),
-                ("h2d_bytes", C.c_size_t), ("algflag", C.c_int), ("nsteps", C.c_long), ("dt", C.c_double)]
+                ("h2d_bytes", C.c_size_t), ("algflag", C.c_int), ("nsteps", C.c_long), ("dt", C.c_double),
+                ("solver", C.c_int), ("nnz", C.c_long), ("node_blocks", C.c_long)]
 
 
 class Step(C.Structure):
@@ -55,6 +60,12 @@ class Timers(C.Structure):
     _fields_ = [("ms_tangent", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double),
                 ("ms_force", C.c_double), ("ms_vector", C.c_double), ("launches", C.c_long),
                 ("solves", C.c_long), ("factorizations", C.c_long), ("force_evals", C.c_long)]
+
+
+class KrylovStats(C.Structure):
+    _fields_ = [("solves", C.c_long), ("iterations", C.c_long), ("unconverged", C.c_long),
+                ("last_iterations", C.c_int), ("last_residual", C.c_double), ("learned_solves", C.c_long),
+                ("fallbacks", C.c_long), ("train_steps", C.c_long), ("train_loss", C.c_double)]
 
 
 _lib = None
@@ -100,6 +111,8 @@ def load(path: Path | None = None):
     L.cb_eval_frame_forces.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
     L.cb_eval_frame_tangent.argtypes = [vp, dp, dp, dp, dp, lp, dp]
     L.cb_eval_frame_mass.argtypes = [vp, dp, dp, dp]
+    L.cb_set_krylov_tolerance.argtypes = [vp, C.c_double]
+    L.cb_get_krylov_stats.argtypes = [vp, C.POINTER(KrylovStats)]
     _lib = L
     return L
 
@@ -143,13 +156,19 @@ class StepResult:
 class Model:
     """A model_def uploaded to the GPU, with its MSAL state (resident API)."""
 
-    def __init__(self, model_def: str, precision: int = FP64, device: int = 0, use_graphs: bool = True):
+    def __init__(self, model_def: str, precision: int = FP64, device: int = 0, use_graphs: bool = True,
+                 solver: int = SOLVER_BAND, restart: int = 0, maxit: int = 0,
+                 precond: int = PRECOND_BLOCK_JACOBI, rtol: float | None = None):
         L = load()
         opt = Options()
         L.cb_default_options(C.byref(opt))
         opt.precision = precision
         opt.device = device
         opt.use_graphs = 1 if use_graphs else 0
+        opt.solver = solver
+        opt.krylov_restart = restart
+        opt.krylov_maxit = maxit
+        opt.precond = precond
         h = C.c_void_p()
         raw = model_def.encode()
         rc = L.cb_model_create(raw, len(raw), C.byref(opt), C.byref(h))
@@ -163,6 +182,8 @@ class Model:
         self.info = {k: getattr(inf, k) for k, _ in Info._fields_}
         self.neq = inf.neq
         self.nj, self.ne_tr, self.ne_fr, self.ne_sh = inf.nj, inf.ne_tr, inf.ne_fr, inf.ne_sh
+        if rtol is not None:
+            self._check(L.cb_set_krylov_tolerance(self.h, rtol))
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:
@@ -306,6 +327,11 @@ class Model:
         ms, by, fl = C.c_double(), C.c_double(), C.c_double()
         self._check(load().cb_profile_kernel(self.h, which, reps, C.byref(ms), C.byref(by), C.byref(fl)))
         return ms.value, by.value, fl.value
+
+    def krylov_stats(self) -> dict:
+        s = KrylovStats()
+        self._check(load().cb_get_krylov_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in KrylovStats._fields_}
 
     def timers(self) -> dict:
         t = Timers()

@@ -50,11 +50,31 @@ enum cb_precision {
     CB_MIXED = 1   /* FP32 tangent and FP32 LDL^T; the modified-Newton loop refines in FP64 */
 };
 
+/* Linear solver of the equilibrium iterations. */
+enum cb_solver {
+    CB_SOLVER_BAND = 0,   /* band LDL^T in the reference's equation order (skyfact/skysolve's
+                             result; pivots give det and ssd) */
+    CB_SOLVER_FGMRES = 1  /* FGMRES(m) with a nodal block-Jacobi preconditioner over a CSR
+                             product (nonlinear Newmark only: MSAL needs det and ssd) */
+};
+
+/* Preconditioner of the FGMRES solver. */
+enum cb_precond {
+    CB_PRECOND_BLOCK_JACOBI = 0,  /* inverse of each joint's diagonal block */
+    CB_PRECOND_LEARNED = 1        /* mesh message-passing network, trained online on the
+                                     solver's own (residual, correction) pairs; block-Jacobi
+                                     FGMRES takes over whenever it stalls */
+};
+
 typedef struct {
-    int precision;   /* enum cb_precision */
-    int device;      /* CUDA device ordinal */
-    int use_graphs;  /* 1: replay the factor and solve launch sequences as CUDA graphs */
-    int reserved[5];
+    int precision;       /* enum cb_precision */
+    int device;          /* CUDA device ordinal */
+    int use_graphs;      /* 1: replay the factor, solve and Arnoldi launch sequences as CUDA graphs */
+    int solver;          /* enum cb_solver */
+    int krylov_restart;  /* FGMRES restart length m (0: 50; at most 64) */
+    int krylov_maxit;    /* FGMRES steps per solve before it gives up (0: 2000) */
+    int precond;         /* enum cb_precond (FGMRES) */
+    int reserved[1];
 } cb_options;
 
 typedef struct {
@@ -70,6 +90,9 @@ typedef struct {
     int algflag;                   /* 3: MSAL model, 5: nonlinear Newmark model */
     long nsteps;                   /* Newmark: time steps NTSTPS (main.c:3361) */
     double dt;                     /* Newmark: time step */
+    int solver;                    /* enum cb_solver in use */
+    long nnz;                      /* FGMRES: stored entries of the CSR matrix (both triangles) */
+    long node_blocks;              /* FGMRES: block-Jacobi blocks */
 } cb_info;
 
 /* Result of one converged increment or time step (what output() records,
@@ -139,6 +162,22 @@ int cb_newmark_state(const cb_model *m, double *u, double *v, double *a);
 /* Reference load vector q (NEQ) and 1-based equation numbers jcode (NJ*7). */
 int cb_get_topology(const cb_model *m, long *jcode, double *q);
 
+/* FGMRES controls and counters. The tolerance is relative to |b| for each
+ * solve (default 1e-12: the Newton iteration counts of the direct solve). */
+typedef struct {
+    long solves;          /* FGMRES solves since the handle was created */
+    long iterations;      /* Arnoldi steps over those solves */
+    long unconverged;     /* solves that hit krylov_maxit */
+    int last_iterations;  /* Arnoldi steps of the latest solve */
+    double last_residual; /* |b - A x| / |b| estimate of the latest solve */
+    long learned_solves;  /* solves preconditioned by the network */
+    long fallbacks;       /* network solves that stalled and were redone with block-Jacobi */
+    long train_steps;     /* Adam steps taken by the network */
+    double train_loss;    /* latest training loss (relative squared error) */
+} cb_krylov_stats;
+int cb_set_krylov_tolerance(cb_model *m, double rtol);
+int cb_get_krylov_stats(const cb_model *m, cb_krylov_stats *s);
+
 int cb_get_timers(const cb_model *m, cb_timers *t);
 int cb_reset_timers(cb_model *m);
 /* Enable/disable per-phase CUDA-event timing (adds event records). */
@@ -158,7 +197,8 @@ enum cb_kernel_id {
     CB_K_FACTOR = 2,       /* one whole band LDL^T + block inverses (graph replay) */
     CB_K_BAND_LDLT = 3,    /* the persistent band LDL^T kernel alone (refactors the band in place) */
     CB_K_SOLVE_BLOCKS = 4, /* Linv, Pn, Rn of the solve from the current factor */
-    CB_K_FRAME_FORCE = 5   /* the frame internal-force kernel over all members */
+    CB_K_FRAME_FORCE = 5,  /* the frame internal-force kernel over all members */
+    CB_K_SPMV = 6          /* FGMRES: one CSR product y = A x of the current matrix */
 };
 /* Launch kernel `which` reps times back to back between two CUDA events and
  * report the mean milliseconds per launch and the algorithmic bytes and

@@ -85,3 +85,23 @@ def test_unsupported_frame_and_newmark_inputs_are_refused_before_upload(lib):
     truss.insert(2, "0,0")
     rc, msg = _create(lib, ("\n".join(truss) + "\n").encode())
     assert rc == 4 and "frame-only" in msg
+
+
+def test_fgmres_is_refused_for_msal_models_before_upload(lib):
+    """The FGMRES solver serves the Newmark driver; the arc-length loop needs
+    the pivots of a factorisation (det for the load direction, ssd for psi)."""
+    from cubens import models
+    text = models.space_truss(bays=2).text.encode()
+    opt = cubens.Options()
+    lib.cb_default_options(C.byref(opt))
+    opt.solver = cubens.SOLVER_FGMRES
+    h = C.c_void_p()
+    rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
+    msg = lib.cb_last_error(h).decode()
+    lib.cb_model_destroy(h)
+    assert rc == 4 and "det" in msg
+    opt.solver = 7
+    h = C.c_void_p()
+    rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
+    lib.cb_model_destroy(h)
+    assert rc == 1
