@@ -202,6 +202,7 @@ struct KrylovCtl {
     int status;   // 0 converged, 1 iteration limit, 2 breakdown to a non-finite value
     int ncols;    // columns of the finished cycle
     int m, maxit;
+    unsigned arrive[4];  // blocks of the running pass that have finished (last-block reductions)
     double rtol, tol_abs, bnorm, beta, scale, resid;
     double hp[kMaxRestart + 1];    // coefficients of the current Gram-Schmidt pass
     double hcol[kMaxRestart + 1];  // Hessenberg column being formed
@@ -218,8 +219,8 @@ struct KrylovSolver {
     int m = 50, maxit = 2000;
     double rtol = 1e-12;
     bool fp32_precond = false;   // block inverses in FP32 (mixed precision)
-    int nred = 148;              // reduction blocks (fixed: bit-reproducible sums)
-    int rows_per_red = 0;
+    int nred = 0;                // blocks of the Gram-Schmidt passes (fixed per model: reproducible sums)
+    int rows_per_red = 0;        // rows per such block
     // matrix (FP64, both triangles)
     int *rowptr = nullptr, *col = nullptr, *diag = nullptr;
     double *val = nullptr;
@@ -261,6 +262,27 @@ int krylov_solve(KrylovSolver &ks, const double *b, double *x, cudaStream_t st, 
                  KrylovPrecond pc, long *launches);
 // y = A x (one CSR product; isolated timing)
 void krylov_spmv(const KrylovSolver &ks, const double *x, double *y, cudaStream_t st);
+// the learned preconditioner's step inside the Arnoldi sequence (mpnn.cu)
+void krylov_apply_learned(KrylovSolver &ks, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Learned preconditioner (mpnn.cu): a message-passing network on the joint
+// graph, trained online by its own forward, backward and Adam kernels.
+// ---------------------------------------------------------------------------
+struct Mpnn;
+Mpnn *mpnn_create(const HostModel &h, unsigned seed, int capacity, cudaStream_t st);
+void mpnn_destroy(Mpnn *mp);
+long mpnn_param_count();
+size_t mpnn_bytes(const Mpnn *mp);
+long mpnn_adam_steps(const Mpnn *mp);
+double mpnn_last_loss(const Mpnn *mp);
+void mpnn_set_lr(Mpnn *mp, double lr);
+void mpnn_set_params(Mpnn *mp, const float *theta, cudaStream_t st);
+void mpnn_get_params(const Mpnn *mp, float *theta, float *grad, cudaStream_t st);
+double mpnn_eval(Mpnn &mp, const KrylovSolver &ks, const double *r, const double *p, const double *t, double *z,
+                 bool train, cudaStream_t st);
+void mpnn_push_pair(Mpnn &mp, const double *b, const double *t, cudaStream_t st);
+double mpnn_train(Mpnn &mp, const KrylovSolver &ks, int steps, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Kernel entry points (host wrappers)

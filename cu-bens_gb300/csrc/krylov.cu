@@ -178,41 +178,89 @@ __global__ void kry_spmv_kernel(const KrylovCtl *__restrict__ ctl, int mode, con
     if (row < n && lane == 0) y[row] = mode == 1 ? bvec[row] - acc : acc;
 }
 
-// partial[k*nred + blk] = v_k . w over the block's rows, k <= j (one warp per k)
-__device__ void chunk_dots(const KrylovCtl *ctl, const double *V, const double *w, double *partial, long n,
-                           long r0, long r1, int nred)
+// ---- Gram-Schmidt passes. FP64 arithmetic is the scarce resource here, so
+// the dots run one warp per basis vector with the lanes accumulating many
+// rows each (few FP64 adds spent on reductions); the per-block sums are
+// reduced across blocks by the last block to arrive (fixed order, so the
+// sums do not depend on which block that is).
+
+constexpr int kWarps = kKT / 32;
+
+// true in every thread of the last block of the grid to get here
+__device__ bool last_block(unsigned *counter)
 {
-    const int j = ctl->j;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int k = warp; k <= j; k += nw) {
+    __shared__ bool s_last;
+    __threadfence();  // every thread's partial writes before the block's arrival
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last;
+}
+
+// partial[k*nred + blk] = v_k . w over rows [r0, r1), k <= j (one warp per k)
+__device__ void block_dots(const double *__restrict__ V, const double *__restrict__ w, long n, int j, long r0,
+                           long r1, double *__restrict__ partial, int nred)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = warp; k <= j; k += kWarps) {
         const double *v = V + (size_t)k * n;
-        double acc = 0;
-        for (long i = r0 + lane; i < r1; i += 32) acc += v[i] * w[i];
-        acc = warp_sum(acc);
-        if (lane == 0) partial[k * nred + blockIdx.x] = acc;
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        long i = r0 + lane;
+        for (; i + 96 < r1; i += 128) {
+            a0 += v[i] * w[i];
+            a1 += v[i + 32] * w[i + 32];
+            a2 += v[i + 64] * w[i + 64];
+            a3 += v[i + 96] * w[i + 96];
+        }
+        for (; i < r1; i += 32) a0 += v[i] * w[i];
+        const double acc = warp_sum((a0 + a1) + (a2 + a3));
+        if (lane == 0) partial[(size_t)k * nred + blockIdx.x] = acc;
     }
 }
 
-__global__ void kry_dots_kernel(const KrylovCtl *__restrict__ ctl, const double *__restrict__ V,
-                                const double *__restrict__ w, double *__restrict__ partial, long n, int rpr,
-                                int nred)
+// partial[blk] = |w|^2 over rows [r0, r1)
+__device__ void block_norm(const double *__restrict__ w, long r0, long r1, double *__restrict__ partial)
 {
-    if (ctl->done) return;
-    const long r0 = blockIdx.x * (long)rpr, r1 = min(n, r0 + rpr);
-    chunk_dots(ctl, V, w, partial, n, r0, r1, nred);
+    __shared__ double red[kWarps];
+    double acc = 0;
+    for (long i = r0 + threadIdx.x; i < r1; i += blockDim.x) acc += w[i] * w[i];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0;
+        for (int k = 0; k < kWarps; ++k) sum += red[k];
+        partial[blockIdx.x] = sum;
+    }
 }
 
-// hp[k] = sum of the partials (one warp per k); pass 0 starts hcol, pass 1 adds
-__global__ void kry_reduce_kernel(KrylovCtl *__restrict__ ctl, const double *__restrict__ partial, int nred,
-                                  int pass)
+// Sum of partial[0..nred) by one warp in a fixed order: each lane loads its
+// strided values sixteen at a time (independent loads in flight), adds them
+// in index order, then a butterfly across the lanes.
+__device__ __forceinline__ double warp_sum_partials(const double *__restrict__ pk, int nred)
 {
-    if (ctl->done) return;
-    const int j = ctl->j;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int k = warp; k <= j; k += nw) {
-        double acc = 0;
-        for (int b = lane; b < nred; b += 32) acc += partial[k * nred + b];
-        acc = warp_sum(acc);
+    const int lane = threadIdx.x & 31;
+    double acc = 0;
+    for (int b0 = 0; b0 < nred; b0 += 32 * 16) {
+        double v[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const int b = b0 + lane + 32 * u;
+            v[u] = b < nred ? __ldcg(pk + b) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u) acc += v[u];
+    }
+    return warp_sum(acc);
+}
+
+// last block: hp[k] = sum_b partial[k*nred + b] (one warp per k)
+__device__ void reduce_hp(KrylovCtl *ctl, const double *partial, int nred, int j, int pass)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = warp; k <= j; k += kWarps) {
+        const double acc = warp_sum_partials(partial + (size_t)k * nred, nred);
         if (lane == 0) {
             ctl->hp[k] = acc;
             ctl->hcol[k] = pass == 0 ? acc : ctl->hcol[k] + acc;
@@ -220,101 +268,25 @@ __global__ void kry_reduce_kernel(KrylovCtl *__restrict__ ctl, const double *__r
     }
 }
 
-// w -= sum_k hp[k] v_k over the block's rows, then (second) the pass-2 dots
-// or (last) the partial |w|^2.
-__global__ void kry_update_kernel(const KrylovCtl *__restrict__ ctl, const double *__restrict__ V,
-                                  double *__restrict__ w, double *__restrict__ partial, long n, int rpr, int nred,
-                                  int last)
+// last block, warp 0: sum_b partial[b]
+__device__ double reduce_norm(const double *partial, int nred) { return warp_sum_partials(partial, nred); }
+
+// w[i] -= sum_k hp[k] V_k[i] over rows [r0, r1)
+__device__ void block_update(const double *__restrict__ V, double *__restrict__ w, long n, int j, const double *hp,
+                             long r0, long r1)
 {
-    if (ctl->done) return;
-    __shared__ double hp[kMaxRestart + 1];
-    __shared__ double red[kKT / 32];
-    const int j = ctl->j;
-    for (int k = threadIdx.x; k <= j; k += blockDim.x) hp[k] = ctl->hp[k];
-    __syncthreads();
-    const long r0 = blockIdx.x * (long)rpr, r1 = min(n, r0 + rpr);
-    double nrm = 0;
     for (long i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
         double s = w[i];
+#pragma unroll 8
         for (int k = 0; k <= j; ++k) s -= hp[k] * V[(size_t)k * n + i];
         w[i] = s;
-        nrm += s * s;
-    }
-    if (!last) {
-        __syncthreads();
-        chunk_dots(ctl, V, w, partial, n, r0, r1, nred);
-        return;
-    }
-    nrm = warp_sum(nrm);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nrm;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
-        partial[blockIdx.x] = s;
     }
 }
 
-// partial[blk] = |w|^2 over the block's rows. mode 0: always (start of a
-// solve); mode 1: when a cycle ends unconverged (the restart residual).
-__global__ void kry_norm_kernel(const KrylovCtl *__restrict__ ctl, int mode, const double *__restrict__ w,
-                                double *__restrict__ partial, long n, int rpr)
+// Closes Arnoldi step j: h_{j+1,j} = |w|, rotations, residual estimate
+// |g_{j+1}|; at the end of a cycle y = R^-1 g. One thread.
+__device__ void close_step(KrylovCtl *ctl, double ww)
 {
-    if (mode == 1 && (ctl->done || !ctl->finish || ctl->conv)) return;
-    __shared__ double red[kKT / 32];
-    const long r0 = blockIdx.x * (long)rpr, r1 = min(n, r0 + rpr);
-    double s = 0;
-    for (long i = r0 + threadIdx.x; i < r1; i += blockDim.x) s += w[i] * w[i];
-    s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-        partial[blockIdx.x] = t;
-    }
-}
-
-__device__ double sum_partials(const double *partial, int nred)
-{
-    double acc = 0;
-    for (int b = threadIdx.x; b < nred; b += 32) acc += partial[b];
-    return warp_sum(acc);
-}
-
-// start of a solve (one warp): |b| from the partials, the first cycle
-__global__ void kry_start_kernel(KrylovCtl *__restrict__ ctl, const double *__restrict__ partial, int nred,
-                                 int m, int maxit, double rtol)
-{
-    const double bb = sum_partials(partial, nred);
-    if (threadIdx.x != 0) return;
-    const double bn = sqrt(bb);
-    ctl->j = 0;
-    ctl->finish = 0;
-    ctl->conv = 0;
-    ctl->iters = 0;
-    ctl->restarts = 0;
-    ctl->ncols = 0;
-    ctl->m = m;
-    ctl->maxit = maxit;
-    ctl->rtol = rtol;
-    ctl->bnorm = bn;
-    ctl->beta = bn;
-    ctl->resid = bn;
-    ctl->tol_abs = rtol * bn;
-    ctl->g[0] = bn;
-    ctl->scale = bn > 0 ? 1.0 / bn : 0.0;
-    ctl->status = isfinite(bn) ? 0 : 2;
-    ctl->done = (bn == 0 || !isfinite(bn)) ? 1 : 0;
-}
-
-// Closes Arnoldi step j (one warp): h_{j+1,j} = |w|, rotations, residual
-// estimate |g_{j+1}|; at the end of a cycle y = R^-1 g.
-__global__ void kry_close_kernel(KrylovCtl *__restrict__ ctl, const double *__restrict__ partial, int nred)
-{
-    if (ctl->done) return;
-    const double ww = sum_partials(partial, nred);
-    if (threadIdx.x != 0) return;
     const int j = ctl->j, m = ctl->m, ld = m + 1;
     const double hn = sqrt(ww);
     double *Hc = ctl->H + (size_t)j * ld;
@@ -360,6 +332,125 @@ __global__ void kry_close_kernel(KrylovCtl *__restrict__ ctl, const double *__re
     }
 }
 
+struct GsArgs {
+    KrylovCtl *ctl;
+    const double *V;
+    double *w;
+    double *partial;
+    long n;
+    int rpr, nred;
+};
+
+// pass 1: h = V^T w (w = A z_j from the product)
+__global__ void kry_gs_dots_kernel(GsArgs a)
+{
+    KrylovCtl *ctl = a.ctl;
+    if (ctl->done) return;
+    const int j = ctl->j;
+    const long r0 = blockIdx.x * (long)a.rpr, r1 = min(a.n, r0 + a.rpr);
+    block_dots(a.V, a.w, a.n, j, r0, r1, a.partial, a.nred);
+    if (last_block(&ctl->arrive[0])) {
+        reduce_hp(ctl, a.partial, a.nred, j, 0);
+        if (threadIdx.x == 0) ctl->arrive[0] = 0;
+    }
+}
+
+// w -= V h, then pass 2 (last == 0: h2 = V^T w) or the norm and the close of
+// the step (last == 1)
+__global__ void kry_gs_update_kernel(GsArgs a, int last)
+{
+    KrylovCtl *ctl = a.ctl;
+    if (ctl->done) return;
+    __shared__ double hp[kMaxRestart + 1];
+    const int j = ctl->j;
+    for (int k = threadIdx.x; k <= j; k += blockDim.x) hp[k] = ctl->hp[k];
+    __syncthreads();
+    const long r0 = blockIdx.x * (long)a.rpr, r1 = min(a.n, r0 + a.rpr);
+    block_update(a.V, a.w, a.n, j, hp, r0, r1);
+    __syncthreads();
+    if (!last) {
+        block_dots(a.V, a.w, a.n, j, r0, r1, a.partial, a.nred);
+        if (last_block(&ctl->arrive[1])) {
+            reduce_hp(ctl, a.partial, a.nred, j, 1);
+            if (threadIdx.x == 0) ctl->arrive[1] = 0;
+        }
+        return;
+    }
+    block_norm(a.w, r0, r1, a.partial);
+    if (last_block(&ctl->arrive[2])) {
+        if (threadIdx.x < 32) {
+            const double ww = reduce_norm(a.partial, a.nred);
+            if (threadIdx.x == 0) {
+                close_step(ctl, ww);
+                ctl->arrive[2] = 0;
+            }
+        }
+    }
+}
+
+// Start of a solve (mode 0; w = b): |b| and the first cycle. After a
+// finished cycle (mode 1): done when the estimate converged, else restart
+// from the true residual r = b - A x held in w.
+__global__ void kry_norm_start_kernel(GsArgs a, int mode, int m, int maxit, double rtol)
+{
+    KrylovCtl *ctl = a.ctl;
+    if (mode == 1) {
+        if (ctl->done || !ctl->finish) return;
+        if (ctl->conv) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                ctl->status = 0;
+                ctl->done = 1;
+            }
+            return;
+        }
+    }
+    const long r0 = blockIdx.x * (long)a.rpr, r1 = min(a.n, r0 + a.rpr);
+    block_norm(a.w, r0, r1, a.partial);
+    if (!last_block(&ctl->arrive[3])) return;
+    if (threadIdx.x >= 32) return;
+    const double bb = reduce_norm(a.partial, a.nred);
+    if (threadIdx.x != 0) return;
+    ctl->arrive[3] = 0;
+    const double bn = sqrt(bb);
+    if (mode == 0) {
+        ctl->j = 0;
+        ctl->finish = 0;
+        ctl->conv = 0;
+        ctl->iters = 0;
+        ctl->restarts = 0;
+        ctl->ncols = 0;
+        ctl->m = m;
+        ctl->maxit = maxit;
+        ctl->rtol = rtol;
+        ctl->bnorm = bn;
+        ctl->beta = bn;
+        ctl->resid = bn;
+        ctl->tol_abs = rtol * bn;
+        ctl->g[0] = bn;
+        ctl->scale = bn > 0 ? 1.0 / bn : 0.0;
+        ctl->status = isfinite(bn) ? 0 : 2;
+        ctl->done = (bn == 0 || !isfinite(bn)) ? 1 : 0;
+        return;
+    }
+    ctl->resid = bn;
+    ctl->beta = bn;
+    if (bn <= ctl->tol_abs) {
+        ctl->status = 0;
+        ctl->done = 1;
+        return;
+    }
+    if (ctl->iters >= ctl->maxit || !isfinite(bn)) {
+        ctl->status = isfinite(bn) ? 1 : 2;
+        ctl->done = 1;
+        return;
+    }
+    ctl->restarts += 1;
+    ctl->j = 0;
+    ctl->finish = 0;
+    ctl->g[0] = bn;
+    ctl->scale = 1.0 / bn;
+}
+
 // x += Z y at the end of a cycle
 __global__ void kry_xupdate_kernel(const KrylovCtl *__restrict__ ctl, const double *__restrict__ Z,
                                    double *__restrict__ x, long n)
@@ -374,39 +465,6 @@ __global__ void kry_xupdate_kernel(const KrylovCtl *__restrict__ ctl, const doub
     double s = x[i];
     for (int k = 0; k < nc; ++k) s += y[k] * Z[(size_t)k * n + i];
     x[i] = s;
-}
-
-// After a finished cycle: done when the estimate converged, else restart
-// from the true residual r = b - A x (in w, its norm in the partials).
-__global__ void kry_restart_kernel(KrylovCtl *__restrict__ ctl, const double *__restrict__ partial, int nred)
-{
-    if (ctl->done || !ctl->finish) return;
-    const bool conv = ctl->conv != 0;
-    const double rr = conv ? 0.0 : sum_partials(partial, nred);
-    if (threadIdx.x != 0) return;
-    if (conv) {
-        ctl->status = 0;
-        ctl->done = 1;
-        return;
-    }
-    const double beta = sqrt(rr);
-    ctl->resid = beta;
-    ctl->beta = beta;
-    if (beta <= ctl->tol_abs) {
-        ctl->status = 0;
-        ctl->done = 1;
-        return;
-    }
-    if (ctl->iters >= ctl->maxit || !isfinite(beta)) {
-        ctl->status = isfinite(beta) ? 1 : 2;
-        ctl->done = 1;
-        return;
-    }
-    ctl->restarts += 1;
-    ctl->j = 0;
-    ctl->finish = 0;
-    ctl->g[0] = beta;
-    ctl->scale = 1.0 / beta;
 }
 
 inline unsigned nb(long n, int t = kKT) { return (unsigned)((n + t - 1) / t); }
@@ -441,7 +499,16 @@ void krylov_alloc(KrylovSolver &ks, const HostModel &h, int restart, int maxit, 
         for (int q = bstart[b]; q < bstart[b + 1]; ++q) rblk[q] = (int)b;
     }
     ks.binv_n = off[ks.nblk];
-    ks.rows_per_red = (int)((n + ks.nred - 1) / ks.nred);
+    // Gram-Schmidt partition: one block per SM-sized share of the rows (at
+    // least 256 rows a block)
+    {
+        int dev = 0, sms = 148;
+        CB_CUDA(cudaGetDevice(&dev));
+        CB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const long want = std::max<long>(1, std::min<long>(sms, (n + 255) / 256));
+        ks.rows_per_red = (int)((n + want - 1) / want);
+        ks.nred = (int)((n + ks.rows_per_red - 1) / ks.rows_per_red);
+    }
     auto alloc = [&](size_t bytes) {
         void *q = nullptr;
         CB_CUDA(cudaMalloc(&q, std::max<size_t>(bytes, 16)));
@@ -528,15 +595,15 @@ void krylov_spmv(const KrylovSolver &ks, const double *x, double *y, cudaStream_
     kry_spmv_kernel<<<nb(ks.n * 8), kKT, 0, st>>>(ks.ctl, 2, ks.rowptr, ks.col, ks.val, x, nullptr, y, ks.n);
 }
 
-void krylov_apply_learned(KrylovSolver &ks, cudaStream_t st)
-{
-    (void)st;
-    if (!ks.mpnn) throw cb_status_error(CB_ERR_STATE, "no learned preconditioner attached");
-}
 
 namespace {
 
-// One Arnoldi step (12 launches).
+GsArgs gs_args(KrylovSolver &ks)
+{
+    return GsArgs{ks.ctl, ks.V, ks.w, ks.partial, ks.n, ks.rows_per_red, ks.nred};
+}
+
+// One Arnoldi step (8 launches; the last three act only when a cycle ends).
 void arnoldi_step(KrylovSolver &ks, KrylovPrecond pc, cudaStream_t st)
 {
     const long n = ks.n;
@@ -550,19 +617,16 @@ void arnoldi_step(KrylovSolver &ks, KrylovPrecond pc, cudaStream_t st)
                                                            ks.blk_off, (const double *)ks.binv, n);
     }
     kry_spmv_kernel<<<nb(n * 8), kKT, 0, st>>>(ks.ctl, 0, ks.rowptr, ks.col, ks.val, ks.Z, nullptr, ks.w, n);
-    kry_dots_kernel<<<ks.nred, kKT, 0, st>>>(ks.ctl, ks.V, ks.w, ks.partial, n, ks.rows_per_red, ks.nred);
-    kry_reduce_kernel<<<1, kKT, 0, st>>>(ks.ctl, ks.partial, ks.nred, 0);
-    kry_update_kernel<<<ks.nred, kKT, 0, st>>>(ks.ctl, ks.V, ks.w, ks.partial, n, ks.rows_per_red, ks.nred, 0);
-    kry_reduce_kernel<<<1, kKT, 0, st>>>(ks.ctl, ks.partial, ks.nred, 1);
-    kry_update_kernel<<<ks.nred, kKT, 0, st>>>(ks.ctl, ks.V, ks.w, ks.partial, n, ks.rows_per_red, ks.nred, 1);
-    kry_close_kernel<<<1, 32, 0, st>>>(ks.ctl, ks.partial, ks.nred);
+    const GsArgs ga = gs_args(ks);
+    kry_gs_dots_kernel<<<ks.nred, kKT, 0, st>>>(ga);
+    kry_gs_update_kernel<<<ks.nred, kKT, 0, st>>>(ga, 0);
+    kry_gs_update_kernel<<<ks.nred, kKT, 0, st>>>(ga, 1);
     kry_xupdate_kernel<<<nb(n), kKT, 0, st>>>(ks.ctl, ks.Z, ks.x, n);
     kry_spmv_kernel<<<nb(n * 8), kKT, 0, st>>>(ks.ctl, 1, ks.rowptr, ks.col, ks.val, ks.x, ks.b, ks.w, n);
-    kry_norm_kernel<<<ks.nred, kKT, 0, st>>>(ks.ctl, 1, ks.w, ks.partial, n, ks.rows_per_red);
-    kry_restart_kernel<<<1, 32, 0, st>>>(ks.ctl, ks.partial, ks.nred);
+    kry_norm_start_kernel<<<ks.nred, kKT, 0, st>>>(ga, 1, 0, 0, 0.0);
 }
 
-constexpr int kStepLaunches = 12;
+constexpr int kStepLaunches = 8;
 
 }  // namespace
 
@@ -573,10 +637,9 @@ int krylov_solve(KrylovSolver &ks, const double *b, double *x, cudaStream_t st, 
     CB_CUDA(cudaMemcpyAsync(ks.b, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     CB_CUDA(cudaMemcpyAsync(ks.w, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     CB_CUDA(cudaMemsetAsync(ks.x, 0, sizeof(double) * n, st));
-    kry_norm_kernel<<<ks.nred, kKT, 0, st>>>(ks.ctl, 0, ks.w, ks.partial, n, ks.rows_per_red);
-    kry_start_kernel<<<1, 32, 0, st>>>(ks.ctl, ks.partial, ks.nred, ks.m, ks.maxit, ks.rtol);
+    kry_norm_start_kernel<<<ks.nred, kKT, 0, st>>>(gs_args(ks), 0, ks.m, ks.maxit, ks.rtol);
     CB_CUDA(cudaGetLastError());
-    if (launches) *launches += 2;
+    if (launches) *launches += 1;
     const int gi = pc == KrylovPrecond::learned ? 1 : 0;
     if (use_graph && !ks.step_graph[gi]) {
         cudaGraph_t g;

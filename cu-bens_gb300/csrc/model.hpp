@@ -62,6 +62,10 @@ struct cb_model {
     long tmap_n = 0;
     cb::BandFactor bf;           // band LDL^T (CB_SOLVER_BAND)
     cb::KrylovSolver *ks = nullptr;  // FGMRES (CB_SOLVER_FGMRES)
+    cb::Mpnn *mp = nullptr;          // learned preconditioner (CB_PRECOND_LEARNED)
+    int learn_steps = -1, learn_adam = 4;
+    double learn_stall = 2.0;
+    long bj_solves = 0, bj_iters = 0, learned_solves = 0, fallbacks = 0;
     cb::MsalScalars *sc = nullptr, *sc_h = nullptr;
     double *partial = nullptr;
 

@@ -171,6 +171,11 @@ void upload_model(cb_model *m)
         m->ks = new cb::KrylovSolver();
         cb::krylov_alloc(*m->ks, h, m->opt.krylov_restart, m->opt.krylov_maxit, fp32, st);
         m->bytes += m->ks->bytes;
+        if (m->opt.precond == CB_PRECOND_LEARNED) {
+            m->mp = cb::mpnn_create(h, 20240611u, 32, st);
+            m->ks->mpnn = m->mp;
+            m->bytes += cb::mpnn_bytes(m->mp);
+        }
         m->kel = m->alloc<double>(171 * E + 21 * T + 105 * F);
         m->sc = m->alloc<cb::MsalScalars>(1);
         m->partial = m->alloc<double>(16 * cb::kRedBlocks);
@@ -697,6 +702,7 @@ int cb_model_destroy(cb_model *m)
         cb::krylov_free(*m->ks);
         delete m->ks;
     }
+    cb::mpnn_destroy(m->mp);
     for (void *p : m->allocs) cudaFree(p);
     if (m->sc_h) cudaFreeHost(m->sc_h);
     for (auto &e : m->ev)

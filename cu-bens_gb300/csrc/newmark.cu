@@ -86,6 +86,9 @@ void newmark_begin(cb_model *m)
 
 // Keff dd = Reff with FGMRES: the preconditioner from the current matrix,
 // then the solve (m->r -> m->dd).
+// With the learned preconditioner: the first time steps solve with
+// block-Jacobi and train the network on each solve's (Reff, dd) pair; later
+// solves use the network and fall back to block-Jacobi when one stalls.
 void krylov_newmark_solve(cb_model *m)
 {
     cb::KrylovSolver &ks = *m->ks;
@@ -95,10 +98,44 @@ void krylov_newmark_solve(cb_model *m)
         m->tm.launches += 1;
         m->tm.factorizations++;
     }
-    PhaseTimer t(m, &m->tm.ms_solve);
-    cb::krylov_solve(ks, m->r, m->dd, m->st, m->opt.use_graphs != 0, cb::KrylovPrecond::block_jacobi,
-                     &m->tm.launches);
-    m->tm.solves++;
+    const bool graphs = m->opt.use_graphs != 0;
+    auto bj_solve = [&] {
+        PhaseTimer t(m, &m->tm.ms_solve);
+        const int it = cb::krylov_solve(ks, m->r, m->dd, m->st, graphs, cb::KrylovPrecond::block_jacobi,
+                                        &m->tm.launches);
+        m->tm.solves++;
+        return it;
+    };
+    if (!m->mp) {
+        bj_solve();
+        return;
+    }
+    const long train = m->learn_steps >= 0 ? m->learn_steps : std::max(1L, m->h.nsteps / 10);
+    if (m->nm_k < train) {
+        m->bj_iters += bj_solve();
+        m->bj_solves++;
+        PhaseTimer t(m, &m->tm.ms_train);
+        cb::mpnn_push_pair(*m->mp, m->r, m->dd, m->st);
+        cb::mpnn_train(*m->mp, ks, m->learn_adam, m->st);
+        return;
+    }
+    const double avg = m->bj_solves ? (double)m->bj_iters / (double)m->bj_solves : (double)ks.maxit;
+    const int cap = std::max(10, (int)(m->learn_stall * avg));
+    const int saved = ks.maxit;
+    ks.maxit = std::min(cap, saved);
+    {
+        PhaseTimer t(m, &m->tm.ms_solve);
+        cb::krylov_solve(ks, m->r, m->dd, m->st, graphs, cb::KrylovPrecond::learned, &m->tm.launches);
+        m->tm.solves++;
+    }
+    ks.maxit = saved;
+    m->learned_solves++;
+    if (ks.ctl_h->status == 1) {
+        // stalled: the unconverged count is the fallback's business
+        ks.unconverged--;
+        m->fallbacks++;
+        bj_solve();
+    }
 }
 
 // one Newton iteration of main.c:3543-3745; returns the scalar block
@@ -364,7 +401,73 @@ int cb_get_krylov_stats(const cb_model *m, cb_krylov_stats *s)
     s->unconverged = ks.unconverged;
     s->last_iterations = ks.last_iters;
     s->last_residual = ks.last_resid;
+    s->learned_solves = m->learned_solves;
+    s->fallbacks = m->fallbacks;
+    s->train_steps = cb::mpnn_adam_steps(m->mp);
+    s->train_loss = cb::mpnn_last_loss(m->mp);
     return CB_OK;
+}
+
+int cb_set_learning(cb_model *m, int train_steps, int adam_per_solve, double lr, double stall_factor)
+{
+    if (!m || adam_per_solve < 0 || !(lr > 0) || !(stall_factor > 0)) return CB_ERR_ARG;
+    if (!m->mp) {
+        m->err = "the handle has no learned preconditioner";
+        return CB_ERR_STATE;
+    }
+    m->learn_steps = train_steps;
+    m->learn_adam = adam_per_solve;
+    m->learn_stall = stall_factor;
+    cb::mpnn_set_lr(m->mp, lr);
+    return CB_OK;
+}
+
+long cb_mpnn_param_count(void) { return cb::mpnn_param_count(); }
+
+int cb_mpnn_set_params(cb_model *m, const float *theta)
+{
+    if (!m || !theta) return CB_ERR_ARG;
+    if (!m->mp) {
+        m->err = "the handle has no learned preconditioner";
+        return CB_ERR_STATE;
+    }
+    return guarded(m, [&] {
+        cb::mpnn_set_params(m->mp, theta, m->st);
+        CB_CUDA(cudaStreamSynchronize(m->st));
+    });
+}
+
+int cb_mpnn_get_params(const cb_model *m, float *theta, float *grad)
+{
+    if (!m) return CB_ERR_ARG;
+    cb_model *mm = const_cast<cb_model *>(m);
+    if (!m->mp) {
+        mm->err = "the handle has no learned preconditioner";
+        return CB_ERR_STATE;
+    }
+    return guarded(mm, [&] { cb::mpnn_get_params(m->mp, theta, grad, m->st); });
+}
+
+int cb_mpnn_eval(cb_model *m, const double *r, const double *p, const double *t, int train, double *z,
+                 double *loss)
+{
+    if (!m || !r || !p) return CB_ERR_ARG;
+    if (!m->mp) {
+        m->err = "the handle has no learned preconditioner";
+        return CB_ERR_STATE;
+    }
+    return guarded(m, [&] {
+        const long N = m->h.neq;
+        cudaStream_t st = m->st;
+        double *rd = m->r, *pd = m->ddr, *td = m->ddq, *zd = m->dt;
+        h2d(rd, r, N, st);
+        h2d(pd, p, N, st);
+        if (t) h2d(td, t, N, st);
+        const double L = cb::mpnn_eval(*m->mp, *m->ks, rd, pd, t ? td : nullptr, zd, train != 0, st);
+        if (z) d2h(z, zd, N, st);
+        CB_CUDA(cudaStreamSynchronize(st));
+        if (loss) *loss = L;
+    });
 }
 
 int cb_newmark_state(const cb_model *m, double *u, double *v, double *a)

@@ -59,7 +59,8 @@ class Step(C.Structure):
 class Timers(C.Structure):
     _fields_ = [("ms_tangent", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double),
                 ("ms_force", C.c_double), ("ms_vector", C.c_double), ("launches", C.c_long),
-                ("solves", C.c_long), ("factorizations", C.c_long), ("force_evals", C.c_long)]
+                ("solves", C.c_long), ("factorizations", C.c_long), ("force_evals", C.c_long),
+                ("ms_train", C.c_double)]
 
 
 class KrylovStats(C.Structure):
@@ -113,6 +114,12 @@ def load(path: Path | None = None):
     L.cb_eval_frame_mass.argtypes = [vp, dp, dp, dp]
     L.cb_set_krylov_tolerance.argtypes = [vp, C.c_double]
     L.cb_get_krylov_stats.argtypes = [vp, C.POINTER(KrylovStats)]
+    fp = C.POINTER(C.c_float)
+    L.cb_set_learning.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double]
+    L.cb_mpnn_param_count.restype = C.c_long
+    L.cb_mpnn_set_params.argtypes = [vp, fp]
+    L.cb_mpnn_get_params.argtypes = [vp, fp, fp]
+    L.cb_mpnn_eval.argtypes = [vp, dp, dp, dp, C.c_int, dp, dp]
     _lib = L
     return L
 
@@ -327,6 +334,31 @@ class Model:
         ms, by, fl = C.c_double(), C.c_double(), C.c_double()
         self._check(load().cb_profile_kernel(self.h, which, reps, C.byref(ms), C.byref(by), C.byref(fl)))
         return ms.value, by.value, fl.value
+
+    def set_learning(self, train_steps: int = -1, adam_per_solve: int = 4, lr: float = 1e-3,
+                     stall_factor: float = 2.0):
+        self._check(load().cb_set_learning(self.h, train_steps, adam_per_solve, lr, stall_factor))
+
+    def mpnn_params(self):
+        L = load()
+        n = L.cb_mpnn_param_count()
+        th = np.zeros(n, dtype=np.float32)
+        gr = np.zeros(n, dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check(L.cb_mpnn_get_params(self.h, th.ctypes.data_as(fp), gr.ctypes.data_as(fp)))
+        return th, gr
+
+    def set_mpnn_params(self, theta):
+        th = np.ascontiguousarray(theta, dtype=np.float32)
+        self._check(load().cb_mpnn_set_params(self.h, th.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def mpnn_eval(self, r, p, t=None, train: bool = False):
+        """The network on (r, p): z, and with t the loss (gradient via mpnn_params)."""
+        z = np.zeros(self.neq)
+        loss = C.c_double()
+        self._check(load().cb_mpnn_eval(self.h, _d(_c64(r)), _d(_c64(p)), None if t is None else _d(_c64(t)),
+                                        1 if train else 0, _d(z), C.byref(loss)))
+        return z, loss.value
 
     def krylov_stats(self) -> dict:
         s = KrylovStats()

@@ -361,5 +361,6 @@ def frame_building(bays_x: int = 20, bays_y: int = 20, storeys: int = 30,
         out.append("0,0,0")                   # no distributed loads
         out += msal.lines()
     name = f"frame{bx}x{by}x{ns}" + ("" if dynamic else "_msal")
+    params["members"] = members               # 1-based joint pairs, in input order
     return ModelSpec(name, "\n".join(out) + "\n", nj=len(nodes), ne_fr=len(members),
                      seed=seed if dynamic else None, params=params)

@@ -115,6 +115,7 @@ typedef struct {
     double ms_tangent, ms_factor, ms_solve, ms_force, ms_vector;
     long launches;
     long solves, factorizations, force_evals;
+    double ms_train;  /* learned preconditioner: training (forward, backward, Adam) */
 } cb_timers;
 
 /* ---- resident API -------------------------------------------------------- */
@@ -177,6 +178,27 @@ typedef struct {
 } cb_krylov_stats;
 int cb_set_krylov_tolerance(cb_model *m, double rtol);
 int cb_get_krylov_stats(const cb_model *m, cb_krylov_stats *s);
+
+/* Learned preconditioner (solver CB_SOLVER_FGMRES, precond CB_PRECOND_LEARNED).
+ * Online schedule: the time steps k < train_steps solve with block-Jacobi
+ * and store each solve's (effective residual, FP64 correction) pair; after
+ * each such solve the network takes adam_per_solve Adam steps (learning rate
+ * lr) on the stored pairs. Later solves use the network; one that has not
+ * converged after stall_factor times the block-Jacobi average of Arnoldi
+ * steps (at least 10) is redone with block-Jacobi. train_steps < 0 keeps the
+ * default (a tenth of the time steps, at least one). */
+int cb_set_learning(cb_model *m, int train_steps, int adam_per_solve, double lr, double stall_factor);
+/* The network itself, for checks against a CPU definition. Parameters are
+ * cb_mpnn_param_count() float32 values (layout in cu-bens_gb300/csrc/mpnn.cu).
+ * cb_mpnn_eval runs the network on host vectors r and p (NEQ; p stands for
+ * the block-Jacobi image of r) into z (may be NULL); with t (may be NULL) it
+ * also forms the loss |z - t|^2 / |t|^2 and the parameter gradient, and with
+ * train = 1 takes one Adam step with it. */
+long cb_mpnn_param_count(void);
+int cb_mpnn_set_params(cb_model *m, const float *theta);
+int cb_mpnn_get_params(const cb_model *m, float *theta, float *grad);
+int cb_mpnn_eval(cb_model *m, const double *r, const double *p, const double *t, int train, double *z,
+                 double *loss);
 
 int cb_get_timers(const cb_model *m, cb_timers *t);
 int cb_reset_timers(cb_model *m);
