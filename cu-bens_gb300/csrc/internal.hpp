@@ -240,6 +240,17 @@ struct KrylovSolver {
     int chunk = 8;               // Arnoldi steps per graph replay
     cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
     size_t bytes = 0;
+    // nested precision (mixed): an FP32 FGMRES over FP32 copies of the matrix
+    // and block inverses is the preconditioner of the FP64 FGMRES
+    bool nested = false;
+    int m32 = 30, maxit32 = 400;
+    double rtol32 = 1e-4;
+    float *valf = nullptr, *V32 = nullptr, *Z32 = nullptr, *w32 = nullptr, *b32 = nullptr, *x32 = nullptr;
+    float *partial32 = nullptr;
+    int nred32 = 0, rows_per_red32 = 0;
+    KrylovCtl *ctl32 = nullptr, *ctl32_h = nullptr;
+    cudaGraphExec_t graph32 = nullptr;
+    long inner_iterations = 0;
     // learned preconditioner hook (filled by the MPNN module)
     void *mpnn = nullptr;
     // statistics
@@ -248,20 +259,24 @@ struct KrylovSolver {
     double last_resid = 0;
 };
 
-void krylov_alloc(KrylovSolver &ks, const HostModel &h, int restart, int maxit, bool fp32_precond,
-                  cudaStream_t st);
+// fp32: mixed precision (FP32 block inverses, nested FP32 inner FGMRES)
+void krylov_alloc(KrylovSolver &ks, const HostModel &h, int restart, int maxit, bool fp32, cudaStream_t st);
 void krylov_free(KrylovSolver &ks);
 // tangent values from the element matrices (FP64) into the CSR matrix
 void krylov_assemble(KrylovSolver &ks, const double *kel, cudaStream_t st);
 // Keff diagonal: val[diag[i]] += c0 sm[i] / den (the band's nm_keff arithmetic)
 void krylov_shift_diag(KrylovSolver &ks, const double *sm, double c0, double den, cudaStream_t st);
-// invert the nodal blocks of the current matrix
+// invert the nodal blocks of the current matrix (and, nested, form the FP32
+// copy of the matrix)
 void krylov_setup_block_jacobi(KrylovSolver &ks, cudaStream_t st);
 // Solve A x = b to rtol (relative to |b|); returns the Arnoldi steps taken.
 int krylov_solve(KrylovSolver &ks, const double *b, double *x, cudaStream_t st, bool use_graph,
                  KrylovPrecond pc, long *launches);
 // y = A x (one CSR product; isolated timing)
 void krylov_spmv(const KrylovSolver &ks, const double *x, double *y, cudaStream_t st);
+// After a solve: t = z_k of the last cycle's preconditioned basis, b = A z_k
+// (a (residual, correction) pair from inside the Krylov process)
+void krylov_basis_pair(const KrylovSolver &ks, int k, double *b, double *t, cudaStream_t st);
 // the learned preconditioner's step inside the Arnoldi sequence (mpnn.cu)
 void krylov_apply_learned(KrylovSolver &ks, cudaStream_t st);
 
@@ -282,6 +297,9 @@ void mpnn_get_params(const Mpnn *mp, float *theta, float *grad, cudaStream_t st)
 double mpnn_eval(Mpnn &mp, const KrylovSolver &ks, const double *r, const double *p, const double *t, double *z,
                  bool train, cudaStream_t st);
 void mpnn_push_pair(Mpnn &mp, const double *b, const double *t, cudaStream_t st);
+// the next ring slot's (b, t) buffers; mpnn_commit_pair then advances the ring
+void mpnn_slot(Mpnn &mp, double **b, double **t);
+void mpnn_commit_pair(Mpnn &mp);
 double mpnn_train(Mpnn &mp, const KrylovSolver &ks, int steps, cudaStream_t st);
 
 // ---------------------------------------------------------------------------

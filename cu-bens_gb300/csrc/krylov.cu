@@ -33,7 +33,8 @@ namespace {
 
 constexpr int kKT = 256;
 
-__device__ __forceinline__ double warp_sum(double v)
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -134,42 +135,42 @@ __global__ void kry_bj_setup_kernel(const int *__restrict__ rowptr, const int *_
     }
 }
 
-// v_j = w * scale; z_j = B^-1 v_j over the row's block.
-template <typename T>
-__global__ void kry_bj_apply_kernel(const KrylovCtl *__restrict__ ctl, const double *__restrict__ w,
-                                    double *__restrict__ V, double *__restrict__ Z, const int *__restrict__ row_blk,
+// v_j = w * scale; z_j = B^-1 v_j over the row's block (in Tb arithmetic)
+template <typename Tb, typename T>
+__global__ void kry_bj_apply_kernel(const KrylovCtl *__restrict__ ctl, const T *__restrict__ w, T *__restrict__ V,
+                                    T *__restrict__ Z, const int *__restrict__ row_blk,
                                     const int *__restrict__ blk_start, const int *__restrict__ blk_off,
-                                    const T *__restrict__ binv, long n)
+                                    const Tb *__restrict__ binv, long n)
 {
     if (ctl->done) return;
     long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int j = ctl->j;
-    const double sc = ctl->scale;
+    const T sc = (T)ctl->scale;
     V[(size_t)j * n + i] = w[i] * sc;
     const int b = row_blk[i];
     const int s0 = blk_start[b], bs = blk_start[b + 1] - s0;
-    const T *B = binv + blk_off[b] + (i - s0) * bs;
-    double z = 0;
-    for (int c = 0; c < bs; ++c) z += (double)B[c] * (w[s0 + c] * sc);
-    Z[(size_t)j * n + i] = z;
+    const Tb *B = binv + blk_off[b] + (i - s0) * bs;
+    Tb z = 0;
+    for (int c = 0; c < bs; ++c) z += B[c] * (Tb)(w[s0 + c] * sc);
+    Z[(size_t)j * n + i] = (T)z;
 }
 
 // ---- products and Gram-Schmidt passes ----
 
 // 8 lanes per row, fixed lane order. mode 0: y = A z_j (while the solve
 // runs); mode 1: y = b - A x (when a cycle ends unconverged); mode 2: y = A x.
+template <typename T>
 __global__ void kry_spmv_kernel(const KrylovCtl *__restrict__ ctl, int mode, const int *__restrict__ rowptr,
-                                const int *__restrict__ col, const double *__restrict__ val,
-                                const double *__restrict__ xin, const double *__restrict__ bvec,
-                                double *__restrict__ y, long n)
+                                const int *__restrict__ col, const T *__restrict__ val, const T *__restrict__ xin,
+                                const T *__restrict__ bvec, T *__restrict__ y, long n)
 {
     if (mode == 0 && ctl->done) return;
     if (mode == 1 && (ctl->done || !ctl->finish || ctl->conv)) return;
-    const double *x = mode == 0 ? xin + (size_t)ctl->j * n : xin;
+    const T *x = mode == 0 ? xin + (size_t)ctl->j * n : xin;
     const long row = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 3;
     const int lane = threadIdx.x & 7;
-    double acc = 0;
+    T acc = 0;
     if (row < n)
         for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += 8) acc += val[k] * x[col[k]];
     acc += __shfl_xor_sync(0xffffffffu, acc, 4);
@@ -199,13 +200,14 @@ __device__ bool last_block(unsigned *counter)
 }
 
 // partial[k*nred + blk] = v_k . w over rows [r0, r1), k <= j (one warp per k)
-__device__ void block_dots(const double *__restrict__ V, const double *__restrict__ w, long n, int j, long r0,
-                           long r1, double *__restrict__ partial, int nred)
+template <typename T>
+__device__ void block_dots(const T *__restrict__ V, const T *__restrict__ w, long n, int j, long r0, long r1,
+                           T *__restrict__ partial, int nred)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int k = warp; k <= j; k += kWarps) {
-        const double *v = V + (size_t)k * n;
-        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        const T *v = V + (size_t)k * n;
+        T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
         long i = r0 + lane;
         for (; i + 96 < r1; i += 128) {
             a0 += v[i] * w[i];
@@ -214,22 +216,23 @@ __device__ void block_dots(const double *__restrict__ V, const double *__restric
             a3 += v[i + 96] * w[i + 96];
         }
         for (; i < r1; i += 32) a0 += v[i] * w[i];
-        const double acc = warp_sum((a0 + a1) + (a2 + a3));
+        const T acc = warp_sum((a0 + a1) + (a2 + a3));
         if (lane == 0) partial[(size_t)k * nred + blockIdx.x] = acc;
     }
 }
 
 // partial[blk] = |w|^2 over rows [r0, r1)
-__device__ void block_norm(const double *__restrict__ w, long r0, long r1, double *__restrict__ partial)
+template <typename T>
+__device__ void block_norm(const T *__restrict__ w, long r0, long r1, T *__restrict__ partial)
 {
-    __shared__ double red[kWarps];
-    double acc = 0;
+    __shared__ T red[kWarps];
+    T acc = 0;
     for (long i = r0 + threadIdx.x; i < r1; i += blockDim.x) acc += w[i] * w[i];
     acc = warp_sum(acc);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double sum = 0;
+        T sum = 0;
         for (int k = 0; k < kWarps; ++k) sum += red[k];
         partial[blockIdx.x] = sum;
     }
@@ -238,25 +241,27 @@ __device__ void block_norm(const double *__restrict__ w, long r0, long r1, doubl
 // Sum of partial[0..nred) by one warp in a fixed order: each lane loads its
 // strided values sixteen at a time (independent loads in flight), adds them
 // in index order, then a butterfly across the lanes.
-__device__ __forceinline__ double warp_sum_partials(const double *__restrict__ pk, int nred)
+template <typename T>
+__device__ __forceinline__ double warp_sum_partials(const T *__restrict__ pk, int nred)
 {
     const int lane = threadIdx.x & 31;
-    double acc = 0;
+    T acc = 0;
     for (int b0 = 0; b0 < nred; b0 += 32 * 16) {
-        double v[16];
+        T v[16];
 #pragma unroll
         for (int u = 0; u < 16; ++u) {
             const int b = b0 + lane + 32 * u;
-            v[u] = b < nred ? __ldcg(pk + b) : 0.0;
+            v[u] = b < nred ? __ldcg(pk + b) : (T)0;
         }
 #pragma unroll
         for (int u = 0; u < 16; ++u) acc += v[u];
     }
-    return warp_sum(acc);
+    return (double)warp_sum(acc);
 }
 
 // last block: hp[k] = sum_b partial[k*nred + b] (one warp per k)
-__device__ void reduce_hp(KrylovCtl *ctl, const double *partial, int nred, int j, int pass)
+template <typename T>
+__device__ void reduce_hp(KrylovCtl *ctl, const T *partial, int nred, int j, int pass)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int k = warp; k <= j; k += kWarps) {
@@ -269,14 +274,19 @@ __device__ void reduce_hp(KrylovCtl *ctl, const double *partial, int nred, int j
 }
 
 // last block, warp 0: sum_b partial[b]
-__device__ double reduce_norm(const double *partial, int nred) { return warp_sum_partials(partial, nred); }
+template <typename T>
+__device__ double reduce_norm(const T *partial, int nred)
+{
+    return warp_sum_partials(partial, nred);
+}
 
 // w[i] -= sum_k hp[k] V_k[i] over rows [r0, r1)
-__device__ void block_update(const double *__restrict__ V, double *__restrict__ w, long n, int j, const double *hp,
-                             long r0, long r1)
+template <typename T>
+__device__ void block_update(const T *__restrict__ V, T *__restrict__ w, long n, int j, const T *hp, long r0,
+                             long r1)
 {
     for (long i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        double s = w[i];
+        T s = w[i];
 #pragma unroll 8
         for (int k = 0; k <= j; ++k) s -= hp[k] * V[(size_t)k * n + i];
         w[i] = s;
@@ -332,17 +342,19 @@ __device__ void close_step(KrylovCtl *ctl, double ww)
     }
 }
 
+template <typename T>
 struct GsArgs {
     KrylovCtl *ctl;
-    const double *V;
-    double *w;
-    double *partial;
+    const T *V;
+    T *w;
+    T *partial;
     long n;
     int rpr, nred;
 };
 
 // pass 1: h = V^T w (w = A z_j from the product)
-__global__ void kry_gs_dots_kernel(GsArgs a)
+template <typename T>
+__global__ void kry_gs_dots_kernel(GsArgs<T> a)
 {
     KrylovCtl *ctl = a.ctl;
     if (ctl->done) return;
@@ -357,26 +369,27 @@ __global__ void kry_gs_dots_kernel(GsArgs a)
 
 // w -= V h, then pass 2 (last == 0: h2 = V^T w) or the norm and the close of
 // the step (last == 1)
-__global__ void kry_gs_update_kernel(GsArgs a, int last)
+template <typename T>
+__global__ void kry_gs_update_kernel(GsArgs<T> a, int last)
 {
     KrylovCtl *ctl = a.ctl;
     if (ctl->done) return;
-    __shared__ double hp[kMaxRestart + 1];
+    __shared__ T hp[kMaxRestart + 1];
     const int j = ctl->j;
-    for (int k = threadIdx.x; k <= j; k += blockDim.x) hp[k] = ctl->hp[k];
+    for (int k = threadIdx.x; k <= j; k += blockDim.x) hp[k] = (T)ctl->hp[k];
     __syncthreads();
     const long r0 = blockIdx.x * (long)a.rpr, r1 = min(a.n, r0 + a.rpr);
     block_update(a.V, a.w, a.n, j, hp, r0, r1);
     __syncthreads();
     if (!last) {
-        block_dots(a.V, a.w, a.n, j, r0, r1, a.partial, a.nred);
+        block_dots(a.V, (const T *)a.w, a.n, j, r0, r1, a.partial, a.nred);
         if (last_block(&ctl->arrive[1])) {
             reduce_hp(ctl, a.partial, a.nred, j, 1);
             if (threadIdx.x == 0) ctl->arrive[1] = 0;
         }
         return;
     }
-    block_norm(a.w, r0, r1, a.partial);
+    block_norm((const T *)a.w, r0, r1, a.partial);
     if (last_block(&ctl->arrive[2])) {
         if (threadIdx.x < 32) {
             const double ww = reduce_norm(a.partial, a.nred);
@@ -391,7 +404,8 @@ __global__ void kry_gs_update_kernel(GsArgs a, int last)
 // Start of a solve (mode 0; w = b): |b| and the first cycle. After a
 // finished cycle (mode 1): done when the estimate converged, else restart
 // from the true residual r = b - A x held in w.
-__global__ void kry_norm_start_kernel(GsArgs a, int mode, int m, int maxit, double rtol)
+template <typename T>
+__global__ void kry_norm_start_kernel(GsArgs<T> a, int mode, int m, int maxit, double rtol)
 {
     KrylovCtl *ctl = a.ctl;
     if (mode == 1) {
@@ -405,7 +419,7 @@ __global__ void kry_norm_start_kernel(GsArgs a, int mode, int m, int maxit, doub
         }
     }
     const long r0 = blockIdx.x * (long)a.rpr, r1 = min(a.n, r0 + a.rpr);
-    block_norm(a.w, r0, r1, a.partial);
+    block_norm((const T *)a.w, r0, r1, a.partial);
     if (!last_block(&ctl->arrive[3])) return;
     if (threadIdx.x >= 32) return;
     const double bb = reduce_norm(a.partial, a.nred);
@@ -452,19 +466,46 @@ __global__ void kry_norm_start_kernel(GsArgs a, int mode, int m, int maxit, doub
 }
 
 // x += Z y at the end of a cycle
-__global__ void kry_xupdate_kernel(const KrylovCtl *__restrict__ ctl, const double *__restrict__ Z,
-                                   double *__restrict__ x, long n)
+template <typename T>
+__global__ void kry_xupdate_kernel(const KrylovCtl *__restrict__ ctl, const T *__restrict__ Z, T *__restrict__ x,
+                                   long n)
 {
     if (ctl->done || !ctl->finish) return;
-    __shared__ double y[kMaxRestart];
+    __shared__ T y[kMaxRestart];
     const int nc = ctl->ncols;
-    for (int k = threadIdx.x; k < nc; k += blockDim.x) y[k] = ctl->y[k];
+    for (int k = threadIdx.x; k < nc; k += blockDim.x) y[k] = (T)ctl->y[k];
     __syncthreads();
     long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double s = x[i];
+    T s = x[i];
     for (int k = 0; k < nc; ++k) s += y[k] * Z[(size_t)k * n + i];
     x[i] = s;
+}
+
+// nested precision: v_j = w * scale (FP64) and its FP32 copy, the inner
+// right-hand side
+__global__ void kry_outer_pre_kernel(const KrylovCtl *__restrict__ ctl, const double *__restrict__ w,
+                                     double *__restrict__ V, float *__restrict__ b32, long n)
+{
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = w[i] * ctl->scale;
+    V[(size_t)ctl->j * n + i] = v;
+    b32[i] = (float)v;
+}
+
+// z_j = the inner FP32 solution
+__global__ void kry_outer_post_kernel(const KrylovCtl *__restrict__ ctl, const float *__restrict__ x32,
+                                      double *__restrict__ Z, long n)
+{
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) Z[(size_t)ctl->j * n + i] = (double)x32[i];
+}
+
+__global__ void kry_to_f32_kernel(const double *__restrict__ a, float *__restrict__ b, long n)
+{
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
 }
 
 inline unsigned nb(long n, int t = kKT) { return (unsigned)((n + t - 1) / t); }
@@ -473,14 +514,15 @@ inline unsigned nb(long n, int t = kKT) { return (unsigned)((n + t - 1) / t); }
 
 // ---------------------------------------------------------------------------
 
-void krylov_alloc(KrylovSolver &ks, const HostModel &h, int restart, int maxit, bool fp32_precond,
-                  cudaStream_t st)
+void krylov_alloc(KrylovSolver &ks, const HostModel &h, int restart, int maxit, bool fp32, cudaStream_t st)
 {
     const long n = h.neq;
     ks.n = n;
     ks.m = std::max(2, std::min(restart > 0 ? restart : 50, kMaxRestart));
     ks.maxit = maxit > 0 ? maxit : 2000;
-    ks.fp32_precond = fp32_precond;
+    const bool fp32_precond = fp32;
+    ks.fp32_precond = fp32;
+    ks.nested = fp32;
     CsrPattern p;
     GatherMap g;
     std::vector<int64_t> dst2;
@@ -499,8 +541,9 @@ void krylov_alloc(KrylovSolver &ks, const HostModel &h, int restart, int maxit, 
         for (int q = bstart[b]; q < bstart[b + 1]; ++q) rblk[q] = (int)b;
     }
     ks.binv_n = off[ks.nblk];
-    // Gram-Schmidt partition: one block per SM-sized share of the rows (at
-    // least 256 rows a block)
+    // Gram-Schmidt partition: one block per SM (at least 256 rows a block).
+    // The FP64 pipe bounds these passes on GB300; every extra block adds
+    // FP64 reduction work per basis vector.
     {
         int dev = 0, sms = 148;
         CB_CUDA(cudaGetDevice(&dev));
@@ -538,6 +581,24 @@ void krylov_alloc(KrylovSolver &ks, const HostModel &h, int restart, int maxit, 
     ks.ctl = (KrylovCtl *)alloc(sizeof(KrylovCtl));
     CB_CUDA(cudaMallocHost(&ks.ctl_h, sizeof(KrylovCtl)));
     std::memset(ks.ctl_h, 0, sizeof(KrylovCtl));
+    if (ks.nested) {
+        ks.valf = (float *)alloc(sizeof(float) * ks.nnz);
+        ks.V32 = (float *)alloc(sizeof(float) * (size_t)(ks.m32 + 1) * n);
+        ks.Z32 = (float *)alloc(sizeof(float) * (size_t)ks.m32 * n);
+        for (float **v : {&ks.w32, &ks.b32, &ks.x32}) *v = (float *)alloc(sizeof(float) * n);
+        // FP32 passes: four blocks per SM, FP32 partial sums (the FP32 pipe is
+        // not the limit there, the round trips are)
+        int dev = 0, sms = 148;
+        CB_CUDA(cudaGetDevice(&dev));
+        CB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const long want = std::max<long>(1, std::min<long>(4L * sms, (n + 63) / 64));
+        ks.rows_per_red32 = (int)((n + want - 1) / want);
+        ks.nred32 = (int)((n + ks.rows_per_red32 - 1) / ks.rows_per_red32);
+        ks.partial32 = (float *)alloc(sizeof(float) * (size_t)(kMaxRestart + 1) * ks.nred32 + 16);
+        ks.ctl32 = (KrylovCtl *)alloc(sizeof(KrylovCtl));
+        CB_CUDA(cudaMallocHost(&ks.ctl32_h, sizeof(KrylovCtl)));
+        std::memset(ks.ctl32_h, 0, sizeof(KrylovCtl));
+    }
     CB_CUDA(cudaMemcpyAsync(ks.rowptr, p.rowptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st));
     CB_CUDA(cudaMemcpyAsync(ks.col, p.col.data(), sizeof(int) * ks.nnz, cudaMemcpyHostToDevice, st));
     CB_CUDA(cudaMemcpyAsync(ks.diag, p.diag.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
@@ -558,12 +619,15 @@ void krylov_free(KrylovSolver &ks)
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+    if (ks.graph32) cudaGraphExecDestroy(ks.graph32);
     void *ptrs[] = {ks.rowptr, ks.col,      ks.diag,    ks.val,     ks.amap_ptr, ks.amap_src, ks.amap_dst,
                     ks.amap_dst2, ks.blk_start, ks.blk_off, ks.row_blk, ks.binv, ks.V,        ks.Z,
-                    ks.w,      ks.b,        ks.x,       ks.partial, ks.ctl};
+                    ks.w,      ks.b,        ks.x,       ks.partial, ks.ctl,      ks.valf,     ks.V32,
+                    ks.Z32,    ks.w32,      ks.b32,     ks.x32,     ks.partial32, ks.ctl32};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (ks.ctl_h) cudaFreeHost(ks.ctl_h);
+    if (ks.ctl32_h) cudaFreeHost(ks.ctl32_h);
     ks = KrylovSolver();
 }
 
@@ -588,45 +652,163 @@ void krylov_setup_block_jacobi(KrylovSolver &ks, cudaStream_t st)
     else
         kry_bj_setup_kernel<double><<<nb(ks.nblk, 128), 128, 0, st>>>(ks.rowptr, ks.col, ks.val, ks.blk_start,
                                                                        ks.blk_off, (double *)ks.binv, ks.nblk, flag);
+    if (ks.nested) kry_to_f32_kernel<<<nb(ks.nnz), kKT, 0, st>>>(ks.val, ks.valf, ks.nnz);
+}
+
+void krylov_basis_pair(const KrylovSolver &ks, int k, double *b, double *t, cudaStream_t st)
+{
+    const double *z = ks.Z + (size_t)k * ks.n;
+    CB_CUDA(cudaMemcpyAsync(t, z, sizeof(double) * ks.n, cudaMemcpyDeviceToDevice, st));
+    krylov_spmv(ks, z, b, st);
 }
 
 void krylov_spmv(const KrylovSolver &ks, const double *x, double *y, cudaStream_t st)
 {
-    kry_spmv_kernel<<<nb(ks.n * 8), kKT, 0, st>>>(ks.ctl, 2, ks.rowptr, ks.col, ks.val, x, nullptr, y, ks.n);
+    kry_spmv_kernel<double><<<nb(ks.n * 8), kKT, 0, st>>>(ks.ctl, 2, ks.rowptr, ks.col, ks.val, x, nullptr, y,
+                                                          ks.n);
 }
-
 
 namespace {
 
-GsArgs gs_args(KrylovSolver &ks)
+// One precision level of the solver: its matrix values, basis and control.
+template <typename T>
+struct Core {
+    long n;
+    int m, maxit;
+    double rtol;
+    const T *val;
+    T *V, *Z, *w, *b, *x;
+    T *partial;
+    int rpr, nred;  // Gram-Schmidt partition: rows per block, blocks
+    KrylovCtl *ctl, *ctl_h;
+    cudaGraphExec_t *graph;
+};
+
+Core<double> core64(KrylovSolver &ks, int gi)
 {
-    return GsArgs{ks.ctl, ks.V, ks.w, ks.partial, ks.n, ks.rows_per_red, ks.nred};
+    return Core<double>{ks.n, ks.m,       ks.maxit,     ks.rtol, ks.val,  ks.V,     ks.Z,
+                        ks.w, ks.b,       ks.x,         ks.partial, ks.rows_per_red, ks.nred, ks.ctl,
+                        ks.ctl_h, &ks.step_graph[gi]};
 }
 
-// One Arnoldi step (8 launches; the last three act only when a cycle ends).
-void arnoldi_step(KrylovSolver &ks, KrylovPrecond pc, cudaStream_t st)
+Core<float> core32(KrylovSolver &ks)
 {
-    const long n = ks.n;
-    if (pc == KrylovPrecond::learned) {
-        krylov_apply_learned(ks, st);
-    } else if (ks.fp32_precond) {
-        kry_bj_apply_kernel<float><<<nb(n), kKT, 0, st>>>(ks.ctl, ks.w, ks.V, ks.Z, ks.row_blk, ks.blk_start,
-                                                          ks.blk_off, (const float *)ks.binv, n);
+    return Core<float>{ks.n,   ks.m32,  ks.maxit32, ks.rtol32, ks.valf,          ks.V32,    ks.Z32,
+                       ks.w32, ks.b32,  ks.x32,     ks.partial32, ks.rows_per_red32, ks.nred32, ks.ctl32,
+                       ks.ctl32_h, &ks.graph32};
+}
+
+template <typename T>
+GsArgs<T> gs_args(const KrylovSolver &, const Core<T> &c)
+{
+    return GsArgs<T>{c.ctl, c.V, c.w, c.partial, c.n, c.rpr, c.nred};
+}
+
+// The product, Gram-Schmidt, close and cycle-end launches of an Arnoldi
+// step (7 launches; the last three act only when a cycle ends).
+template <typename T>
+void step_after_precond(const KrylovSolver &ks, const Core<T> &c, cudaStream_t st)
+{
+    const long n = c.n;
+    kry_spmv_kernel<T><<<nb(n * 8), kKT, 0, st>>>(c.ctl, 0, ks.rowptr, ks.col, c.val, c.Z, nullptr, c.w, n);
+    const GsArgs<T> ga = gs_args(ks, c);
+    kry_gs_dots_kernel<T><<<c.nred, kKT, 0, st>>>(ga);
+    kry_gs_update_kernel<T><<<c.nred, kKT, 0, st>>>(ga, 0);
+    kry_gs_update_kernel<T><<<c.nred, kKT, 0, st>>>(ga, 1);
+    kry_xupdate_kernel<T><<<nb(n), kKT, 0, st>>>(c.ctl, c.Z, c.x, n);
+    kry_spmv_kernel<T><<<nb(n * 8), kKT, 0, st>>>(c.ctl, 1, ks.rowptr, ks.col, c.val, c.x, c.b, c.w, n);
+    kry_norm_start_kernel<T><<<c.nred, kKT, 0, st>>>(ga, 1, 0, 0, 0.0);
+}
+
+// One Arnoldi step with the block-Jacobi (or learned, FP64) preconditioner.
+template <typename T>
+void arnoldi_step(KrylovSolver &ks, const Core<T> &c, KrylovPrecond pc, cudaStream_t st)
+{
+    const long n = c.n;
+    if constexpr (sizeof(T) == 8) {
+        if (pc == KrylovPrecond::learned) krylov_apply_learned(ks, st);
+        else if (ks.fp32_precond)
+            kry_bj_apply_kernel<float, double><<<nb(n), kKT, 0, st>>>(c.ctl, c.w, c.V, c.Z, ks.row_blk, ks.blk_start,
+                                                                     ks.blk_off, (const float *)ks.binv, n);
+        else
+            kry_bj_apply_kernel<double, double><<<nb(n), kKT, 0, st>>>(
+                c.ctl, c.w, c.V, c.Z, ks.row_blk, ks.blk_start, ks.blk_off, (const double *)ks.binv, n);
     } else {
-        kry_bj_apply_kernel<double><<<nb(n), kKT, 0, st>>>(ks.ctl, ks.w, ks.V, ks.Z, ks.row_blk, ks.blk_start,
-                                                           ks.blk_off, (const double *)ks.binv, n);
+        kry_bj_apply_kernel<float, float><<<nb(n), kKT, 0, st>>>(c.ctl, c.w, c.V, c.Z, ks.row_blk, ks.blk_start,
+                                                                ks.blk_off, (const float *)ks.binv, n);
     }
-    kry_spmv_kernel<<<nb(n * 8), kKT, 0, st>>>(ks.ctl, 0, ks.rowptr, ks.col, ks.val, ks.Z, nullptr, ks.w, n);
-    const GsArgs ga = gs_args(ks);
-    kry_gs_dots_kernel<<<ks.nred, kKT, 0, st>>>(ga);
-    kry_gs_update_kernel<<<ks.nred, kKT, 0, st>>>(ga, 0);
-    kry_gs_update_kernel<<<ks.nred, kKT, 0, st>>>(ga, 1);
-    kry_xupdate_kernel<<<nb(n), kKT, 0, st>>>(ks.ctl, ks.Z, ks.x, n);
-    kry_spmv_kernel<<<nb(n * 8), kKT, 0, st>>>(ks.ctl, 1, ks.rowptr, ks.col, ks.val, ks.x, ks.b, ks.w, n);
-    kry_norm_start_kernel<<<ks.nred, kKT, 0, st>>>(ga, 1, 0, 0, 0.0);
+    step_after_precond(ks, c, st);
 }
 
 constexpr int kStepLaunches = 8;
+
+// x = 0, w = b (already in c.b), |b|: the start of a solve
+template <typename T>
+void start_solve(const KrylovSolver &ks, const Core<T> &c, cudaStream_t st)
+{
+    CB_CUDA(cudaMemcpyAsync(c.w, c.b, sizeof(T) * c.n, cudaMemcpyDeviceToDevice, st));
+    CB_CUDA(cudaMemsetAsync(c.x, 0, sizeof(T) * c.n, st));
+    kry_norm_start_kernel<T><<<c.nred, kKT, 0, st>>>(gs_args(ks, c), 0, c.m, c.maxit, c.rtol);
+    CB_CUDA(cudaGetLastError());
+}
+
+void read_ctl(const KrylovCtl *dev, KrylovCtl *host, cudaStream_t st)
+{
+    CB_CUDA(cudaMemcpyAsync(host, dev, offsetof(KrylovCtl, hp), cudaMemcpyDeviceToHost, st));
+    CB_CUDA(cudaStreamSynchronize(st));
+}
+
+// A whole solve of c.b at one precision, chunks of Arnoldi steps replayed
+// (as a graph) until the control block reports the end.
+template <typename T>
+void core_solve(KrylovSolver &ks, Core<T> &c, bool use_graph, KrylovPrecond pc, long *launches, cudaStream_t st)
+{
+    start_solve(ks, c, st);
+    if (launches) *launches += 1;
+    if (use_graph && !*c.graph) {
+        cudaGraph_t g;
+        CB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < ks.chunk; ++k) arnoldi_step(ks, c, pc, st);
+        CB_CUDA(cudaStreamEndCapture(st, &g));
+        CB_CUDA(cudaGraphInstantiate(c.graph, g, 0));
+        cudaGraphDestroy(g);
+    }
+    const long max_chunks = c.maxit / ks.chunk + 2;
+    for (long chunks = 0;; ++chunks) {
+        if (use_graph) {
+            CB_CUDA(cudaGraphLaunch(*c.graph, st));
+        } else {
+            for (int k = 0; k < ks.chunk; ++k) arnoldi_step(ks, c, pc, st);
+            CB_CUDA(cudaGetLastError());
+        }
+        if (launches) *launches += (long)kStepLaunches * ks.chunk;
+        read_ctl(c.ctl, c.ctl_h, st);
+        if (c.ctl_h->done) break;
+        if (chunks > max_chunks) throw cb_status_error(CB_ERR_TIMEOUT, "the Krylov solve did not report an end");
+    }
+}
+
+// Nested precision: each outer (FP64) Arnoldi step is preconditioned by an
+// FP32 FGMRES solve with the FP32 matrix and block inverses.
+void nested_solve(KrylovSolver &ks, bool use_graph, long *launches, cudaStream_t st)
+{
+    Core<double> c = core64(ks, 0);
+    Core<float> in = core32(ks);
+    const long n = ks.n;
+    start_solve(ks, c, st);
+    read_ctl(c.ctl, c.ctl_h, st);
+    for (int steps = 0; !c.ctl_h->done; ++steps) {
+        if (steps > c.maxit + 1) throw cb_status_error(CB_ERR_TIMEOUT, "the Krylov solve did not report an end");
+        kry_outer_pre_kernel<<<nb(n), kKT, 0, st>>>(c.ctl, c.w, c.V, in.b, n);
+        core_solve(ks, in, use_graph, KrylovPrecond::block_jacobi, launches, st);
+        ks.inner_iterations += in.ctl_h->iters;
+        kry_outer_post_kernel<<<nb(n), kKT, 0, st>>>(c.ctl, in.x, c.Z, n);
+        step_after_precond(ks, c, st);
+        CB_CUDA(cudaGetLastError());
+        if (launches) *launches += 9;
+        read_ctl(c.ctl, c.ctl_h, st);
+    }
+}
 
 }  // namespace
 
@@ -635,37 +817,11 @@ int krylov_solve(KrylovSolver &ks, const double *b, double *x, cudaStream_t st, 
 {
     const long n = ks.n;
     CB_CUDA(cudaMemcpyAsync(ks.b, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    CB_CUDA(cudaMemcpyAsync(ks.w, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    CB_CUDA(cudaMemsetAsync(ks.x, 0, sizeof(double) * n, st));
-    kry_norm_start_kernel<<<ks.nred, kKT, 0, st>>>(gs_args(ks), 0, ks.m, ks.maxit, ks.rtol);
-    CB_CUDA(cudaGetLastError());
-    if (launches) *launches += 1;
-    const int gi = pc == KrylovPrecond::learned ? 1 : 0;
-    if (use_graph && !ks.step_graph[gi]) {
-        cudaGraph_t g;
-        CB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        for (int c = 0; c < ks.chunk; ++c) arnoldi_step(ks, pc, st);
-        CB_CUDA(cudaStreamEndCapture(st, &g));
-        CB_CUDA(cudaGraphInstantiate(&ks.step_graph[gi], g, 0));
-        cudaGraphDestroy(g);
-    }
-    const long max_chunks = ks.maxit / ks.chunk + 2;
-    const size_t head = offsetof(KrylovCtl, hp);
-    long chunks = 0;
-    for (;;) {
-        if (use_graph) {
-            CB_CUDA(cudaGraphLaunch(ks.step_graph[gi], st));
-        } else {
-            for (int c = 0; c < ks.chunk; ++c) arnoldi_step(ks, pc, st);
-            CB_CUDA(cudaGetLastError());
-        }
-        if (launches) *launches += (long)kStepLaunches * ks.chunk;
-        ++chunks;
-        CB_CUDA(cudaMemcpyAsync(ks.ctl_h, ks.ctl, head, cudaMemcpyDeviceToHost, st));
-        CB_CUDA(cudaStreamSynchronize(st));
-        if (ks.ctl_h->done) break;
-        if (chunks > max_chunks)
-            throw cb_status_error(CB_ERR_TIMEOUT, "the Krylov solve did not report an end");
+    if (ks.nested && pc == KrylovPrecond::block_jacobi) {
+        nested_solve(ks, use_graph, launches, st);
+    } else {
+        Core<double> c = core64(ks, pc == KrylovPrecond::learned ? 1 : 0);
+        core_solve(ks, c, use_graph, pc, launches, st);
     }
     CB_CUDA(cudaMemcpyAsync(x, ks.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     const KrylovCtl &c = *ks.ctl_h;

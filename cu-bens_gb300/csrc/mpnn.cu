@@ -766,6 +766,19 @@ void mpnn_push_pair(Mpnn &mp, const double *b, const double *t, cudaStream_t st)
     mp.count = std::min(mp.count + 1, mp.cap);
 }
 
+void mpnn_slot(Mpnn &mp, double **b, double **t)
+{
+    const size_t off = (size_t)mp.next * mp.neq;
+    *b = mp.pair_b + off;
+    *t = mp.pair_t + off;
+}
+
+void mpnn_commit_pair(Mpnn &mp)
+{
+    mp.next = (mp.next + 1) % mp.cap;
+    mp.count = std::min(mp.count + 1, mp.cap);
+}
+
 // `steps` Adam steps on stored pairs (one pair per step, newest first, then
 // back through the ring); returns the last loss.
 double mpnn_train(Mpnn &mp, const KrylovSolver &ks, int steps, cudaStream_t st)

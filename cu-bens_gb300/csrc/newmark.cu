@@ -115,7 +115,17 @@ void krylov_newmark_solve(cb_model *m)
         m->bj_iters += bj_solve();
         m->bj_solves++;
         PhaseTimer t(m, &m->tm.ms_train);
+        // the solve's own pair and three from inside its last Arnoldi cycle
+        // (the vectors the preconditioner is applied to)
         cb::mpnn_push_pair(*m->mp, m->r, m->dd, m->st);
+        const int nc = ks.ctl_h->ncols;
+        for (int k : {0, nc / 2, nc - 1}) {
+            if (k < 0 || nc <= 0) continue;
+            double *b = nullptr, *tt = nullptr;
+            cb::mpnn_slot(*m->mp, &b, &tt);
+            cb::krylov_basis_pair(ks, k, b, tt, m->st);
+            cb::mpnn_commit_pair(*m->mp);
+        }
         cb::mpnn_train(*m->mp, ks, m->learn_adam, m->st);
         return;
     }
@@ -405,6 +415,7 @@ int cb_get_krylov_stats(const cb_model *m, cb_krylov_stats *s)
     s->fallbacks = m->fallbacks;
     s->train_steps = cb::mpnn_adam_steps(m->mp);
     s->train_loss = cb::mpnn_last_loss(m->mp);
+    s->inner_iterations = ks.inner_iterations;
     return CB_OK;
 }
 

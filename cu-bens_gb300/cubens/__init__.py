@@ -66,7 +66,8 @@ class Timers(C.Structure):
 class KrylovStats(C.Structure):
     _fields_ = [("solves", C.c_long), ("iterations", C.c_long), ("unconverged", C.c_long),
                 ("last_iterations", C.c_int), ("last_residual", C.c_double), ("learned_solves", C.c_long),
-                ("fallbacks", C.c_long), ("train_steps", C.c_long), ("train_loss", C.c_double)]
+                ("fallbacks", C.c_long), ("train_steps", C.c_long), ("train_loss", C.c_double),
+                ("inner_iterations", C.c_long)]
 
 
 _lib = None

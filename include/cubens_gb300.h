@@ -55,7 +55,9 @@ enum cb_solver {
     CB_SOLVER_BAND = 0,   /* band LDL^T in the reference's equation order (skyfact/skysolve's
                              result; pivots give det and ssd) */
     CB_SOLVER_FGMRES = 1  /* FGMRES(m) with a nodal block-Jacobi preconditioner over a CSR
-                             product (nonlinear Newmark only: MSAL needs det and ssd) */
+                             product (nonlinear Newmark only: MSAL needs det and ssd). In
+                             CB_MIXED precision each FP64 Arnoldi step is preconditioned by
+                             an FP32 FGMRES(30) solve to 1e-4 with FP32 matrix and blocks */
 };
 
 /* Preconditioner of the FGMRES solver. */
@@ -175,6 +177,7 @@ typedef struct {
     long fallbacks;       /* network solves that stalled and were redone with block-Jacobi */
     long train_steps;     /* Adam steps taken by the network */
     double train_loss;    /* latest training loss (relative squared error) */
+    long inner_iterations; /* mixed precision: Arnoldi steps of the FP32 inner solves */
 } cb_krylov_stats;
 int cb_set_krylov_tolerance(cb_model *m, double rtol);
 int cb_get_krylov_stats(const cb_model *m, cb_krylov_stats *s);
