@@ -185,7 +185,8 @@ __global__ void kry_spmv_kernel(const KrylovCtl *__restrict__ ctl, int mode, con
 // reduced across blocks by the last block to arrive (fixed order, so the
 // sums do not depend on which block that is).
 
-constexpr int kWarps = kKT / 32;
+constexpr int kGT = 512;  // threads of the Gram-Schmidt blocks (more warps in flight, same reductions)
+constexpr int kWarps = kGT / 32;
 
 // true in every thread of the last block of the grid to get here
 __device__ bool last_block(unsigned *counter)
@@ -712,12 +713,12 @@ void step_after_precond(const KrylovSolver &ks, const Core<T> &c, cudaStream_t s
     const long n = c.n;
     kry_spmv_kernel<T><<<nb(n * 8), kKT, 0, st>>>(c.ctl, 0, ks.rowptr, ks.col, c.val, c.Z, nullptr, c.w, n);
     const GsArgs<T> ga = gs_args(ks, c);
-    kry_gs_dots_kernel<T><<<c.nred, kKT, 0, st>>>(ga);
-    kry_gs_update_kernel<T><<<c.nred, kKT, 0, st>>>(ga, 0);
-    kry_gs_update_kernel<T><<<c.nred, kKT, 0, st>>>(ga, 1);
+    kry_gs_dots_kernel<T><<<c.nred, kGT, 0, st>>>(ga);
+    kry_gs_update_kernel<T><<<c.nred, kGT, 0, st>>>(ga, 0);
+    kry_gs_update_kernel<T><<<c.nred, kGT, 0, st>>>(ga, 1);
     kry_xupdate_kernel<T><<<nb(n), kKT, 0, st>>>(c.ctl, c.Z, c.x, n);
     kry_spmv_kernel<T><<<nb(n * 8), kKT, 0, st>>>(c.ctl, 1, ks.rowptr, ks.col, c.val, c.x, c.b, c.w, n);
-    kry_norm_start_kernel<T><<<c.nred, kKT, 0, st>>>(ga, 1, 0, 0, 0.0);
+    kry_norm_start_kernel<T><<<c.nred, kGT, 0, st>>>(ga, 1, 0, 0, 0.0);
 }
 
 // One Arnoldi step with the block-Jacobi (or learned, FP64) preconditioner.
@@ -748,7 +749,7 @@ void start_solve(const KrylovSolver &ks, const Core<T> &c, cudaStream_t st)
 {
     CB_CUDA(cudaMemcpyAsync(c.w, c.b, sizeof(T) * c.n, cudaMemcpyDeviceToDevice, st));
     CB_CUDA(cudaMemsetAsync(c.x, 0, sizeof(T) * c.n, st));
-    kry_norm_start_kernel<T><<<c.nred, kKT, 0, st>>>(gs_args(ks, c), 0, c.m, c.maxit, c.rtol);
+    kry_norm_start_kernel<T><<<c.nred, kGT, 0, st>>>(gs_args(ks, c), 0, c.m, c.maxit, c.rtol);
     CB_CUDA(cudaGetLastError());
 }
 

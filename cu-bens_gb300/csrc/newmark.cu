@@ -112,7 +112,9 @@ void krylov_newmark_solve(cb_model *m)
     }
     const long train = m->learn_steps >= 0 ? m->learn_steps : std::max(1L, m->h.nsteps / 10);
     if (m->nm_k < train) {
-        m->bj_iters += bj_solve();
+        // the block-Jacobi work per solve: Arnoldi steps, inner ones included
+        const long inner0 = ks.inner_iterations;
+        m->bj_iters += bj_solve() + (ks.inner_iterations - inner0);
         m->bj_solves++;
         PhaseTimer t(m, &m->tm.ms_train);
         // the solve's own pair and three from inside its last Arnoldi cycle
