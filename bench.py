@@ -649,8 +649,11 @@ def run_ours(args, world, rank, local, pg):
                        "shell_force_ms": ms_force,
                        "shell_force_GBps": bytes_force / (ms_force * 1e-3) / 1e9,
                        "shell_force_fp64_GFLOPs": flops_force / (ms_force * 1e-3) / 1e9},
-            "roofline": {"kernel": "factor_f32_kernel (persistent band LDL^T, FP32, one grid barrier "
-                                   "per 32-column panel)",
+            "roofline": {"kernel": (f"factor_cluster_kernel (band LDL^T, FP32, one {info['factor_cluster']}-CTA "
+                                    "thread-block cluster, the band's window in distributed shared memory, one "
+                                    "cluster barrier per 32-column panel)") if info.get("factor_cluster") else
+                                   "factor_f32_kernel (persistent band LDL^T, FP32, one grid barrier per 32-column "
+                                   "panel)",
                          "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": None,
                          "bytes_per_launch": bytes_ldlt, "ms_per_launch": ms_ldlt,

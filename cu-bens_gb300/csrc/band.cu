@@ -29,6 +29,7 @@
 // coalesced row dots). A
 // larger s lowers the number of sequential steps while the bytes per step
 // (s*w) and per solve stay about the same.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -552,6 +553,255 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
     }
 }
 
+// LDL^T of a 32x32 block in shared memory by one warp in registers, without
+// the inverse of L (the panel rows are then formed by substitution). On
+// return A holds L below and D on the diagonal, di = 1/D.
+__device__ __noinline__ void ldlt32_noinv(float (*A)[NB + 1], float *di)
+{
+    const int lane = threadIdx.x % 32;
+    float r[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) r[j] = A[lane][j];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+        const float d = __shfl_sync(0xffffffffu, r[k], k);
+        const float rd = 1.0f / d;
+        const float l = lane > k ? r[k] * rd : 0.0f;
+        if (lane > k) r[k] = l;
+        const float ldk = l * d;
+#pragma unroll
+        for (int j = k + 1; j < NB; ++j) {
+            const float ljk = __shfl_sync(0xffffffffu, l, j);
+            if (j <= lane) r[j] -= ldk * ljk;
+        }
+    }
+    float dl = 0;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        A[lane][j] = j <= lane ? r[j] : 0.0f;
+        if (j == lane) dl = r[j];
+    }
+    di[lane] = 1.0f / dl;
+}
+
+// FP32 narrow bands: one thread-block cluster of C CTAs holds the active
+// window of the band in its distributed shared memory.
+//   - CTA o owns the 32-column blocks B = o, o + C, o + 2C, ...; block B lives
+//     in slot (B / C) % nslot of its owner (32 band columns, ld rows each,
+//     the band's own layout) from its load until it is factored;
+//   - panel b: its owner factors the diagonal block (ldlt32_noinv), forms
+//     the panel rows W (W L^T = A, by substitution) and L = W D^-1 into its
+//     slot, publishes W and 1/D in its shared memory, writes the finished
+//     block back to the band and loads the owned block (nslot - 1) C ahead
+//     into the slot it frees;
+//   -- cluster barrier --
+//   - every CTA applies A_ij -= sum_k W_ik W_jk / d_k to its own blocks in
+//     the window (b, b + nwin], reading W through distributed shared memory.
+// One hardware cluster barrier per panel and no grid-wide synchronisation;
+// each band entry is read from and written to HBM once. The owner of block
+// b+1 applies panel b to it before factoring it, in program order, so one
+// barrier per panel is enough: a CTA rewrites its W only C panels later,
+// after every CTA has passed C barriers.
+struct ClusterArgs {
+    FactorArgs<float> f;
+    int nslot, nwin;
+};
+
+constexpr int kClusterThreads = 256;
+constexpr int kWs = NB + 4;  // row stride of W rows in shared memory (16-byte aligned rows)
+
+// dst[e] = src[e] for e in [e0, e1) (float4), eight loads in flight per
+// thread before their stores (the source may be global or another CTA's
+// shared memory)
+__device__ __forceinline__ void copy4(float4 *dst, const float4 *src, long e0, long e1)
+{
+    const long step = blockDim.x;
+    for (long base = e0 + threadIdx.x; base < e1; base += 8 * step) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const long e = base + u * step;
+            if (e < e1) v[u] = src[e];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const long e = base + u * step;
+            if (e < e1) dst[e] = v[u];
+        }
+    }
+}
+
+__device__ __forceinline__ void copy_block_in(const float *__restrict__ band, long ld, long B, float *slot)
+{
+    copy4(reinterpret_cast<float4 *>(slot), reinterpret_cast<const float4 *>(band + (size_t)B * NB * ld), 0,
+          (long)NB * ld / 4);
+}
+
+__device__ __forceinline__ void copy_block_out(float *__restrict__ band, long ld, long B, const float *slot)
+{
+    float4 *dst = reinterpret_cast<float4 *>(band + (size_t)B * NB * ld);
+    const float4 *src = reinterpret_cast<const float4 *>(slot);
+    const long n4 = (long)NB * ld / 4;
+    for (long e = threadIdx.x; e < n4; e += blockDim.x) dst[e] = src[e];
+}
+
+// Panel row r (band row 32(b+1) + r of block b's columns): W_r L^T = A_r by
+// substitution with the unit-lower L of the diagonal block; W_r to wout,
+// L_r = W_r D^-1 over A_r in the slot.
+__device__ __noinline__ void panel_row(float *S, long ld, long bw, long r, const float (*L)[NB + 1],
+                                       const float *di, float *wout)
+{
+    float w[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        const long off = NB + r - c;
+        float x = off <= bw ? S[(size_t)c * ld + off] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < c; ++k) x -= w[k] * L[c][k];
+        w[c] = x;
+    }
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        const long off = NB + r - c;
+        wout[c] = w[c];
+        if (off <= bw) S[(size_t)c * ld + off] = w[c] * di[c];
+    }
+}
+
+// A_ij -= sum_k W_ik W_jk / d_k for the 32 columns j of a block (W rows of the
+// columns at panel row c0..c0+31) and its rows c0..r1-1 (panel rows), from
+// the W rows in Wl (local copy) and LjT[k][j] = W_jk / d_k. 128 rows per
+// pass, a 4x4 register block per thread.
+__device__ void update_block(float *S, long ld, long bw, const float *Wl, const float (*LjT)[kWs], long c0,
+                             long r1)
+{
+    const int tr = threadIdx.x >> 3, tc = threadIdx.x & 7;
+    for (long rb = c0; rb < r1; rb += 128) {
+        float acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+        long rr[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            rr[i] = rb + 4 * tr + i;
+            if (rr[i] >= r1) rr[i] = r1 - 1;  // clamped rows compute a copy, not stored
+        }
+#pragma unroll 8
+        for (int k = 0; k < NB; ++k) {
+            const float4 l = *reinterpret_cast<const float4 *>(&LjT[k][4 * tc]);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float w = Wl[rr[i] * kWs + k];
+                acc[i][0] += w * l.x;
+                acc[i][1] += w * l.y;
+                acc[i][2] += w * l.z;
+                acc[i][3] += w * l.w;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const long r = rb + 4 * tr + i;
+            if (r >= r1) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const long jj = 4 * tc + j;
+                const long off = r - (c0 + jj);
+                if (off >= 0 && off <= bw) S[(size_t)jj * ld + off] -= acc[i][j];
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kClusterThreads) factor_cluster_kernel(ClusterArgs ca)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const FactorArgs<float> &a = ca.f;
+    const int C = (int)cl.num_blocks(), o = (int)cl.block_rank();
+    const int nslot = ca.nslot;
+    const long ld = a.ld, bw = a.bw, nb = a.npad / NB;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    extern __shared__ float4 dsm4[];
+    float *slots = reinterpret_cast<float *>(dsm4);           // nslot x 32 x ld
+    float *Wb = slots + (size_t)nslot * NB * ld;               // bw x kWs: this CTA's last panel rows W
+    float *Wl = Wb + (size_t)bw * kWs;                         // bw x kWs: a local copy of the owner's W
+    float *dib = Wl + (size_t)bw * kWs;                        // 32: 1/D of this CTA's last panel
+    __shared__ float A[NB][NB + 1];
+    __shared__ float di[NB];
+    __shared__ __align__(16) float LjT[NB][kWs];  // L rows of the updated block's columns, k-major
+    for (int k = 0; k < nslot - 1; ++k) {
+        const long B = o + (long)k * C;
+        if (B < nb) copy_block_in(a.band, ld, B, slots + (size_t)k * NB * ld);
+    }
+    __syncthreads();
+    for (long b = 0; b < nb; ++b) {
+        const int owner = (int)(b % C);
+        long m = a.npad - NB * (b + 1);
+        if (m > bw) m = bw;
+        if (o == owner) {
+            const long kk = b / C;
+            float *S = slots + (size_t)(kk % nslot) * NB * ld;
+            for (int e = tid; e < NB * NB; e += blockDim.x) {
+                const int j = e / NB, i = e % NB;
+                A[i][j] = (i >= j && i - j <= bw) ? S[(size_t)j * ld + (i - j)] : 0.0f;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                ldlt32_noinv(A, di);
+                record_pivots(a, b * NB, A[lane][lane], di[lane], lane);
+            }
+            __syncthreads();
+            for (int e = tid; e < NB * NB; e += blockDim.x) {
+                const int j = e / NB, i = e % NB;
+                if (i >= j && i - j <= bw) S[(size_t)j * ld + (i - j)] = A[i][j];
+            }
+            for (long r = tid; r < m; r += blockDim.x) panel_row(S, ld, bw, r, A, di, Wb + r * kWs);
+            if (tid < NB) dib[tid] = di[tid];
+            __syncthreads();
+        }
+        cl.sync();
+        const long first = b + 1 + (((long)o - (b + 1)) % C + C) % C;  // first owned block after b
+        const bool work = first <= b + ca.nwin && first < nb && NB * (first - b - 1) < m;
+        if (work) {
+            // the owner's W rows from this block's first column on, one pass
+            const long c0f = NB * (first - b - 1);
+            const float4 *src = reinterpret_cast<const float4 *>(cl.map_shared_rank(Wb, owner));
+            float4 *dst = reinterpret_cast<float4 *>(Wl);
+            copy4(dst, src, c0f * (kWs / 4), m * (kWs / 4));
+            const float *dio = cl.map_shared_rank(dib, owner);
+            if (tid < NB) A[0][tid] = dio[tid];  // the owner's 1/D (A is free outside the owner's factor)
+            __syncthreads();
+            for (long B = first; B <= b + ca.nwin && B < nb; B += C) {
+                const long c0 = NB * (B - b - 1);
+                if (c0 >= m) break;
+                float *S = slots + (size_t)((B / C) % nslot) * NB * ld;
+                for (int e = tid; e < NB * NB; e += blockDim.x) {
+                    const int jj = e / NB, k = e % NB;
+                    LjT[k][jj] = c0 + jj < m ? Wl[(c0 + jj) * kWs + k] * A[0][k] : 0.0f;
+                }
+                __syncthreads();
+                long r1 = c0 + NB + bw;
+                if (r1 > m) r1 = m;
+                update_block(S, ld, bw, Wl, LjT, c0, r1);
+                __syncthreads();
+            }
+        }
+        if (o == owner) {
+            // the finished block to the band; the owned block nslot - 1 turns
+            // ahead into the slot of the previous one (finished and written)
+            const long kk = b / C;
+            copy_block_out(a.band, ld, b, slots + (size_t)(kk % nslot) * NB * ld);
+            const long Bn = b + (long)(nslot - 1) * C;
+            if (Bn < nb) copy_block_in(a.band, ld, Bn, slots + (size_t)((kk + nslot - 1) % nslot) * NB * ld);
+            __syncthreads();
+        }
+    }
+    // no CTA leaves while another may still read its shared memory
+    cl.sync();
+}
+
 // FP64 (the FP64 pipe is the bound): two grid barriers per panel.
 //   1. every CTA factors the diagonal block with all 256 threads (one
 //      elimination step per column, warp-uniform columns);
@@ -840,6 +1090,26 @@ void factor_band(BandFactor &f, cudaStream_t st, long *launches)
     const int dist = (f.fp32 && ntiles > 2L * grid) ? 1 : 0;
     FactorArgs<T> a{band, f.ld, f.bw, npad, f.n, (T *)f.dinv, f.ssd, f.flags, (T *)f.work, (T *)f.stage, f.fbar,
                     dist};
+    if constexpr (sizeof(T) == 4) {
+        if (f.cluster > 0) {
+            ClusterArgs ca{a, f.cluster_slots, f.cluster_nwin};
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)f.cluster);
+            cfg.blockDim = dim3(kClusterThreads);
+            cfg.dynamicSmemBytes = f.cluster_smem;
+            cfg.stream = st;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = (unsigned)f.cluster;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            CB_CUDA(cudaLaunchKernelEx(&cfg, factor_cluster_kernel, ca));
+            ++*launches;
+            return;
+        }
+    }
     void *args[] = {&a};
     const void *fn = f.fp32 ? (const void *)factor_f32_kernel<32> : (const void *)factor_f64_kernel<16>;
     CB_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(256), args, 0, st));
@@ -920,6 +1190,58 @@ int max_cooperative_grid(K kernel)
     CB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 256, 0));
     return std::max(1, sms * std::min(per, 4));
+}
+
+// The cluster factor for FP32 bands whose active window fits the
+// distributed shared memory of a cluster (16 CTAs, or 8 with more slots
+// each): (nslot - 1) C >= nwin blocks of the window.
+void choose_cluster(BandFactor &f)
+{
+    f.cluster = 0;
+    if (!f.fp32 || !f.use_cluster) return;
+    const int nwin = (int)((f.bw + NB - 1) / NB);
+    int dev = 0, optin = 0;
+    CB_CUDA(cudaGetDevice(&dev));
+    CB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa{};
+    CB_CUDA(cudaFuncGetAttributes(&fa, factor_cluster_kernel));
+    for (int C : {16, 8}) {
+        const int nslot = 1 + (nwin + C - 1) / C;
+        const size_t dyn = sizeof(float) * ((size_t)nslot * NB * f.ld + 2 * (size_t)f.bw * kWs + NB);
+        if (dyn + fa.sharedSizeBytes > (size_t)optin) continue;
+        if (C > 8 && cudaFuncSetAttribute(factor_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                         cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        // one attribute for every handle: the most dynamic shared memory a CTA may have
+        if (cudaFuncSetAttribute(factor_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 optin - (int)fa.sharedSizeBytes) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)C);
+        cfg.blockDim = dim3(kClusterThreads);
+        cfg.dynamicSmemBytes = dyn;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)C;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, factor_cluster_kernel, &cfg) != cudaSuccess || nclusters < 1) {
+            cudaGetLastError();
+            continue;
+        }
+        f.cluster = C;
+        f.cluster_slots = nslot;
+        f.cluster_nwin = nwin;
+        f.cluster_smem = dyn;
+        return;
+    }
 }
 
 template <typename T>
@@ -1032,12 +1354,13 @@ void band_profile_launch(BandFactor &f, int which, cudaStream_t st)
     CB_CUDA(cudaGetLastError());
 }
 
-void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct)
+void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use_cluster)
 {
     f.n = n;
     f.bw = std::max(1L, bw);
     f.fp32 = fp32;
     f.direct = direct;
+    f.use_cluster = use_cluster;
     f.ld = ((f.bw + 1 + 7) / 8) * 8;
     f.w = std::max(32L, ((f.bw + 31) / 32) * 32);
     const size_t es = fp32 ? 4 : 8;
@@ -1090,6 +1413,7 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct)
     }
     f.solve_grid_full = f.solve_grid;
     f.factor_grid = fp32 ? max_cooperative_grid(factor_f32_kernel<32>) : max_cooperative_grid(factor_f64_kernel<16>);
+    if (fp32) choose_cluster(f);
     f.bytes = es * ((size_t)f.ld * npad + npad + blocks * (2 * f.s + 2 * f.w) + work);
 }
 

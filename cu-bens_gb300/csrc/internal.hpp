@@ -146,6 +146,10 @@ struct BandFactor {
     int solve_grid = 1;          // CTAs of the cooperative solve launch
     int solve_grid_full = 1;     // ... when the handle has the GPU to itself
     int factor_grid = 1;         // most CTAs of the cooperative factor launch
+    bool use_cluster = false;    // FP32: the cluster factor where the band's window fits
+    int cluster = 0;             // CTAs of the cluster factor (0: the cooperative grid factor)
+    int cluster_slots = 0, cluster_nwin = 0;
+    size_t cluster_smem = 0;
     size_t bytes = 0;            // device memory held
     cudaGraphExec_t factor_graph = nullptr;
     long factor_launches = 0;
@@ -153,7 +157,7 @@ struct BandFactor {
 
 // direct: the factor serves one solve (Newmark's full Newton): the solve
 // substitutes with the band itself and no solve blocks are formed
-void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct = false);
+void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct = false, bool use_cluster = false);
 void band_free(BandFactor &f);
 // The band already holds an LDL^T factor (L below, D on the diagonal): form
 // 1/d and the solve blocks so that band_solve can use it.

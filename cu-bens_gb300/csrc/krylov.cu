@@ -185,8 +185,13 @@ __global__ void kry_spmv_kernel(const KrylovCtl *__restrict__ ctl, int mode, con
 // reduced across blocks by the last block to arrive (fixed order, so the
 // sums do not depend on which block that is).
 
-constexpr int kGT = 512;  // threads of the Gram-Schmidt blocks (more warps in flight, same reductions)
-constexpr int kWarps = kGT / 32;
+// Threads of the Gram-Schmidt blocks: 512 for FP64 (one block per SM; more
+// warps in flight for the same FP64 reductions), 256 for FP32 (four blocks
+// per SM).
+constexpr int kGTMax = 512;
+constexpr int kWarpsMax = kGTMax / 32;
+template <typename T>
+constexpr int gs_threads() { return sizeof(T) == 8 ? 512 : 256; }
 
 // true in every thread of the last block of the grid to get here
 __device__ bool last_block(unsigned *counter)
@@ -206,7 +211,8 @@ __device__ void block_dots(const T *__restrict__ V, const T *__restrict__ w, lon
                            T *__restrict__ partial, int nred)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = warp; k <= j; k += kWarps) {
+    const int nw = blockDim.x >> 5;
+    for (int k = warp; k <= j; k += nw) {
         const T *v = V + (size_t)k * n;
         T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
         long i = r0 + lane;
@@ -226,7 +232,7 @@ __device__ void block_dots(const T *__restrict__ V, const T *__restrict__ w, lon
 template <typename T>
 __device__ void block_norm(const T *__restrict__ w, long r0, long r1, T *__restrict__ partial)
 {
-    __shared__ T red[kWarps];
+    __shared__ T red[kWarpsMax];
     T acc = 0;
     for (long i = r0 + threadIdx.x; i < r1; i += blockDim.x) acc += w[i] * w[i];
     acc = warp_sum(acc);
@@ -234,7 +240,7 @@ __device__ void block_norm(const T *__restrict__ w, long r0, long r1, T *__restr
     __syncthreads();
     if (threadIdx.x == 0) {
         T sum = 0;
-        for (int k = 0; k < kWarps; ++k) sum += red[k];
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) sum += red[k];
         partial[blockIdx.x] = sum;
     }
 }
@@ -264,8 +270,8 @@ __device__ __forceinline__ double warp_sum_partials(const T *__restrict__ pk, in
 template <typename T>
 __device__ void reduce_hp(KrylovCtl *ctl, const T *partial, int nred, int j, int pass)
 {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = warp; k <= j; k += kWarps) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int k = warp; k <= j; k += nw) {
         const double acc = warp_sum_partials(partial + (size_t)k * nred, nred);
         if (lane == 0) {
             ctl->hp[k] = acc;
@@ -713,12 +719,12 @@ void step_after_precond(const KrylovSolver &ks, const Core<T> &c, cudaStream_t s
     const long n = c.n;
     kry_spmv_kernel<T><<<nb(n * 8), kKT, 0, st>>>(c.ctl, 0, ks.rowptr, ks.col, c.val, c.Z, nullptr, c.w, n);
     const GsArgs<T> ga = gs_args(ks, c);
-    kry_gs_dots_kernel<T><<<c.nred, kGT, 0, st>>>(ga);
-    kry_gs_update_kernel<T><<<c.nred, kGT, 0, st>>>(ga, 0);
-    kry_gs_update_kernel<T><<<c.nred, kGT, 0, st>>>(ga, 1);
+    kry_gs_dots_kernel<T><<<c.nred, gs_threads<T>(), 0, st>>>(ga);
+    kry_gs_update_kernel<T><<<c.nred, gs_threads<T>(), 0, st>>>(ga, 0);
+    kry_gs_update_kernel<T><<<c.nred, gs_threads<T>(), 0, st>>>(ga, 1);
     kry_xupdate_kernel<T><<<nb(n), kKT, 0, st>>>(c.ctl, c.Z, c.x, n);
     kry_spmv_kernel<T><<<nb(n * 8), kKT, 0, st>>>(c.ctl, 1, ks.rowptr, ks.col, c.val, c.x, c.b, c.w, n);
-    kry_norm_start_kernel<T><<<c.nred, kGT, 0, st>>>(ga, 1, 0, 0, 0.0);
+    kry_norm_start_kernel<T><<<c.nred, gs_threads<T>(), 0, st>>>(ga, 1, 0, 0, 0.0);
 }
 
 // One Arnoldi step with the block-Jacobi (or learned, FP64) preconditioner.
@@ -749,7 +755,7 @@ void start_solve(const KrylovSolver &ks, const Core<T> &c, cudaStream_t st)
 {
     CB_CUDA(cudaMemcpyAsync(c.w, c.b, sizeof(T) * c.n, cudaMemcpyDeviceToDevice, st));
     CB_CUDA(cudaMemsetAsync(c.x, 0, sizeof(T) * c.n, st));
-    kry_norm_start_kernel<T><<<c.nred, kGT, 0, st>>>(gs_args(ks, c), 0, c.m, c.maxit, c.rtol);
+    kry_norm_start_kernel<T><<<c.nred, gs_threads<T>(), 0, st>>>(gs_args(ks, c), 0, c.m, c.maxit, c.rtol);
     CB_CUDA(cudaGetLastError());
 }
 

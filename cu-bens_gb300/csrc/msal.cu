@@ -186,7 +186,7 @@ void upload_model(cb_model *m)
     }
     // Newmark refactors every iteration and solves once per factorisation:
     // direct substitution, no solve blocks
-    cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5);
+    cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5, m->opt.factor_kernel == 1);
     m->bytes += m->bf.bytes;
     cb::build_tangent_map(h, m->bf.ld, tm);
     m->tmap_n = (long)tm.dst.size();
@@ -735,6 +735,7 @@ int cb_model_info(const cb_model *m, cb_info *info)
     info->solver = m->ks ? CB_SOLVER_FGMRES : CB_SOLVER_BAND;
     info->nnz = m->ks ? m->ks->nnz : 0;
     info->node_blocks = m->ks ? m->ks->nblk : 0;
+    info->factor_cluster = m->bf.cluster;
     return CB_OK;
 }
 

@@ -40,7 +40,7 @@ class CubensError(RuntimeError):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("use_graphs", C.c_int),
                 ("solver", C.c_int), ("krylov_restart", C.c_int), ("krylov_maxit", C.c_int),
-                ("precond", C.c_int), ("reserved", C.c_int * 1)]
+                ("precond", C.c_int), ("factor_kernel", C.c_int)]
 
 
 class Info(C.Structure):
@@ -48,7 +48,7 @@ class Info(C.Structure):
                 ("neq", C.c_long), ("lss", C.c_long), ("bandwidth", C.c_long), ("block", C.c_long),
                 ("nblocks", C.c_long), ("dkdof", C.c_long), ("device_bytes", C.c_size_t),
                 ("h2d_bytes", C.c_size_t), ("algflag", C.c_int), ("nsteps", C.c_long), ("dt", C.c_double),
-                ("solver", C.c_int), ("nnz", C.c_long), ("node_blocks", C.c_long)]
+                ("solver", C.c_int), ("nnz", C.c_long), ("node_blocks", C.c_long), ("factor_cluster", C.c_int)]
 
 
 class Step(C.Structure):
@@ -166,7 +166,7 @@ class Model:
 
     def __init__(self, model_def: str, precision: int = FP64, device: int = 0, use_graphs: bool = True,
                  solver: int = SOLVER_BAND, restart: int = 0, maxit: int = 0,
-                 precond: int = PRECOND_BLOCK_JACOBI, rtol: float | None = None):
+                 precond: int = PRECOND_BLOCK_JACOBI, rtol: float | None = None, factor_kernel: int = 0):
         L = load()
         opt = Options()
         L.cb_default_options(C.byref(opt))
@@ -177,6 +177,7 @@ class Model:
         opt.krylov_restart = restart
         opt.krylov_maxit = maxit
         opt.precond = precond
+        opt.factor_kernel = factor_kernel
         h = C.c_void_p()
         raw = model_def.encode()
         rc = L.cb_model_create(raw, len(raw), C.byref(opt), C.byref(h))

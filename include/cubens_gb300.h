@@ -76,7 +76,10 @@ typedef struct {
     int krylov_restart;  /* FGMRES restart length m (0: 50; at most 64) */
     int krylov_maxit;    /* FGMRES steps per solve before it gives up (0: 2000) */
     int precond;         /* enum cb_precond (FGMRES) */
-    int reserved[1];
+    int factor_kernel;   /* band LDL^T in FP32: 0 the cooperative grid factor; 1 the
+                            thread-block-cluster factor where the band's window fits a cluster's
+                            distributed shared memory (measured slower on GB300: the grid factor
+                            stays the default) */
 } cb_options;
 
 typedef struct {
@@ -95,6 +98,8 @@ typedef struct {
     int solver;                    /* enum cb_solver in use */
     long nnz;                      /* FGMRES: stored entries of the CSR matrix (both triangles) */
     long node_blocks;              /* FGMRES: block-Jacobi blocks */
+    int factor_cluster;            /* band LDL^T: CTAs of the thread-block-cluster factor (0: the
+                                      cooperative grid factor) */
 } cb_info;
 
 /* Result of one converged increment or time step (what output() records,

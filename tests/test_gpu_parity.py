@@ -11,6 +11,7 @@ import pytest
 
 import cubens
 import oracle
+from cubens import models
 
 pytestmark = pytest.mark.gpu
 
@@ -139,3 +140,49 @@ def test_benchmark_panel64_matches_oracle():
     mx = cubens.Model(text, precision=cubens.MIXED).run(steps)
     np.testing.assert_array_equal(mx["its"], o["its"])
     assert _rel(mx["lam"], o["lam"]) < 1e-5
+
+
+def test_cluster_factor_matches_grid_factor_and_oracle():
+    """The FP32 band LDL^T as one thread-block cluster (the window of the band
+    in distributed shared memory) and as the cooperative grid kernel: the
+    oracle's iteration counts on the benchmark panel, curves within the mixed
+    tolerance, the cluster run reproducible bit for bit, and one factor+solve
+    of a small panel against the FP64 factor."""
+    import bench
+    text, _ = bench.panel_text(64)
+    steps = 5
+    o = oracle.OracleModel(text).msal(steps)
+    cl = cubens.Model(text, precision=cubens.MIXED, factor_kernel=1)
+    assert cl.info["factor_cluster"] in (8, 16)
+    a = cl.run(steps)
+    gr = cubens.Model(text, precision=cubens.MIXED)
+    assert gr.info["factor_cluster"] == 0
+    b = gr.run(steps)
+    for r in (a, b):
+        np.testing.assert_array_equal(r["its"], o["its"])
+        assert _rel(r["lam"], o["lam"]) < 1e-5
+    a2 = cubens.Model(text, precision=cubens.MIXED, factor_kernel=1).run(steps)
+    assert np.array_equal(a["d"], a2["d"])
+
+
+def test_cluster_factor_solve_against_reference(golden_dir):
+    """One FP32 factor+solve of the reference's own tangent (skyfact/skysolve
+    golden vectors) by the cluster kernel and by the grid kernel: the same
+    determinant flag, pivots and solution to FP32 accuracy (norm-wise: the
+    drilling pivots, 1e-4 of the others, lose relative digits in FP32 in
+    both kernels)."""
+    z = np.load(golden_dir / "elem_shell_panel8.npz")
+    q = oracle.OracleModel(str(z["model_def"])).q
+    out, errs = [], []
+    for fk in (1, 0):
+        m = cubens.Model(str(z["model_def"]), precision=cubens.MIXED, factor_kernel=fk)
+        assert (m.info["factor_cluster"] > 0) == (fk == 1)
+        m.eval_tangent(z["x_after"], z["c_i"], z["area_i"])
+        v, ssd, det = m.factor_solve(q)
+        assert det == int(z["det"])
+        errs.append((np.linalg.norm(ssd - z["ssd"]) / np.linalg.norm(z["ssd"]),
+                     np.linalg.norm(v - z["ldlt_solution"]) / np.linalg.norm(z["ldlt_solution"])))
+        out.append(v)
+    for e_ssd, e_v in errs:
+        assert e_ssd < 2e-4 and e_v < 1e-3, errs
+    assert np.linalg.norm(out[0] - out[1]) / np.linalg.norm(out[1]) < 1e-3, errs
