@@ -28,7 +28,7 @@ struct HostModel {
     std::vector<double> fr_prop;  // NE_FR*8, per member: E, G, rho, A, I strong, I weak, J, I warping
     std::vector<double> fr_aux;   // NE_FR*3 auxiliary points
     std::vector<long> fr_mc;      // NE_FR*14 1-based equation numbers (0 = fixed), warping per member
-    int alg = 3;                  // ALGFLAG: 3 MSAL, 5 nonlinear Newmark
+    int alg = 3;                  // ALGFLAG: 1 NR, 2 modified NR, 3 MSAL, 5 nonlinear Newmark
     // nonlinear Newmark input (main.c:1600-1607, 3320-3326; load, model.c:1492-1609)
     long ntin = 0;                // input time points
     long nsteps = 0;              // NTSTPS = (long)(ttot/dt + 1)
@@ -357,6 +357,7 @@ struct MsalScalars {
     int convchk;         // misc.c:187-250
     int test_err;        // 1 when a denominator of the test is zero
     double toldisp, tolforc, tolener, intener1;
+    int intener_first;   // the test takes intener1 from this iteration's dd . (qtot - f_ip) (static NR)
 };
 
 constexpr int kRedBlocks = 148;  // fixed partial-sum grid: bit-reproducible reductions

@@ -86,6 +86,11 @@ struct cb_model {
     // FP64 element tangents and the refinement vectors (r, correction, scratch)
     double *band64 = nullptr, *kel64 = nullptr, *ref_r = nullptr, *ref_x = nullptr, *ref_w = nullptr;
     int nm_phase = 0;       // 0 not started, 1 running, 2 finished
+    // static Newton-Raphson load control (main.c:1820-2157)
+    int nr_phase = 0;       // 0 not started, 1 running
+    long nr_incs = 0;       // converged increments
+    double nr_lpf = 0, nr_dlpf = 0;
+    int nr_solcnt = 0, nr_subcnt = 0;
     long nm_k = 0;          // next time step
     double nm_ddt = 1;      // time increment multiplier carried between steps (main.c:3452)
 

@@ -58,9 +58,10 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         status = CB_ERR_UNSUPPORTED;
         return "only ANAFLAG 2 (second-order elastic) is on the GPU path";
     }
-    if (alg != 3 && alg != 5) {
+    if (alg != 1 && alg != 2 && alg != 3 && alg != 5) {
         status = CB_ERR_UNSUPPORTED;
-        return "only ALGFLAG 3 (modified spherical arc length) and 5 (nonlinear Newmark) are on the GPU path";
+        return "only ALGFLAG 1 and 2 (static Newton-Raphson, modified Newton-Raphson), 3 (modified spherical "
+               "arc length) and 5 (nonlinear Newmark) are on the GPU path";
     }
     m.alg = alg;
     if (alg == 5) {
@@ -349,6 +350,23 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         }
     }
     if (!any_load) return "no forces present in input file";
+    if (alg == 1 || alg == 2) {
+        // load-control parameters (main.c:1809-1812)
+        m.lpfmax = t.next();
+        m.lpf0 = t.next();
+        m.dlpf0 = t.next();
+        m.dlpfmax = t.next();
+        m.dlpfmin = t.next();
+        m.itemax = (int)t.next();
+        m.submax = (int)t.next();
+        m.solmin = (int)t.next();
+        m.toldisp = t.next();
+        m.tolforc = t.next();
+        m.tolener = t.next();
+        if (!t.ok) return "model_def ended inside the Newton-Raphson controls";
+        status = CB_OK;
+        return "";
+    }
     long jt = (long)t.next();
     long dir = (long)t.next();
     m.dk = t.next();

@@ -184,9 +184,9 @@ void upload_model(cb_model *m)
         CB_CUDA(cudaStreamSynchronize(st));
         return;
     }
-    // Newmark refactors every iteration and solves once per factorisation:
-    // direct substitution, no solve blocks
-    cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5, m->opt.factor_kernel == 1);
+    // Newmark and full Newton-Raphson refactor every iteration and solve once
+    // per factorisation: direct substitution, no solve blocks
+    cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5 || h.alg == 1, m->opt.factor_kernel == 1);
     m->bytes += m->bf.bytes;
     cb::build_tangent_map(h, m->bf.ld, tm);
     m->tmap_n = (long)tm.dst.size();
@@ -299,8 +299,26 @@ void assemble_tangent_t(cb_model *m, TangentState which)
     const long E = m->h.ne_sh, T = m->h.ne_tr, F = m->h.ne_fr;
     cb::BandFactor &bf = m->bf;
     K *k = (K *)m->kel;
-    if (E) cb::launch_shell_tangent<K>(m->sh, m->x_c, k, E, m->st);
-    if (T) cb::launch_truss_tangent<K>(m->tr, k + 171 * E, T, m->st);
+    if (which == TangentState::converged) {
+        if (E) cb::launch_shell_tangent<K>(m->sh, m->x_c, k, E, m->st);
+        if (T) cb::launch_truss_tangent<K>(m->tr, k + 171 * E, T, m->st);
+    } else {
+        // the latest iteration's state (stiff_sh with x_temp, c_ip, deffarea_ip;
+        // stiff_tr with defllen_ip, c_ip, ef_ip: main.c:1897-1919)
+        if (E) {
+            cb::DevShell s = m->sh;
+            s.c_c = m->sh.c_ip;
+            s.a_c = m->sh.a_i;
+            cb::launch_shell_tangent<K>(s, m->x_t, k, E, m->st);
+        }
+        if (T) {
+            cb::DevTruss t = m->tr;
+            t.len_c = m->tr.len_i;
+            t.dir_c = m->tr.dir_i;
+            t.n_c = m->tr.n_i;
+            cb::launch_truss_tangent<K>(t, k + 171 * E, T, m->st);
+        }
+    }
     if (F) {
         const cb::DevFrame &fr = m->fr;
         const bool conv = which == TangentState::converged;
@@ -669,8 +687,9 @@ int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb
         return CB_ERR_ARG;
     }
     if (m->opt.solver == CB_SOLVER_FGMRES && m->h.alg != 5) {
-        m->err = "the FGMRES solver serves the nonlinear Newmark driver; MSAL needs the pivots of a "
-                 "factorisation (det, ssd)";
+        m->err = "the FGMRES solver serves the nonlinear Newmark driver (its effective stiffness is "
+                 "mass-shifted); MSAL needs the pivots of a factorisation (det, ssd), and static "
+                 "Newton-Raphson keeps the direct solve";
         *out = m;
         return CB_ERR_UNSUPPORTED;
     }

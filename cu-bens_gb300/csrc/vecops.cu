@@ -188,6 +188,12 @@ __global__ void test_kernel(const double *partial, MsalScalars *sc)
     __syncthreads();
     if (threadIdx.x != 0) return;
     for (int k = 0; k < 7; ++k) sc->dots[k] = d[k];
+    if (sc->intener_first) {
+        // first iteration of a Newton-Raphson increment: intener1 = dd . (qtot - fp), and fp
+        // is f_ip then (main.c:1975-1981)
+        sc->intener1 = d[4];
+        sc->intener_first = 0;
+    }
     int conv = 0, err = 0;
     if (sc->toldisp < 1) {
         if (d[1] != 0) {

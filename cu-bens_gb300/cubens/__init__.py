@@ -107,6 +107,8 @@ def load(path: Path | None = None):
     L.cb_factor_solve.argtypes = [vp, dp, dp, dp, ip]
     L.cb_solve_noalloc.argtypes = [vp, vp, vp]
     L.cb_batch_msal.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.POINTER(Step), ip]
+    L.cb_newton_begin.argtypes = [vp]
+    L.cb_newton_step.argtypes = [vp, C.POINTER(Step)]
     L.cb_newmark_begin.argtypes = [vp]
     L.cb_newmark_step.argtypes = [vp, C.POINTER(Step)]
     L.cb_newmark_state.argtypes = [vp, dp, dp, dp]
@@ -250,6 +252,30 @@ class Model:
                     d=np.array(ds) if with_d else None)
 
     # ---- nonlinear Newmark (ALGFLAG 5) ----
+    def newton_begin(self):
+        self._check(load().cb_newton_begin(self.h))
+
+    def newton_step(self) -> StepResult:
+        return self._step(load().cb_newton_step)
+
+    def run_newton(self, steps: int = 10_000, with_d: bool = True):
+        """Static (modified) Newton-Raphson: lam, its, res, d per converged increment."""
+        self.newton_begin()
+        lam, its, res, ds = [], [], [], []
+        for _ in range(steps):
+            r = self.newton_step()
+            if r.done:
+                break
+            lam.append(r.lam)
+            its.append(r.iterations)
+            res.append(r.residual)
+            if with_d:
+                ds.append(self.displacements()[0])
+        out = {"lam": np.array(lam), "its": np.array(its), "res": np.array(res)}
+        if with_d:
+            out["d"] = np.array(ds)
+        return out
+
     def newmark_begin(self):
         self._check(load().cb_newmark_begin(self.h))
 

@@ -55,6 +55,37 @@ class MsalControls:
 
 
 @dataclass
+class NewtonControls:
+    """Static load-control parameters of the Newton-Raphson (alg 1) and
+    modified Newton-Raphson (alg 2) loops, in the order main.c:1809-1812
+    reads them."""
+
+    alg: int = 1          # ALGFLAG: 1 Newton-Raphson, 2 modified Newton-Raphson
+    lpfmax: float = 1.0
+    lpf: float = 0.1
+    dlpf: float = 0.1
+    dlpfmax: float = 0.2
+    dlpfmin: float = 0.0125
+    itemax: int = 20
+    submax: int = 8
+    solmin: int = 2
+    toldisp: float = 1e-8
+    tolforc: float = 1.0
+    tolener: float = 1e-8
+
+    def lines(self) -> list[str]:
+        return [
+            f"{self.lpfmax!r},{self.lpf!r},{self.dlpf!r},{self.dlpfmax!r},{self.dlpfmin!r}",
+            f"{self.itemax},{self.submax},{self.solmin}",
+            f"{self.toldisp!r},{self.tolforc!r},{self.tolener!r}",
+        ]
+
+
+def _alg(controls) -> str:
+    return str(controls.alg) if isinstance(controls, NewtonControls) else "3"
+
+
+@dataclass
 class ModelSpec:
     name: str
     text: str
@@ -120,7 +151,7 @@ def space_truss(bays: int = 10, bay: float = 3.0, depth: float = 1.5,
         controls = MsalControls(joint=centre, direction=3, dk=-0.005,
                                 toldisp=1e-10, tolforc=1.0, tolener=1e-10,
                                 itemax=20)
-    out = ["2", "3", "0", "1", str(len(nodes)), f"{len(el)},0,0,0,0"]
+    out = ["2", _alg(controls), "0", "1", str(len(nodes)), f"{len(el)},0,0,0,0"]
     out += [f"{a},{b}" for a, b in el]
     out += cons + ["0,0"]
     out += [f"{_fmt(x)},{_fmt(y)},{_fmt(z)}" for x, y, z in nodes]
@@ -195,7 +226,7 @@ def cylindrical_panel(n: int = 64, seed: int | None = None, imperfection: float 
     centre = idx(n // 2, n // 2)
     if controls is None:
         controls = MsalControls(joint=centre, direction=3, dk=-0.5)
-    out = ["2", "3", "0", "1", str(len(nodes)), f"0,0,{len(tris)},0,0"]
+    out = ["2", _alg(controls), "0", "1", str(len(nodes)), f"0,0,{len(tris)},0,0"]
     out += [f"{a},{b},{c}" for a, b, c in tris]
     out += cons + ["0,0"]
     out += [f"{_fmt(x)},{_fmt(y)},{_fmt(z)}" for x, y, z in nodes]
@@ -328,7 +359,7 @@ def frame_building(bays_x: int = 20, bays_y: int = 20, storeys: int = 30,
         aux.append(",".join(_fmt(x0[k] + off[k]) for k in range(3)))
     face = lambda s: [jid(0, j, s) for j in range(by + 1)]  # noqa: E731
     dynamic = msal is None
-    out = ["2", "5" if dynamic else "3"]
+    out = ["2", "5" if dynamic else _alg(msal)]
     if dynamic:
         out.append("0,0")                     # CHKPT, RFLAG
     out += ["0", "1", str(len(nodes)), f"0,{len(members)},0,0,0"]

@@ -92,7 +92,7 @@ typedef struct {
     long dkdof;                    /* 0-based DOF of the prescribed displacement */
     size_t device_bytes;           /* GPU memory held by the handle */
     size_t h2d_bytes;              /* bytes copied host -> device when the model was created */
-    int algflag;                   /* 3: MSAL model, 5: nonlinear Newmark model */
+    int algflag;                   /* 1, 2: static (modified) Newton-Raphson, 3: MSAL, 5: nonlinear Newmark */
     long nsteps;                   /* Newmark: time steps NTSTPS (main.c:3361) */
     double dt;                     /* Newmark: time step */
     int solver;                    /* enum cb_solver in use */
@@ -157,6 +157,19 @@ int cb_get_displacements(const cb_model *m, double *d, double *lam);
  * handle's code. The handles must be distinct and not used by others
  * meanwhile. */
 int cb_batch_msal(cb_model **models, int n, int steps, int threads, cb_step *out, int *status);
+
+/* Static Newton-Raphson (ALGFLAG 1) and modified Newton-Raphson (ALGFLAG 2)
+ * under load control (main.c:1820-2157). cb_newton_begin sets the undeformed
+ * state (main.c:1672-1711); each cb_newton_step runs the passes of
+ * main.c:1822-2150 until one load increment converges (subdivisions
+ * included) and returns CB_OK with its record (lam = lpf), or out->done = 1
+ * once lpf has passed lpfmax. Errors: CB_ERR_DIVERGED for the reference's
+ * "maximum allowable load proportionality factor attempted without
+ * convergence", "minimum allowable increment of load proportionality factor
+ * reached" and "maximum allowable number of subdivisions exceeded";
+ * CB_ERR_NUMERIC for a zero pivot or a zero norm in the test. */
+int cb_newton_begin(cb_model *m);
+int cb_newton_step(cb_model *m, cb_step *out);
 
 /* Nonlinear Newmark (ALGFLAG 5, frame models). cb_newmark_begin sets the
  * initial state of main.c:3398-3447 (zero motion); each cb_newmark_step runs

@@ -7,7 +7,9 @@ unmodified from its sources by ``make -C oracle ref``:
   MSAL loop) run on seeded models, with every converged step's lambda,
   iteration count and FP64 displacement vector dumped by the output() shim;
   The Newmark fixtures run main.c's ALGFLAG 5 loop the same way and record,
-  per time step, the time (in the "lam" slot), iteration count and d;
+  per time step, the time (in the "lam" slot), iteration count and d; the
+  Newton-Raphson fixtures (ALGFLAG 1 and 2) record every converged load
+  increment's lpf, iteration count and d;
 * element fixtures: the reference's prop_sh/prop_tr/prop_fr, updatc,
   forces_sh, forces_tr, forces_fr, stiff_sh, stiff_tr, stiff_fr, mass_fr,
   skyfact and skysolve called through oracle/_ref/libcuben_ref_elem.so on
@@ -88,6 +90,36 @@ def whole_runs():
                             steps=r["steps"], iterations=r["iterations"], lam=r["lam"],
                             d=r["d"], neq=r["neq"])
         print(name, "neq", r["neq"], "steps", len(r["lam"]), "its", r["iterations"].tolist())
+
+
+def newton_cases():
+    """Static Newton-Raphson (alg 1) and modified Newton-Raphson (alg 2) runs:
+    load control below the panel's limit point, and the truss."""
+    N = models.NewtonControls
+    return {
+        "truss_nr": (models.space_truss(controls=N(alg=1, lpfmax=1.5, lpf=0.1, dlpf=0.1, dlpfmax=0.4,
+                                                   toldisp=1e-10, tolener=1e-10)), 20),
+        "truss_mnr": (models.space_truss(controls=N(alg=2, lpfmax=1.5, lpf=0.1, dlpf=0.1, dlpfmax=0.4, itemax=60,
+                                                    toldisp=1e-10, tolener=1e-10)), 20),
+        "panel8_nr": (models.cylindrical_panel(8, controls=N(alg=1, lpfmax=85.0, lpf=10.0, dlpf=10.0, dlpfmax=20.0,
+                                                             dlpfmin=0.625, toldisp=1e-5, tolener=1.0)), 20),
+        "panel8_mnr": (models.cylindrical_panel(8, controls=N(alg=2, lpfmax=60.0, lpf=10.0, dlpf=10.0,
+                                                              dlpfmax=20.0, dlpfmin=0.625, itemax=100,
+                                                              toldisp=1e-5, tolener=1.0)), 20),
+    }
+    # Frames are left out: on the frame buildings the reference's static loop
+    # reports a non-positive pivot, solves on the partly factored matrix
+    # (solve ignores skyfact's error) and returns NaN displacements.
+
+
+def newton_runs():
+    for name, (m, steps) in newton_cases().items():
+        r = refrun.run(m.text, steps, timeout=600)
+        assert r["returncode"] == 0 and len(r["lam"]) > 0, r["results1"][-400:]
+        np.savez_compressed(OUT / f"run_{name}.npz", model_def=np.array(m.text),
+                            steps=r["steps"], iterations=r["iterations"], lam=r["lam"],
+                            d=r["d"], neq=r["neq"], results_tail=np.array(r["results1"][-200:]))
+        print(name, "neq", r["neq"], "incs", len(r["lam"]), "its", r["iterations"].tolist())
 
 
 class RefElem:
@@ -338,3 +370,4 @@ if __name__ == "__main__":
     shell_element_fixture()
     truss_element_fixture()
     whole_runs()
+    newton_runs()

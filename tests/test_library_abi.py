@@ -105,3 +105,24 @@ def test_fgmres_is_refused_for_msal_models_before_upload(lib):
     rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
     lib.cb_model_destroy(h)
     assert rc == 1
+
+
+def test_newton_raphson_models_parse_and_fgmres_is_refused_for_them(lib):
+    """ALGFLAG 1 and 2 (static load control) pass the parser: without a GPU
+    the create call gets as far as the device check. FGMRES is refused for
+    them before any upload."""
+    from cubens import models
+    for alg in (1, 2):
+        text = models.space_truss(controls=models.NewtonControls(alg=alg)).text.encode()
+        opt = cubens.Options()
+        lib.cb_default_options(C.byref(opt))
+        h = C.c_void_p()
+        rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
+        msg = lib.cb_last_error(h).decode()
+        lib.cb_model_destroy(h)
+        assert rc in (0, 3), (rc, msg)  # 3: no CUDA device here
+        opt.solver = cubens.SOLVER_FGMRES
+        h = C.c_void_p()
+        rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
+        lib.cb_model_destroy(h)
+        assert rc == 4
