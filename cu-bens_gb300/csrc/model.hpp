@@ -33,6 +33,8 @@ struct cb_status_error : std::runtime_error {
     cb_status_error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
 
+struct cb_results_state;
+
 struct cb_model {
     cb::HostModel h;
     cb_options opt{};
@@ -93,6 +95,8 @@ struct cb_model {
     int nr_solcnt = 0, nr_subcnt = 0;
     long nm_k = 0;          // next time step
     double nm_ddt = 1;      // time increment multiplier carried between steps (main.c:3452)
+
+    cb_results_state *results = nullptr;  // open results*.txt files (results.cpp)
 
     // timing
     bool timing = false;

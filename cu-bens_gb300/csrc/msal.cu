@@ -716,6 +716,7 @@ int cb_model_destroy(cb_model *m)
 {
     if (!m) return CB_ERR_ARG;
     if (m->st) cudaStreamSynchronize(m->st);
+    cb_results_close(m);
     cb::band_free(m->bf);
     if (m->ks) {
         cb::krylov_free(*m->ks);

@@ -107,6 +107,9 @@ def load(path: Path | None = None):
     L.cb_factor_solve.argtypes = [vp, dp, dp, dp, ip]
     L.cb_solve_noalloc.argtypes = [vp, vp, vp]
     L.cb_batch_msal.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.POINTER(Step), ip]
+    L.cb_results_open.argtypes = [vp, C.c_char_p]
+    L.cb_results_write.argtypes = [vp, C.c_double, C.c_int]
+    L.cb_results_close.argtypes = [vp]
     L.cb_newton_begin.argtypes = [vp]
     L.cb_newton_step.argtypes = [vp, C.POINTER(Step)]
     L.cb_newmark_begin.argtypes = [vp]
@@ -252,6 +255,15 @@ class Model:
                     d=np.array(ds) if with_d else None)
 
     # ---- nonlinear Newmark (ALGFLAG 5) ----
+    def results_open(self, directory):
+        self._check(load().cb_results_open(self.h, str(directory).encode()))
+
+    def results_write(self, lam: float, iterations: int):
+        self._check(load().cb_results_write(self.h, lam, iterations))
+
+    def results_close(self):
+        self._check(load().cb_results_close(self.h))
+
     def newton_begin(self):
         self._check(load().cb_newton_begin(self.h))
 

@@ -221,6 +221,18 @@ int cb_mpnn_get_params(const cb_model *m, float *theta, float *grad);
 int cb_mpnn_eval(cb_model *m, const double *r, const double *p, const double *t, int train, double *z,
                  double *loss);
 
+/* results*.txt writers (output(), misc.c:345-451). cb_results_open creates
+ * dir/results2.txt (displacements), results3.txt (truss forces),
+ * results4.txt (frame forces) and results5.txt (shell forces) with the
+ * reference's layout lines; cb_results_write appends the current converged
+ * state as one record (lam: the load factor or time, iterations: itecnt),
+ * element forces averaged over the element's nodes as output() does;
+ * cb_results_close closes them (cb_model_destroy does too). results1.txt,
+ * the reference's input echo and message log, is not written. */
+int cb_results_open(cb_model *m, const char *dir);
+int cb_results_write(cb_model *m, double lam, int iterations);
+int cb_results_close(cb_model *m);
+
 int cb_get_timers(const cb_model *m, cb_timers *t);
 int cb_reset_timers(cb_model *m);
 /* Enable/disable per-phase CUDA-event timing (adds event records). */

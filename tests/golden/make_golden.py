@@ -122,6 +122,31 @@ def newton_runs():
         print(name, "neq", r["neq"], "incs", len(r["lam"]), "its", r["iterations"].tolist())
 
 
+def results_cases():
+    return {
+        "truss_msal": (models.space_truss(controls=truss_controls()), 3),
+        "panel8_msal": (models.cylindrical_panel(8, controls=panel_controls(8)), 4),
+        "frame_newmark": (frame_newmark_model("fixed", 6), 5),
+        "truss_nr": (newton_cases()["truss_nr"][0], 20),
+    }
+
+
+def results_fixtures():
+    """The reference's own results2..5.txt (output(), misc.c:345-451) for
+    short runs of each driver and element type."""
+    texts, files = [], []
+    names = list(results_cases())
+    for name in names:
+        m, steps = results_cases()[name]
+        r = refrun.run(m.text, steps, timeout=600)
+        assert r["returncode"] == 0, r["results1"][-400:]
+        texts.append(m.text)
+        files.append([r["results"].get(k, "") for k in range(2, 6)])
+        print("results", name, [len(f) for f in files[-1]])
+    np.savez_compressed(OUT / "results_files.npz", names=np.array(names), model_def=np.array(texts),
+                        files=np.array(files), steps=np.array([results_cases()[n][1] for n in names]))
+
+
 class RefElem:
     """The reference's element routines, called through the harness library."""
 
@@ -371,3 +396,4 @@ if __name__ == "__main__":
     truss_element_fixture()
     whole_runs()
     newton_runs()
+    results_fixtures()
