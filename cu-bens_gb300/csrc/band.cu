@@ -291,6 +291,7 @@ struct FactorArgs {
     int *flags;
     T *wbuf;     // 32 * bw: W of the current panel (FP64) / staged L rows, two buffers (FP32)
     T *dstage;   // 2 * 32 * 32: staged factored diagonal blocks (FP32)
+    T *look;     // 2 * (2 * 32 * 32 + 32): the next panel's factored diagonal block, Linv, 1/D (FP32)
     GridBarrier *bar;
     int dist;    // FP32: panel rows formed once per panel (wide bands) instead of per tile
 };
@@ -317,59 +318,48 @@ __device__ __forceinline__ void record_pivots(const FactorArgs<T> &a, long p, T 
     }
 }
 
-// LDL^T of a 32x32 block in shared memory and the inverse of its unit-lower
-// factor, by one warp in registers: lane i holds row i, l_jk and L_rk come by
-// shuffle, so the 32 dependent elimination steps cost no block-wide
-// synchronisation. On return A holds L below and D on the diagonal, Li the
-// inverse of the unit-lower L (row-major) and di = 1/D. A separate function
-// so that both loop nests unroll completely (the row stays in registers).
-template <typename T>
-__device__ __noinline__ void ldlt32_warp(T (*A)[NB + 1], T (*Li)[NB + 1], T *di)
+__device__ __noinline__ void ldlt32_noinv(float (*A)[NB + 1], float *di);
+
+// Inverse of the unit-lower L held below the diagonal of A (one warp, lane
+// j forms column j: x_rr = -sum_{k<rr} L_rr,k x_k, the terms in ascending
+// k), into Li (row-major).
+__device__ __noinline__ void linv32_warp(const float (*A)[NB + 1], float (*Li)[NB + 1])
 {
     const int lane = threadIdx.x % 32;
-    T r[NB];
-#pragma unroll
-    for (int j = 0; j < NB; ++j) r[j] = A[lane][j];
-#pragma unroll
-    for (int k = 0; k < NB; ++k) {
-        const T d = __shfl_sync(0xffffffffu, r[k], k);
-        const T rd = T(1) / d;
-        const T l = lane > k ? r[k] * rd : T(0);
-        if (lane > k) r[k] = l;
-        const T ldk = l * d;
-#pragma unroll
-        for (int j = k + 1; j < NB; ++j) {
-            const T ljk = __shfl_sync(0xffffffffu, l, j);
-            if (j <= lane) r[j] -= ldk * ljk;
-        }
-    }
-    T x[NB];
+    float x[NB];
 #pragma unroll
     for (int rr = 0; rr < NB; ++rr) {
-        T acc = 0;
+        float acc = 0;
 #pragma unroll
-        for (int k = 0; k < rr; ++k) acc += __shfl_sync(0xffffffffu, r[k], rr) * x[k];
-        x[rr] = rr == lane ? T(1) : (rr < lane ? T(0) : -acc);
+        for (int k = 0; k < rr; ++k) acc += A[rr][k] * x[k];
+        x[rr] = rr == lane ? 1.0f : (rr < lane ? 0.0f : -acc);
     }
-    T dl = 0;
 #pragma unroll
-    for (int j = 0; j < NB; ++j) {
-        A[lane][j] = j <= lane ? r[j] : T(0);
-        Li[j][lane] = x[j];
-        if (j == lane) dl = r[j];
-    }
-    di[lane] = T(1) / dl;
+    for (int j = 0; j < NB; ++j) Li[j][lane] = x[j];
+}
+
+// LDL^T and the inverse of L in two steps (no register spills in either)
+__device__ __forceinline__ void ldlt32_split(float (*A)[NB + 1], float (*Li)[NB + 1], float *di)
+{
+    ldlt32_noinv(A, di);
+    __syncwarp();
+    linv32_warp(A, Li);
 }
 
 // FP32: one grid barrier per 32-column panel p (m = min(bw, npad - p - 32)).
-//   1. every CTA factors the diagonal block and inverts its unit-lower factor
-//      in the registers of warp 0 (ldlt32_warp);
+//   1. the panel's factored diagonal block, the inverse of its unit-lower
+//      factor and 1/D: factored by every CTA for the first panel (warp 0:
+//      ldlt32_noinv, then linv32_warp), afterwards read from the look-ahead
+//      buffer that CTA 0 filled in step 3 of the previous panel;
 //   2. each CTA takes TS x TS tiles (ti, tj) of the trailing lower triangle,
 //      forms the panel rows it needs from the band, W = A Linv^T (= L D) for
 //      the tile's rows and L = W D^-1 for its columns, and applies
 //      A_rj -= sum_k W_rk L_jk. The owner of a diagonal tile stages its L
-//      rows, CTA 0 the factored diagonal block: other CTAs still read the
-//      panel's A values from the band during this phase;
+//      rows: other CTAs still read the panel's A values from the band during
+//      this phase;
+//   3. CTA 0, whose tile (0,0) is the next panel's diagonal block (final once
+//      CTA 0 has applied this panel to it), factors that block, records its
+//      pivots, stages it and publishes it with its inverse;
 //   -- grid barrier --
 //   0. (next panel) all CTAs copy the staged L rows and block into the band.
 template <int TS>
@@ -412,20 +402,32 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
         if (m > bw) m = bw;
         if (m < 0) m = 0;
         const int buf = (int)((p / NB) & 1);
-        // ---- 1. diagonal block: LDL^T and Linv by warp 0 in registers ----
-        for (int e = tid; e < NB * NB; e += 256) {
-            const int jj = e / NB, ii = e % NB;
-            A[ii][jj] = (ii >= jj && ii - jj <= bw) ? a.band[(p + jj) * ld + (ii - jj)] : T(0);
-        }
-        __syncthreads();
-        if (warp == 0) {
-            ldlt32_warp<T>(A, Li, di);
-            if (blockIdx.x == 0) record_pivots(a, p, A[lane][lane], di[lane], lane);
-        }
-        __syncthreads();
-        if (blockIdx.x == 0 && !a.dist) {
-            T *ds = a.dstage + buf * NB * NB;
-            for (int idx = tid; idx < NB * NB; idx += 256) ds[idx] = A[idx % NB][idx / NB];
+        // ---- 1. diagonal block: LDL^T and Linv by warp 0 in registers; on
+        //         the narrow path after the first panel CTA 0 has factored it
+        //         ahead (step 3) and every CTA reads its result ----
+        if (!a.dist && p > 0) {
+            const T *lk = a.look + buf * (2 * NB * NB + NB);
+            for (int e = tid; e < NB * NB; e += 256) {
+                A[e / NB][e % NB] = lk[e];
+                Li[e / NB][e % NB] = lk[NB * NB + e];
+            }
+            if (tid < NB) di[tid] = lk[2 * NB * NB + tid];
+            __syncthreads();
+        } else {
+            for (int e = tid; e < NB * NB; e += 256) {
+                const int jj = e / NB, ii = e % NB;
+                A[ii][jj] = (ii >= jj && ii - jj <= bw) ? a.band[(p + jj) * ld + (ii - jj)] : T(0);
+            }
+            __syncthreads();
+            if (warp == 0) {
+                ldlt32_split(A, Li, di);
+                if (blockIdx.x == 0) record_pivots(a, p, A[lane][lane], di[lane], lane);
+            }
+            __syncthreads();
+            if (blockIdx.x == 0 && !a.dist) {
+                T *ds = a.dstage + buf * NB * NB;
+                for (int idx = tid; idx < NB * NB; idx += 256) ds[idx] = A[idx % NB][idx / NB];
+            }
         }
         if (a.dist) {
             // ---- 2'. wide band: panel rows once, one warp per row; W to wbuf,
@@ -548,14 +550,41 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
             }
             __syncthreads();
         }
+        // ---- 3. look-ahead (CTA 0, whose first tile (0,0) is the next panel's
+        //         diagonal block, final now): factor it before the barrier,
+        //         record its pivots, stage it, publish A, Linv, 1/D ----
+        if (blockIdx.x == 0 && m > 0) {
+            const long pn = p + NB;
+            const int bn = (int)((pn / NB) & 1);
+            __syncthreads();
+            for (int e = tid; e < NB * NB; e += 256) {
+                const int jj = e / NB, ii = e % NB;
+                A[ii][jj] = (ii >= jj && ii - jj <= bw) ? a.band[(pn + jj) * ld + (ii - jj)] : T(0);
+            }
+            __syncthreads();
+            if (warp == 0) {
+                ldlt32_split(A, Li, di);
+                record_pivots(a, pn, A[lane][lane], di[lane], lane);
+            }
+            __syncthreads();
+            T *ds = a.dstage + bn * NB * NB;
+            T *lk = a.look + bn * (2 * NB * NB + NB);
+            for (int idx = tid; idx < NB * NB; idx += 256) {
+                ds[idx] = A[idx % NB][idx / NB];
+                lk[idx] = A[idx / NB][idx % NB];
+                lk[NB * NB + idx] = Li[idx / NB][idx % NB];
+            }
+            if (tid < NB) lk[2 * NB * NB + tid] = di[tid];
+        }
         mprev = m;
         if (!grid_barrier(a.bar, gridDim.x)) return;
     }
 }
 
-// LDL^T of a 32x32 block in shared memory by one warp in registers, without
-// the inverse of L (the panel rows are then formed by substitution). On
-// return A holds L below and D on the diagonal, di = 1/D.
+// LDL^T of a 32x32 block in shared memory by one warp in registers (lane i
+// holds row i, l_jk by shuffle), without the inverse of L: the grid factor
+// forms it next with linv32_warp, the cluster factor substitutes instead.
+// On return A holds L below and D on the diagonal, di = 1/D.
 __device__ __noinline__ void ldlt32_noinv(float (*A)[NB + 1], float *di)
 {
     const int lane = threadIdx.x % 32;
@@ -565,7 +594,7 @@ __device__ __noinline__ void ldlt32_noinv(float (*A)[NB + 1], float *di)
 #pragma unroll
     for (int k = 0; k < NB; ++k) {
         const float d = __shfl_sync(0xffffffffu, r[k], k);
-        const float rd = 1.0f / d;
+        const float rd = __frcp_rn(d);  // the correctly rounded 1/d
         const float l = lane > k ? r[k] * rd : 0.0f;
         if (lane > k) r[k] = l;
         const float ldk = l * d;
@@ -581,7 +610,7 @@ __device__ __noinline__ void ldlt32_noinv(float (*A)[NB + 1], float *di)
         A[lane][j] = j <= lane ? r[j] : 0.0f;
         if (j == lane) dl = r[j];
     }
-    di[lane] = 1.0f / dl;
+    di[lane] = __frcp_rn(dl);
 }
 
 // FP32 narrow bands: one thread-block cluster of C CTAs holds the active
@@ -1088,8 +1117,8 @@ void factor_band(BandFactor &f, cudaStream_t st, long *launches)
     // FP32: form each panel's rows once (two barriers per panel) when the
     // trailing triangle has many more tiles than CTAs; otherwise per tile
     const int dist = (f.fp32 && ntiles > 2L * grid) ? 1 : 0;
-    FactorArgs<T> a{band, f.ld, f.bw, npad, f.n, (T *)f.dinv, f.ssd, f.flags, (T *)f.work, (T *)f.stage, f.fbar,
-                    dist};
+    FactorArgs<T> a{band, f.ld, f.bw, npad, f.n, (T *)f.dinv, f.ssd, f.flags, (T *)f.work, (T *)f.stage,
+                    (T *)f.look, f.fbar, dist};
     if constexpr (sizeof(T) == 4) {
         if (f.cluster > 0) {
             ClusterArgs ca{a, f.cluster_slots, f.cluster_nwin};
@@ -1398,6 +1427,7 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use
     CB_CUDA(cudaMalloc(&f.flags, 2 * sizeof(int)));
     CB_CUDA(cudaMalloc(&f.bar, sizeof(GridBarrier)));
     CB_CUDA(cudaMalloc(&f.stage, es * 2 * NB * NB));
+    CB_CUDA(cudaMalloc(&f.look, es * 2 * (2 * NB * NB + NB)));
     CB_CUDA(cudaMemset(f.bar, 0, sizeof(GridBarrier)));
     CB_CUDA(cudaMalloc(&f.fbar, sizeof(GridBarrier)));
     CB_CUDA(cudaMemset(f.fbar, 0, sizeof(GridBarrier)));
@@ -1420,7 +1450,7 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use
 void band_free(BandFactor &f)
 {
     if (f.factor_graph) cudaGraphExecDestroy(f.factor_graph);
-    for (void *p : {f.band, f.dinv, f.linv, f.linvt, f.pmat, f.rmat, f.work, f.stage, (void *)f.ssd,
+    for (void *p : {f.band, f.dinv, f.linv, f.linvt, f.pmat, f.rmat, f.work, f.stage, f.look, (void *)f.ssd,
                     (void *)f.flags, (void *)f.bar, (void *)f.fbar})
         if (p) cudaFree(p);
     f = BandFactor{};
