@@ -400,7 +400,11 @@ def run_frame(args, world, rank, local, pg):
                    "spmv_ms": ms_spmv, "frame_force_ms": ms_ff},
         "roofline": {"kernel": "kry_spmv_kernel (CSR y = A x, FP64 values, 8 lanes per row)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "peak_kind": peak_kind, "traffic": None, "bytes_per_launch": bytes_spmv,
+                     "peak_kind": peak_kind,
+                     # dram__bytes_read.sum + dram__bytes_write.sum of one launch (ncu capture of the
+                     # same command with --steps 4, profiles/fgmres_frame_building.md)
+                     "traffic": 39.5e6 + 2.56e3, "traffic_source": "profiles/fgmres_frame_building.md",
+                     "bytes_per_launch": bytes_spmv,
                      "ms_per_launch": ms_spmv,
                      "note": "bytes = 12 per stored entry + row pointers + x once + y; timed alone, back to back "
                              "(the matrix is L2-resident between launches)"},
@@ -655,7 +659,11 @@ def run_ours(args, world, rank, local, pg):
                                    "factor_f32_kernel (persistent band LDL^T, FP32, one grid barrier per 32-column "
                                    "panel)",
                          "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                         # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the grid factor
+                         # (ncu capture, profiles/factor_f32_kernel_panel64.md); the cluster factor has none
+                         "traffic": None if info.get("factor_cluster") else 39.7e6 + 3.7e6,
+                         "traffic_source": "profiles/factor_f32_kernel_panel64.md",
                          "bytes_per_launch": bytes_ldlt, "ms_per_launch": ms_ldlt,
                          "note": "latency-bound: 780 dependent panels; bytes = the band read and written "
                                  "once; FP32 FMA work n*bw^2/2 per launch"},

@@ -150,6 +150,181 @@ __global__ void __launch_bounds__(256) inv_row_kernel(const T *band, long ld, lo
     }
 }
 
+// Column sweep of Linv: CTA (i, J) forms tile column J of block i's inverse,
+//     X_JJ = T_JJ,   X_IJ = -T_II sum_K L_IK X_KJ   for I = J+1 .. nt-1,
+// K in [max(J, I-kb), I), with T_II the inverse diagonal tiles written by
+// inv_diag_kernel. The last kb tiles of the column stay in shared memory
+// (a ring indexed by K mod kb), so the only global reads on the dependent
+// chain are the L tiles and T_II, which do not depend on X and stream in by
+// cp.async two chunks ahead of the multiply. Each finished tile goes to linv
+// and, transposed through the ring, to linvt. One launch replaces the
+// nt - 1 launches of inv_row_kernel plus the transpose.
+constexpr int kInvChunk = 4;  // L tiles per cp.async group
+
+__device__ __forceinline__ void cp_async_elem(float *dst, const float *src, bool valid)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_elem(double *dst, const double *src, bool valid)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__device__ __forceinline__ void lds4(const float *p, float (&v)[4])
+{
+    const float4 u = *reinterpret_cast<const float4 *>(p);
+    v[0] = u.x, v[1] = u.y, v[2] = u.z, v[3] = u.w;
+}
+
+__device__ __forceinline__ void lds4(const double *p, double (&v)[4])
+{
+    const double2 u = *reinterpret_cast<const double2 *>(p);
+    const double2 t = *reinterpret_cast<const double2 *>(p + 2);
+    v[0] = u.x, v[1] = u.y, v[2] = t.x, v[3] = t.y;
+}
+
+// Dynamic shared memory of inv_col_kernel: ring (kb tiles, padded rows),
+// two chunks of L tiles (k-major), two T_II tiles, one staging tile.
+template <typename T>
+size_t inv_col_smem(long kb)
+{
+    return sizeof(T) * ((size_t)kb * NB * (NB + 1) + 2 * (size_t)kInvChunk * NB * NB + 2 * NB * NB + NB * (NB + 1));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) inv_col_kernel(const T *band, long ld, long bw, long s, long kb, T *linv,
+                                                      T *linvt)
+{
+    extern __shared__ __align__(16) unsigned char inv_smem[];
+    constexpr int P = NB + 1;
+    T *ring = reinterpret_cast<T *>(inv_smem);  // ring[slot][r][c], row stride P
+    T *Ls = ring + kb * NB * P;                 // Ls[buf][t][k][r]: L_IK(r, k)
+    T *Ts = Ls + 2 * kInvChunk * NB * NB;       // Ts[I & 1][r][k]: T_II(r, k)
+    T *Y = Ts + 2 * NB * NB;                    // Y[r][c], row stride P
+    const long i = blockIdx.x, J = blockIdx.y;
+    const long nt = s / NB, g0 = i * s;
+    T *Li = linv + i * s * s;
+    T *Lt = linvt + i * s * s;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+
+    // X_JJ = T_JJ into the ring; its transpose into linvt
+    {
+        T *X0 = ring + (J % kb) * NB * P;
+        for (int q = 0; q < 4; ++q) {
+            const int r = w + 8 * q;
+            X0[r * P + lane] = Li[(J * NB + r) * s + J * NB + lane];
+        }
+        __syncthreads();
+        for (int q = 0; q < 4; ++q) {
+            const int c = w + 8 * q;
+            Lt[(J * NB + c) * s + J * NB + lane] = X0[lane * P + c];
+        }
+    }
+    if (J == nt - 1) return;
+
+    auto kfirst = [&](long I) { return I - kb > J ? I - kb : J; };
+    // chunk c of step I: L_IK for K = kfirst(I) + c*kInvChunk + t (K < I);
+    // the first chunk of a step also brings T_II
+    auto issue = [&](long I, long c, int buf) {
+        const long K0 = kfirst(I) + c * kInvChunk;
+        const long R = g0 + I * NB + lane;
+        for (int t = 0; t < kInvChunk; ++t) {
+            const long K = K0 + t;
+            if (K >= I) break;
+            T *dst = Ls + ((long)buf * kInvChunk + t) * NB * NB;
+            for (int q = 0; q < 4; ++q) {
+                const int k = w + 8 * q;
+                const long C = g0 + K * NB + k;
+                const long off = R - C;  // >= 1 because K < I
+                const bool ok = off <= bw;
+                cp_async_elem(dst + k * NB + lane, ok ? band + C * ld + off : band, ok);
+            }
+        }
+        if (c == 0) {
+            T *dst = Ts + (I & 1) * NB * NB;
+            for (int q = 0; q < 4; ++q) {
+                const int r = w + 8 * q;
+                cp_async_elem(dst + r * NB + lane, Li + (I * NB + r) * s + I * NB + lane, true);
+            }
+        }
+    };
+
+    long I = J + 1, c = 0;
+    int buf = 0;
+    issue(I, c, buf);
+    cp_async_commit();
+    T acc[4] = {0, 0, 0, 0};  // rows 4w .. 4w+3, column lane
+    for (;;) {
+        long In = I, cn = c + 1;
+        if (kfirst(I) + cn * kInvChunk >= I) {
+            In = I + 1;
+            cn = 0;
+        }
+        const bool more = In < nt;
+        if (more) issue(In, cn, buf ^ 1);
+        cp_async_commit();
+        cp_async_wait1();
+        __syncthreads();
+        const long K0 = kfirst(I) + c * kInvChunk;
+        for (int t = 0; t < kInvChunk; ++t) {
+            const long K = K0 + t;
+            if (K >= I) break;
+            const T *X = ring + (K % kb) * NB * P + lane;
+            const T *A = Ls + ((long)buf * kInvChunk + t) * NB * NB + 4 * w;
+#pragma unroll 8
+            for (int k = 0; k < NB; ++k) {
+                T a[4];
+                lds4(A + k * NB, a);
+                const T x = X[k * P];
+                acc[0] += a[0] * x;
+                acc[1] += a[1] * x;
+                acc[2] += a[2] * x;
+                acc[3] += a[3] * x;
+            }
+        }
+        if (In != I) {
+            // step I done: X_IJ = -T_II * acc
+            for (int q = 0; q < 4; ++q) {
+                Y[(4 * w + q) * P + lane] = acc[q];
+                acc[q] = 0;
+            }
+            __syncthreads();
+            const T *Tb = Ts + (I & 1) * NB * NB + 4 * w * NB;
+            T v[4] = {0, 0, 0, 0};
+            for (int k = 0; k < 4 * w + 4; ++k) {  // T_II(r, k) = 0 for k > r
+                const T y = Y[k * P + lane];
+                for (int q = 0; q < 4; ++q) v[q] += Tb[q * NB + k] * y;
+            }
+            T *Xn = ring + (I % kb) * NB * P;
+            for (int q = 0; q < 4; ++q) Xn[(4 * w + q) * P + lane] = -v[q];
+            __syncthreads();
+            for (int q = 0; q < 4; ++q) {
+                const int r = w + 8 * q;
+                Li[(I * NB + r) * s + J * NB + lane] = Xn[r * P + lane];
+            }
+            for (int q = 0; q < 4; ++q) {
+                const int cc = w + 8 * q;
+                Lt[(J * NB + cc) * s + I * NB + lane] = Xn[lane * P + cc];
+            }
+        }
+        __syncthreads();
+        if (!more) break;
+        I = In;
+        c = cn;
+        buf ^= 1;
+    }
+    cp_async_wait0();
+}
+
 // linvt_i = Linv_i^T (row-major), 32x32 tiles through shared memory.
 template <typename T>
 __global__ void __launch_bounds__(256) transpose_kernel(const T *linv, long s, T *linvt)
@@ -1044,8 +1219,51 @@ __device__ __forceinline__ T warp_row_dot(const T *__restrict__ row, const T *__
     return warp_reduce(s);
 }
 
+// The chain rows of the block-bidiagonal solve: a warp holds its row of the
+// next step in registers (the first 32 * row_regs<T>() entries), loaded before
+// the barrier that ends the current step, so a step waits on the vector only.
 template <typename T>
-__global__ void __launch_bounds__(256) solve_kernel(SolveArgs<T> a)
+constexpr int row_regs()
+{
+    return sizeof(T) == 4 ? 16 : 8;
+}
+
+template <typename T>
+__device__ __forceinline__ void row_to_regs(T (&pre)[row_regs<T>()], const T *__restrict__ row, long len, int lane)
+{
+#pragma unroll
+    for (int u = 0; u < row_regs<T>(); ++u) {
+        const long j = lane + 32L * u;
+        pre[u] = j < len ? row[j] : T(0);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T regs_row_dot(const T (&pre)[row_regs<T>()], const T *__restrict__ row,
+                                          const T *__restrict__ vec, long len, int lane)
+{
+    T acc[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int u = 0; u < row_regs<T>(); ++u) {
+        const long j = lane + 32L * u;
+        if (j < len) acc[u & 3] += pre[u] * vec[j];
+    }
+    for (long j = lane + 32L * row_regs<T>(); j < len; j += 32) acc[0] += row[j] * vec[j];
+    return warp_reduce((acc[0] + acc[1]) + (acc[2] + acc[3]));
+}
+
+// Block-bidiagonal solve in one cooperative launch:
+//   A  y_i = Linv_i b_i                                 (all rows)
+//   B  y_i[s-w:s] -= Pn_i[s-w:s] y_{i-1}[s-w:s]         (chain, i = 1 .. nb-1)
+//      y_i[0:s-w] -= Pn_i[0:s-w] y_{i-1}[s-w:s], z = y / D
+//   C  v_i = Linv_i^T z_i                               (all rows)
+//   D  v_i[0:w]   -= Rn_i[0:w] v_{i+1}[0:w]             (chain, i = nb-2 .. 0)
+//      v_i[w:s]   -= Rn_i[w:s] v_{i+1}[0:w], x = v
+// Only the w chain rows of each step depend on the previous step; they run
+// on the first ceil(w/8) CTAs with a barrier of their own (bar[1]), and the
+// remaining rows of every block follow in one grid-wide pass.
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) solve_kernel(SolveArgs<T> a)
 {
     const long s = a.s, w = a.w, nb = a.nblk, npad = nb * s;
     const int lane = threadIdx.x % 32;
@@ -1053,7 +1271,17 @@ __global__ void __launch_bounds__(256) solve_kernel(SolveArgs<T> a)
     const long nwarps = gridDim.x * 8L;
     const long gthr = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const long nthr = gridDim.x * (long)blockDim.x;
-    // A: y = blockdiag(Linv) b (b converted to T into w first)
+    const unsigned nchain = (unsigned)min((w + 7) / 8, (long)gridDim.x);
+    const bool in_chain = blockIdx.x < nchain;
+    const long cw = 8L * nchain;          // chain warps
+    const bool regs = cw >= w;            // one chain row per warp
+    GridBarrier *cbar = a.bar + 1;
+    auto chain_failed = [&]() {
+        if (threadIdx.x == 0) atomicExch(&a.bar->err, 1);  // releases the CTAs waiting on bar[0]
+    };
+    T pre[row_regs<T>()];
+
+    // A: y = blockdiag(Linv) b (b converted to T into z first)
     for (long g = gthr; g < npad; g += nthr) a.z[g] = g < a.n ? (T)a.rhs[g] : T(0);
     if (!grid_barrier(a.bar, gridDim.x)) return;
     for (long row = gwarp; row < npad; row += nwarps) {
@@ -1061,35 +1289,79 @@ __global__ void __launch_bounds__(256) solve_kernel(SolveArgs<T> a)
         T acc = warp_row_dot(a.linv + i * s * s + r * s, a.z + i * s, r + 1, lane);
         if (lane == 0) a.y[row] = acc;
     }
+    if (in_chain && regs && gwarp < w && nb > 1) row_to_regs(pre, a.pn + s * w + (s - w + gwarp) * w, w, lane);
     if (!grid_barrier(a.bar, gridDim.x)) return;
-    // B: y_i -= Pn_i y_{i-1}[s-w:s]
-    for (long i = 1; i < nb; ++i) {
-        const T *yp = a.y + i * s - w;
-        for (long r = gwarp; r < s; r += nwarps) {
-            T acc = warp_row_dot(a.pn + i * s * w + r * w, yp, w, lane);
-            if (lane == 0) a.y[i * s + r] -= acc;
+    // B, chain rows
+    if (in_chain) {
+        for (long i = 1; i < nb; ++i) {
+            const T *yp = a.y + i * s - w;
+            if (regs) {
+                if (gwarp < w) {
+                    const T *row = a.pn + i * s * w + (s - w + gwarp) * w;
+                    const T acc = regs_row_dot(pre, row, yp, w, lane);
+                    if (lane == 0) a.y[i * s + s - w + gwarp] -= acc;
+                    if (i + 1 < nb) row_to_regs(pre, row + s * w, w, lane);
+                }
+            } else {
+                for (long r = gwarp; r < w; r += cw) {
+                    const T acc = warp_row_dot(a.pn + i * s * w + (s - w + r) * w, yp, w, lane);
+                    if (lane == 0) a.y[i * s + s - w + r] -= acc;
+                }
+            }
+            if (!grid_barrier(cbar, nchain)) {
+                chain_failed();
+                return;
+            }
         }
-        if (!grid_barrier(a.bar, gridDim.x)) return;
     }
-    // C: v = blockdiag(Linv^T) (y / D), warp per row of the stored transpose
-    for (long g = gthr; g < npad; g += nthr) a.z[g] = a.y[g] * a.dinv[g];
     if (!grid_barrier(a.bar, gridDim.x)) return;
+    // B, the other rows, and z = y / D
+    for (long row = gwarp; row < npad; row += nwarps) {
+        const long i = row / s, r = row % s;
+        T acc = 0;
+        if (i >= 1 && r < s - w) acc = warp_row_dot(a.pn + i * s * w + r * w, a.y + i * s - w, w, lane);
+        if (lane == 0) a.z[row] = (a.y[row] - acc) * a.dinv[row];
+    }
+    if (!grid_barrier(a.bar, gridDim.x)) return;
+    // C: v = blockdiag(Linv^T) z, warp per row of the stored transpose
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, c = row % s;
         T acc = warp_row_dot(a.linvt + i * s * s + c * s + c, a.z + i * s + c, s - c, lane);
         if (lane == 0) a.v[row] = acc;
     }
+    if (in_chain && regs && gwarp < w && nb > 1) row_to_regs(pre, a.rn + (nb - 2) * s * w + gwarp * w, w, lane);
     if (!grid_barrier(a.bar, gridDim.x)) return;
-    // D: x_i -= Rn_i x_{i+1}[0:w]
-    for (long i = nb - 2; i >= 0; --i) {
-        const T *xn = a.v + (i + 1) * s;
-        for (long c = gwarp; c < s; c += nwarps) {
-            T acc = warp_row_dot(a.rn + i * s * w + c * w, xn, w, lane);
-            if (lane == 0) a.v[i * s + c] -= acc;
+    // D, chain rows
+    if (in_chain) {
+        for (long i = nb - 2; i >= 0; --i) {
+            const T *xn = a.v + (i + 1) * s;
+            if (regs) {
+                if (gwarp < w) {
+                    const T *row = a.rn + i * s * w + gwarp * w;
+                    const T acc = regs_row_dot(pre, row, xn, w, lane);
+                    if (lane == 0) a.v[i * s + gwarp] -= acc;
+                    if (i > 0) row_to_regs(pre, row - s * w, w, lane);
+                }
+            } else {
+                for (long c = gwarp; c < w; c += cw) {
+                    const T acc = warp_row_dot(a.rn + i * s * w + c * w, xn, w, lane);
+                    if (lane == 0) a.v[i * s + c] -= acc;
+                }
+            }
+            if (!grid_barrier(cbar, nchain)) {
+                chain_failed();
+                return;
+            }
         }
-        if (!grid_barrier(a.bar, gridDim.x)) return;
     }
-    for (long g = gthr; g < a.n; g += nthr) a.out[g] = (double)a.v[g];
+    if (!grid_barrier(a.bar, gridDim.x)) return;
+    // D, the other rows, and x = v
+    for (long row = gwarp; row < a.n; row += nwarps) {
+        const long i = row / s, c = row % s;
+        T acc = 0;
+        if (i <= nb - 2 && c >= w) acc = warp_row_dot(a.rn + i * s * w + c * w, a.v + (i + 1) * s, w, lane);
+        if (lane == 0) a.out[row] = (double)(a.v[row] - acc);
+    }
 }
 
 // -------------------------------------------------------------------------
@@ -1145,6 +1417,25 @@ void factor_band(BandFactor &f, cudaStream_t st, long *launches)
     ++*launches;
 }
 
+// The most dynamic shared memory inv_col_kernel<T> may take on this device
+// (the attribute is set once, to the opt-in limit, for every handle).
+template <typename T>
+size_t inv_col_smem_max()
+{
+    static const size_t cap = [] {
+        int dev = 0, optin = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+            cudaFuncSetAttribute(inv_col_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            return (size_t)0;
+        }
+        return (size_t)optin;
+    }();
+    return cap;
+}
+
 // Solve blocks from the factored band: Linv_i, its transpose, Pn_i, Rn_i.
 template <typename T>
 void form_solve_blocks(BandFactor &f, cudaStream_t st, long *launches)
@@ -1153,13 +1444,21 @@ void form_solve_blocks(BandFactor &f, cudaStream_t st, long *launches)
     const long nt = f.s / NB;
     const long kb = (f.bw + NB - 1) / NB + 1;
     inv_diag_kernel<T><<<dim3((unsigned)nt, (unsigned)f.nblk), 32, 0, st>>>(band, f.ld, f.bw, f.s, (T *)f.linv);
-    for (long I = 1; I < nt; ++I)
-        inv_row_kernel<T><<<dim3((unsigned)I, (unsigned)f.nblk), 256, 0, st>>>(band, f.ld, f.bw, f.s, I, kb,
-                                                                               (T *)f.linv);
-    *launches += nt;
-    transpose_kernel<T><<<dim3((unsigned)nt, (unsigned)nt, (unsigned)f.nblk), 256, 0, st>>>((const T *)f.linv, f.s,
-                                                                                        (T *)f.linvt);
-    *launches += 1;
+    const size_t smem = inv_col_smem<T>(kb);
+    if (smem <= inv_col_smem_max<T>()) {
+        // CTAs ordered by column: the longest sweeps (J = 0) start first
+        inv_col_kernel<T><<<dim3((unsigned)f.nblk, (unsigned)nt), 256, smem, st>>>(band, f.ld, f.bw, f.s, kb,
+                                                                                  (T *)f.linv, (T *)f.linvt);
+        *launches += 2;
+    } else {
+        // bands too wide for the column ring: one launch per tile row, then the transpose
+        for (long I = 1; I < nt; ++I)
+            inv_row_kernel<T><<<dim3((unsigned)I, (unsigned)f.nblk), 256, 0, st>>>(band, f.ld, f.bw, f.s, I, kb,
+                                                                                   (T *)f.linv);
+        transpose_kernel<T><<<dim3((unsigned)nt, (unsigned)nt, (unsigned)f.nblk), 256, 0, st>>>((const T *)f.linv,
+                                                                                            f.s, (T *)f.linvt);
+        *launches += nt + 1;
+    }
     if (f.nblk > 1) {
         dim3 g((unsigned)(f.w / NB), (unsigned)(f.s / NB), (unsigned)(f.nblk - 1));
         pn_kernel<T><<<g, 256, 0, st>>>(band, f.ld, f.bw, f.s, f.w, (const T *)f.linv, (T *)f.pmat);
@@ -1205,7 +1504,7 @@ void solve_launch(const BandFactor &f, const double *rhs, double *x, void *work,
     a.v = a.y + npad;
     a.z = a.v + npad;
     a.bar = bar;
-    CB_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), st));
+    CB_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(GridBarrier), st));  // grid and chain barriers
     void *args[] = {&a};
     CB_CUDA(cudaLaunchCooperativeKernel((const void *)solve_kernel<T>, dim3((unsigned)f.solve_grid), dim3(256),
                                         args, 0, st));
@@ -1425,10 +1724,10 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use
     CB_CUDA(cudaMalloc(&f.work, es * work));
     CB_CUDA(cudaMalloc(&f.ssd, sizeof(double) * (size_t)n));
     CB_CUDA(cudaMalloc(&f.flags, 2 * sizeof(int)));
-    CB_CUDA(cudaMalloc(&f.bar, sizeof(GridBarrier)));
+    CB_CUDA(cudaMalloc(&f.bar, 2 * sizeof(GridBarrier)));  // the solve's grid and chain barriers
     CB_CUDA(cudaMalloc(&f.stage, es * 2 * NB * NB));
     CB_CUDA(cudaMalloc(&f.look, es * 2 * (2 * NB * NB + NB)));
-    CB_CUDA(cudaMemset(f.bar, 0, sizeof(GridBarrier)));
+    CB_CUDA(cudaMemset(f.bar, 0, 2 * sizeof(GridBarrier)));
     CB_CUDA(cudaMalloc(&f.fbar, sizeof(GridBarrier)));
     CB_CUDA(cudaMemset(f.fbar, 0, sizeof(GridBarrier)));
     // The direct solve's grid is sized to the work of one panel step (at most
