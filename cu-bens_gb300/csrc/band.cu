@@ -410,30 +410,32 @@ __global__ void __launch_bounds__(256) rn_kernel(const T *band, long ld, long bw
 // Persistent solve
 // -------------------------------------------------------------------------
 
-// Grid barrier for a cooperative launch. The wait is bounded: after 2^24
-// polls (well over a second) the CTA records a timeout in bar->err; once the
-// flag is set no CTA waits any more. Returns false when the flag is set, and
-// the caller then leaves the kernel, so a fault cannot hang the GPU; the host
-// turns the flag into CB_ERR_TIMEOUT.
-__device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks)
+// Grid barrier for a cooperative launch. bar->count is zeroed before the
+// launch and only grows: the k-th barrier of a kernel (epoch, counted by
+// every thread) is passed once count reaches k * nblocks, so a CTA arrives
+// with one atomic and nothing is reset on the critical path. The wait is
+// bounded: after 2^24 polls (well over a second) the CTA records a timeout in
+// bar->err; once the flag is set no CTA waits any more. Returns false when
+// the flag is set, and the caller then leaves the kernel, so a fault cannot
+// hang the GPU; the host turns the flag into CB_ERR_TIMEOUT. leader is the
+// thread that arrives for the CTA.
+__device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks, unsigned &epoch,
+                                             unsigned leader = 0)
 {
     __shared__ int failed;
     __syncthreads();
-    if (threadIdx.x == 0) {
+    ++epoch;
+    if (threadIdx.x == leader) {
         volatile int *verr = &bar->err;
         failed = *verr;
         if (!failed) {
-            volatile unsigned *vgen = &bar->gen;
-            unsigned gen = *vgen;
+            const unsigned target = epoch * nblocks;
             __threadfence();
-            unsigned arrived = atomicAdd(&bar->count, 1u) + 1u;
-            if (arrived == nblocks) {
-                bar->count = 0;
-                __threadfence();
-                atomicAdd(&bar->gen, 1u);
-            } else {
+            const unsigned arrived = atomicAdd(&bar->count, 1u) + 1u;
+            if (arrived < target) {
+                volatile unsigned *vcount = &bar->count;
                 unsigned long long polls = 0;
-                while (*vgen == gen) {
+                while (*vcount < target) {
                     if (*verr) {
                         failed = 1;
                         break;
@@ -540,6 +542,7 @@ __device__ __forceinline__ void ldlt32_split(float (*A)[NB + 1], float (*Li)[NB 
 template <int TS>
 __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
 {
+    unsigned ep = 0;  // grid barriers passed
     using T = float;
     __shared__ T A[NB][NB + 1];   // factored diagonal block: L below, D on the diagonal
     __shared__ T Li[NB][NB + 1];  // Linv of the unit-lower L_pp
@@ -619,7 +622,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                 a.wbuf[lane * m + r] = w;
                 if (off <= bw) a.band[(p + lane) * ld + off] = w * di[lane];
             }
-            if (!grid_barrier(a.bar, gridDim.x)) return;
+            if (!grid_barrier(a.bar, gridDim.x, ep)) return;
             if (blockIdx.x == 0)
                 for (int idx = tid; idx < NB * NB; idx += 256) {
                     const int j = idx / NB, i = idx % NB;
@@ -672,7 +675,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                 }
                 __syncthreads();
             }
-            if (!grid_barrier(a.bar, gridDim.x)) return;
+            if (!grid_barrier(a.bar, gridDim.x, ep)) return;
             continue;
         }
         // ---- 2. trailing tiles ----
@@ -752,7 +755,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
             if (tid < NB) lk[2 * NB * NB + tid] = di[tid];
         }
         mprev = m;
-        if (!grid_barrier(a.bar, gridDim.x)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     }
 }
 
@@ -1019,6 +1022,7 @@ __global__ void __launch_bounds__(kClusterThreads) factor_cluster_kernel(Cluster
 template <int TS>
 __global__ void __launch_bounds__(256) factor_f64_kernel(FactorArgs<double> a)
 {
+    unsigned ep = 0;  // grid barriers passed
     using T = double;
     __shared__ T A[NB][NB + 1];
     __shared__ T di[NB];
@@ -1060,7 +1064,7 @@ __global__ void __launch_bounds__(256) factor_f64_kernel(FactorArgs<double> a)
             a.wbuf[lane * m + r] = w;
             if (off <= bw) a.band[(p + lane) * ld + off] = w * di[lane];
         }
-        if (!grid_barrier(a.bar, gridDim.x)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
         // ---- 3. diagonal block out, trailing update ----
         if (blockIdx.x == 0) {
             for (int e = tid; e < NB * NB; e += 256) {
@@ -1093,7 +1097,7 @@ __global__ void __launch_bounds__(256) factor_f64_kernel(FactorArgs<double> a)
             }
             __syncthreads();
         }
-        if (!grid_barrier(a.bar, gridDim.x)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     }
 }
 
@@ -1116,12 +1120,13 @@ struct DirectArgs {
 template <typename T>
 __global__ void __launch_bounds__(256) solve_direct_kernel(DirectArgs<T> a)
 {
+    unsigned ep = 0;  // grid barriers passed
     __shared__ T yp[NB];
     const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
     const long ld = a.ld, bw = a.bw, npad = a.npad;
     const long gthr = blockIdx.x * 256L + tid, nthr = gridDim.x * 256L;
     for (long g = gthr; g < npad; g += nthr) a.y[g] = g < a.n ? (T)a.rhs[g] : T(0);
-    if (!grid_barrier(a.bar, gridDim.x)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     // forward: y_p = L_pp^-1 y_p; y_r -= L(r, p..p+31) y_p for the rows below
     for (long p = 0; p < npad; p += NB) {
         long m = npad - p - NB;
@@ -1150,10 +1155,10 @@ __global__ void __launch_bounds__(256) solve_direct_kernel(DirectArgs<T> a)
             }
             a.y[p + NB + r] -= acc;
         }
-        if (!grid_barrier(a.bar, gridDim.x)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     }
     for (long g = gthr; g < npad; g += nthr) a.y[g] *= a.dinv[g];
-    if (!grid_barrier(a.bar, gridDim.x)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     // backward: x_p = L_pp^-T z_p; z_j -= sum_i L(p+i, j) x_i for j in [p-bw, p)
     for (long p = npad - NB; p >= 0; p -= NB) {
         if (warp == 0) {
@@ -1180,7 +1185,7 @@ __global__ void __launch_bounds__(256) solve_direct_kernel(DirectArgs<T> a)
                 if (base + i <= bw) acc += a.band[j * ld + base + i] * yp[i];
             a.y[j] -= acc;
         }
-        if (!grid_barrier(a.bar, gridDim.x)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     }
     for (long g = gthr; g < a.n; g += nthr) a.out[g] = (double)a.y[g];
 }
@@ -1259,62 +1264,76 @@ __device__ __forceinline__ T regs_row_dot(const T (&pre)[row_regs<T>()], const T
 //   C  v_i = Linv_i^T z_i                               (all rows)
 //   D  v_i[0:w]   -= Rn_i[0:w] v_{i+1}[0:w]             (chain, i = nb-2 .. 0)
 //      v_i[w:s]   -= Rn_i[w:s] v_{i+1}[0:w], x = v
-// Only the w chain rows of each step depend on the previous step; they run
-// on the first ceil(w/8) CTAs with a barrier of their own (bar[1]), and the
-// remaining rows of every block follow in one grid-wide pass.
+// Only the w chain rows of each step depend on the previous step. They run
+// on the first ceil(w/7) CTAs, warps 0-6 one row each, with a barrier of
+// their own (bar[1]) led by warp 7, which has no loads in flight for its
+// fence to wait on; a warp's next row and all its steps' own values are in
+// registers before the step starts. The remaining rows of every block
+// follow in one grid-wide pass.
 template <typename T>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) solve_kernel(SolveArgs<T> a)
 {
+    unsigned ep = 0, ep_chain = 0;  // grid and chain barriers passed
+    constexpr int kChainWarps = 7;
+    constexpr unsigned kLeader = 32 * kChainWarps;  // lane 0 of warp 7
     const long s = a.s, w = a.w, nb = a.nblk, npad = nb * s;
-    const int lane = threadIdx.x % 32;
-    const long gwarp = blockIdx.x * 8L + threadIdx.x / 32;
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+    const long gwarp = blockIdx.x * 8L + warp;
     const long nwarps = gridDim.x * 8L;
     const long gthr = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const long nthr = gridDim.x * (long)blockDim.x;
-    const unsigned nchain = (unsigned)min((w + 7) / 8, (long)gridDim.x);
+    const unsigned nchain = (unsigned)min((w + kChainWarps - 1) / kChainWarps, (long)gridDim.x);
     const bool in_chain = blockIdx.x < nchain;
-    const long cw = 8L * nchain;          // chain warps
-    const bool regs = cw >= w;            // one chain row per warp
+    const long cw = (long)kChainWarps * nchain;              // chain warps
+    const long crow = warp < kChainWarps ? blockIdx.x * (long)kChainWarps + warp : w;  // chain row, w: none
+    const bool regs = cw >= w;                               // one chain row per warp
+    const bool own_regs = regs && nb - 1 <= 32;              // a lane per step for the warp's own values
     GridBarrier *cbar = a.bar + 1;
     auto chain_failed = [&]() {
-        if (threadIdx.x == 0) atomicExch(&a.bar->err, 1);  // releases the CTAs waiting on bar[0]
+        if (threadIdx.x == kLeader) atomicExch(&a.bar->err, 1);  // releases the CTAs waiting on bar[0]
     };
     T pre[row_regs<T>()];
+    T own = 0;
 
     // A: y = blockdiag(Linv) b (b converted to T into z first)
     for (long g = gthr; g < npad; g += nthr) a.z[g] = g < a.n ? (T)a.rhs[g] : T(0);
-    if (!grid_barrier(a.bar, gridDim.x)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, r = row % s;
         T acc = warp_row_dot(a.linv + i * s * s + r * s, a.z + i * s, r + 1, lane);
         if (lane == 0) a.y[row] = acc;
     }
-    if (in_chain && regs && gwarp < w && nb > 1) row_to_regs(pre, a.pn + s * w + (s - w + gwarp) * w, w, lane);
-    if (!grid_barrier(a.bar, gridDim.x)) return;
+    if (in_chain && regs && crow < w && nb > 1) row_to_regs(pre, a.pn + s * w + (s - w + crow) * w, w, lane);
+    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     // B, chain rows
     if (in_chain) {
+        if (own_regs && crow < w && lane + 1 < nb) own = a.y[(lane + 1) * s + s - w + crow];
         for (long i = 1; i < nb; ++i) {
             const T *yp = a.y + i * s - w;
             if (regs) {
-                if (gwarp < w) {
-                    const T *row = a.pn + i * s * w + (s - w + gwarp) * w;
+                const T oi = own_regs ? __shfl_sync(0xffffffffu, own, (int)(i - 1)) : T(0);
+                if (crow < w) {
+                    const T *row = a.pn + i * s * w + (s - w + crow) * w;
                     const T acc = regs_row_dot(pre, row, yp, w, lane);
-                    if (lane == 0) a.y[i * s + s - w + gwarp] -= acc;
+                    if (lane == 0) {
+                        T *dst = a.y + i * s + s - w + crow;
+                        *dst = own_regs ? oi - acc : *dst - acc;
+                    }
                     if (i + 1 < nb) row_to_regs(pre, row + s * w, w, lane);
                 }
-            } else {
-                for (long r = gwarp; r < w; r += cw) {
+            } else if (warp < kChainWarps) {
+                for (long r = crow; r < w; r += cw) {
                     const T acc = warp_row_dot(a.pn + i * s * w + (s - w + r) * w, yp, w, lane);
                     if (lane == 0) a.y[i * s + s - w + r] -= acc;
                 }
             }
-            if (!grid_barrier(cbar, nchain)) {
+            if (!grid_barrier(cbar, nchain, ep_chain, kLeader)) {
                 chain_failed();
                 return;
             }
         }
     }
-    if (!grid_barrier(a.bar, gridDim.x)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     // B, the other rows, and z = y / D
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, r = row % s;
@@ -1322,39 +1341,44 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) solve_kernel(Solv
         if (i >= 1 && r < s - w) acc = warp_row_dot(a.pn + i * s * w + r * w, a.y + i * s - w, w, lane);
         if (lane == 0) a.z[row] = (a.y[row] - acc) * a.dinv[row];
     }
-    if (!grid_barrier(a.bar, gridDim.x)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     // C: v = blockdiag(Linv^T) z, warp per row of the stored transpose
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, c = row % s;
         T acc = warp_row_dot(a.linvt + i * s * s + c * s + c, a.z + i * s + c, s - c, lane);
         if (lane == 0) a.v[row] = acc;
     }
-    if (in_chain && regs && gwarp < w && nb > 1) row_to_regs(pre, a.rn + (nb - 2) * s * w + gwarp * w, w, lane);
-    if (!grid_barrier(a.bar, gridDim.x)) return;
+    if (in_chain && regs && crow < w && nb > 1) row_to_regs(pre, a.rn + (nb - 2) * s * w + crow * w, w, lane);
+    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     // D, chain rows
     if (in_chain) {
+        if (own_regs && crow < w && lane + 1 < nb) own = a.v[lane * s + crow];
         for (long i = nb - 2; i >= 0; --i) {
             const T *xn = a.v + (i + 1) * s;
             if (regs) {
-                if (gwarp < w) {
-                    const T *row = a.rn + i * s * w + gwarp * w;
+                const T oi = own_regs ? __shfl_sync(0xffffffffu, own, (int)i) : T(0);
+                if (crow < w) {
+                    const T *row = a.rn + i * s * w + crow * w;
                     const T acc = regs_row_dot(pre, row, xn, w, lane);
-                    if (lane == 0) a.v[i * s + gwarp] -= acc;
+                    if (lane == 0) {
+                        T *dst = a.v + i * s + crow;
+                        *dst = own_regs ? oi - acc : *dst - acc;
+                    }
                     if (i > 0) row_to_regs(pre, row - s * w, w, lane);
                 }
-            } else {
-                for (long c = gwarp; c < w; c += cw) {
+            } else if (warp < kChainWarps) {
+                for (long c = crow; c < w; c += cw) {
                     const T acc = warp_row_dot(a.rn + i * s * w + c * w, xn, w, lane);
                     if (lane == 0) a.v[i * s + c] -= acc;
                 }
             }
-            if (!grid_barrier(cbar, nchain)) {
+            if (!grid_barrier(cbar, nchain, ep_chain, kLeader)) {
                 chain_failed();
                 return;
             }
         }
     }
-    if (!grid_barrier(a.bar, gridDim.x)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
     // D, the other rows, and x = v
     for (long row = gwarp; row < a.n; row += nwarps) {
         const long i = row / s, c = row % s;
