@@ -413,12 +413,28 @@ __global__ void __launch_bounds__(256) rn_kernel(const T *band, long ld, long bw
 // Grid barrier for a cooperative launch. bar->count is zeroed before the
 // launch and only grows: the k-th barrier of a kernel (epoch, counted by
 // every thread) is passed once count reaches k * nblocks, so a CTA arrives
-// with one atomic and nothing is reset on the critical path. The wait is
-// bounded: after 2^24 polls (well over a second) the CTA records a timeout in
-// bar->err; once the flag is set no CTA waits any more. Returns false when
-// the flag is set, and the caller then leaves the kernel, so a fault cannot
-// hang the GPU; the host turns the flag into CB_ERR_TIMEOUT. leader is the
-// thread that arrives for the CTA.
+// with one atomic and nothing is reset on the critical path. The leader
+// thread arrives for its CTA after a CTA barrier, with an acq_rel atomic at
+// gpu scope (releasing the CTA's writes) and polls with acquire loads (so
+// the CTA reads the others' writes after the closing CTA barrier). The wait
+// is bounded: after 2^24 polls (well over a second) the CTA records a
+// timeout in bar->err; once the flag is set no CTA waits any more. Returns
+// false when the flag is set, and the caller then leaves the kernel, so a
+// fault cannot hang the GPU; the host turns the flag into CB_ERR_TIMEOUT.
+__device__ __forceinline__ unsigned barrier_arrive(unsigned *count)
+{
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;\n" : "=r"(old) : "l"(count) : "memory");
+    return old + 1u;
+}
+
+__device__ __forceinline__ unsigned barrier_count(const unsigned *count)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(count) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks, unsigned &epoch,
                                              unsigned leader = 0)
 {
@@ -430,12 +446,9 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks,
         failed = *verr;
         if (!failed) {
             const unsigned target = epoch * nblocks;
-            __threadfence();
-            const unsigned arrived = atomicAdd(&bar->count, 1u) + 1u;
-            if (arrived < target) {
-                volatile unsigned *vcount = &bar->count;
+            if (barrier_arrive(&bar->count) < target) {
                 unsigned long long polls = 0;
-                while (*vcount < target) {
+                while (barrier_count(&bar->count) < target) {
                     if (*verr) {
                         failed = 1;
                         break;
@@ -445,10 +458,8 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks,
                         failed = 1;
                         break;
                     }
-                    __nanosleep(32);
                 }
             }
-            __threadfence();
         }
     }
     __syncthreads();
@@ -555,6 +566,19 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
     const long ld = a.ld, bw = a.bw;
     long mprev = 0;
     for (long p = 0; p <= a.npad; p += NB) {
+        // the look-ahead block of this panel (step 3 of the previous one)
+        // comes into shared memory by cp.async, overlapping the staged copy;
+        // CTA 0 still holds it in A, Li and di
+        const bool look = !a.dist && p > 0 && p < a.npad;
+        if (look && blockIdx.x != 0) {
+            const T *lk = a.look + (int)((p / NB) & 1) * (2 * NB * NB + NB);
+            for (int e = tid; e < NB * NB; e += 256) {
+                cp_async_elem(&A[e / NB][e % NB], lk + e, true);
+                cp_async_elem(&Li[e / NB][e % NB], lk + NB * NB + e, true);
+            }
+            if (tid < NB) cp_async_elem(&di[tid], lk + 2 * NB * NB + tid, true);
+            cp_async_commit();
+        }
         // ---- 0. staged output of the previous panel into the band ----
         if (p > 0 && !a.dist) {
             const long pp = p - NB;
@@ -583,13 +607,8 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
         // ---- 1. diagonal block: LDL^T and Linv by warp 0 in registers; on
         //         the narrow path after the first panel CTA 0 has factored it
         //         ahead (step 3) and every CTA reads its result ----
-        if (!a.dist && p > 0) {
-            const T *lk = a.look + buf * (2 * NB * NB + NB);
-            for (int e = tid; e < NB * NB; e += 256) {
-                A[e / NB][e % NB] = lk[e];
-                Li[e / NB][e % NB] = lk[NB * NB + e];
-            }
-            if (tid < NB) di[tid] = lk[2 * NB * NB + tid];
+        if (look) {
+            if (blockIdx.x != 0) cp_async_wait0();
             __syncthreads();
         } else {
             for (int e = tid; e < NB * NB; e += 256) {
@@ -717,14 +736,21 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                 if (ti == tj && j0 + q < m) ls[c * m + j0 + q] = lv[u];
             }
             __syncthreads();
+            // tile (0,0) is the next panel's diagonal block: with m >= 32 it is
+            // complete here, and CTA 0 keeps it in A for the look-ahead
+            const bool keep = t == 0 && m >= NB;
             for (int idx = tid; idx < TS * TS; idx += 256) {
                 const int ji = idx / TS, ri = idx % TS;
                 const long rr = r0 + ri, jj = j0 + ji;
+                if (keep && ji > ri) A[ri][ji] = T(0);
                 if (rr >= m || jj >= m || jj > rr) continue;
                 T acc = 0;
 #pragma unroll 8
                 for (int k = 0; k < NB; ++k) acc += Ar[ri][k] * Ac[ji][k];
-                a.band[(p + NB + jj) * ld + (rr - jj)] -= acc;
+                T *slot = a.band + (p + NB + jj) * ld + (rr - jj);
+                const T nv = *slot - acc;
+                *slot = nv;
+                if (keep) A[ri][ji] = nv;
             }
             __syncthreads();
         }
@@ -735,11 +761,13 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
             const long pn = p + NB;
             const int bn = (int)((pn / NB) & 1);
             __syncthreads();
-            for (int e = tid; e < NB * NB; e += 256) {
-                const int jj = e / NB, ii = e % NB;
-                A[ii][jj] = (ii >= jj && ii - jj <= bw) ? a.band[(pn + jj) * ld + (ii - jj)] : T(0);
+            if (m < NB) {  // a band narrower than a panel: not all of the block was in tile (0,0)
+                for (int e = tid; e < NB * NB; e += 256) {
+                    const int jj = e / NB, ii = e % NB;
+                    A[ii][jj] = (ii >= jj && ii - jj <= bw) ? a.band[(pn + jj) * ld + (ii - jj)] : T(0);
+                }
+                __syncthreads();
             }
-            __syncthreads();
             if (warp == 0) {
                 ldlt32_split(A, Li, di);
                 record_pivots(a, pn, A[lane][lane], di[lane], lane);
