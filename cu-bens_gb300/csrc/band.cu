@@ -560,6 +560,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
     __shared__ T di[NB];
     __shared__ T Ar[TS][NB + 1];  // raw panel rows of the tile's row block, then W
     __shared__ T Ac[TS][NB + 1];  // raw panel rows of the tile's column block, then L
+    __shared__ T Bo[TS][TS + 1];  // the first tile's band values before this panel's update
     __shared__ T Wd[NB][64];      // wide bands: W of a 64-row block (k-major)
     __shared__ T Ld[NB][64];      // wide bands: L of a 64-column block
     const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
@@ -577,16 +578,45 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                 cp_async_elem(&Li[e / NB][e % NB], lk + NB * NB + e, true);
             }
             if (tid < NB) cp_async_elem(&di[tid], lk + 2 * NB * NB + tid, true);
-            cp_async_commit();
         }
-        // ---- 0. staged output of the previous panel into the band ----
-        if (p > 0 && !a.dist) {
+        long m = a.npad - p - NB;
+        if (m > bw) m = bw;
+        if (m < 0) m = 0;
+        // the first trailing tile's inputs are final at the barrier (the
+        // staged copy below writes only the previous panel's columns): its
+        // raw panel rows and the band values it updates come in by cp.async
+        // too, so the tile starts with its data on chip
+        const long nt_first = (m + TS - 1) / TS;
+        const bool first_pre = !a.dist && p < a.npad && blockIdx.x < nt_first * (nt_first + 1) / 2;
+        if (first_pre) {
+            long ti, tj;
+            tile_of((long)blockIdx.x, ti, tj);
+            const long r0 = ti * TS, j0 = tj * TS;
+            for (int idx = tid; idx < NB * TS; idx += 256) {
+                const int k = idx / TS, q = idx % TS;
+                const long o1 = NB + r0 + q - k, o2 = NB + j0 + q - k;
+                const bool v1 = r0 + q < m && o1 <= bw, v2 = j0 + q < m && o2 <= bw;
+                cp_async_elem(&Ar[q][k], v1 ? a.band + (p + k) * ld + o1 : a.band, v1);
+                cp_async_elem(&Ac[q][k], v2 ? a.band + (p + k) * ld + o2 : a.band, v2);
+            }
+            for (int idx = tid; idx < TS * TS; idx += 256) {
+                const int ji = idx / TS, ri = idx % TS;
+                const long rr = r0 + ri, jj = j0 + ji;
+                const bool v = rr < m && jj < m && jj <= rr;
+                cp_async_elem(&Bo[ri][ji], v ? a.band + (p + NB + jj) * ld + (rr - jj) : a.band, v);
+            }
+        }
+        cp_async_commit();
+        // ---- 0. staged output of the previous panel into the band (CTA 0,
+        //         the look-ahead's owner, stays out when there are others) ----
+        const unsigned c0 = gridDim.x > 1 ? 1u : 0u;
+        if (p > 0 && !a.dist && blockIdx.x >= c0) {
             const long pp = p - NB;
             const int buf = (int)((pp / NB) & 1);
             const T *ls = a.wbuf + (long)buf * NB * bw;
             const T *ds = a.dstage + buf * NB * NB;
             const long total = NB * NB + NB * mprev;
-            for (long idx = blockIdx.x * 256L + tid; idx < total; idx += gridDim.x * 256L) {
+            for (long idx = (blockIdx.x - c0) * 256L + tid; idx < total; idx += (gridDim.x - c0) * 256L) {
                 if (idx < NB * NB) {
                     const int j = (int)(idx / NB), i = (int)(idx % NB);
                     if (i >= j && i - j <= bw) a.band[(pp + j) * ld + (i - j)] = ds[idx];
@@ -600,15 +630,12 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
             }
         }
         if (p == a.npad) break;
-        long m = a.npad - p - NB;
-        if (m > bw) m = bw;
-        if (m < 0) m = 0;
         const int buf = (int)((p / NB) & 1);
         // ---- 1. diagonal block: LDL^T and Linv by warp 0 in registers; on
         //         the narrow path after the first panel CTA 0 has factored it
         //         ahead (step 3) and every CTA reads its result ----
+        cp_async_wait0();  // the look-ahead block and the first tile's inputs
         if (look) {
-            if (blockIdx.x != 0) cp_async_wait0();
             __syncthreads();
         } else {
             for (int e = tid; e < NB * NB; e += 256) {
@@ -705,13 +732,15 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
             long ti, tj;
             tile_of(t, ti, tj);
             const long r0 = ti * TS, j0 = tj * TS;
+            const bool pre = t == blockIdx.x && first_pre;  // inputs already on chip
             // raw panel rows: X[q][k] = A(p+32+r0+q, p+k)
-            for (int idx = tid; idx < NB * TS; idx += 256) {
-                const int k = idx / TS, q = idx % TS;
-                const long o1 = NB + r0 + q - k, o2 = NB + j0 + q - k;
-                Ar[q][k] = (r0 + q < m && o1 <= bw) ? a.band[(p + k) * ld + o1] : T(0);
-                Ac[q][k] = (j0 + q < m && o2 <= bw) ? a.band[(p + k) * ld + o2] : T(0);
-            }
+            if (!pre)
+                for (int idx = tid; idx < NB * TS; idx += 256) {
+                    const int k = idx / TS, q = idx % TS;
+                    const long o1 = NB + r0 + q - k, o2 = NB + j0 + q - k;
+                    Ar[q][k] = (r0 + q < m && o1 <= bw) ? a.band[(p + k) * ld + o1] : T(0);
+                    Ac[q][k] = (j0 + q < m && o2 <= bw) ? a.band[(p + k) * ld + o2] : T(0);
+                }
             __syncthreads();
             // W = X Linv^T for the row block, L = W D^-1 for the column block
             T wv[TS * NB / 256], lv[TS * NB / 256];
@@ -748,7 +777,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
 #pragma unroll 8
                 for (int k = 0; k < NB; ++k) acc += Ar[ri][k] * Ac[ji][k];
                 T *slot = a.band + (p + NB + jj) * ld + (rr - jj);
-                const T nv = *slot - acc;
+                const T nv = (pre ? Bo[ri][ji] : *slot) - acc;
                 *slot = nv;
                 if (keep) A[ri][ji] = nv;
             }
