@@ -509,18 +509,19 @@ __device__ __forceinline__ void record_pivots(const FactorArgs<T> &a, long p, T 
 __device__ __noinline__ void ldlt32_noinv(float (*A)[NB + 1], float *di);
 
 // Inverse of the unit-lower L held below the diagonal of A (one warp, lane
-// j forms column j: x_rr = -sum_{k<rr} L_rr,k x_k, the terms in ascending
-// k), into Li (row-major).
+// j forms column j: x_rr = -sum_{k<rr} L_rr,k x_k, summed in four chains of
+// k mod 4), into Li (row-major).
 __device__ __noinline__ void linv32_warp(const float (*A)[NB + 1], float (*Li)[NB + 1])
 {
     const int lane = threadIdx.x % 32;
     float x[NB];
 #pragma unroll
     for (int rr = 0; rr < NB; ++rr) {
-        float acc = 0;
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // four chains of k mod 4
 #pragma unroll
-        for (int k = 0; k < rr; ++k) acc += A[rr][k] * x[k];
-        x[rr] = rr == lane ? 1.0f : (rr < lane ? 0.0f : -acc);
+        for (int k = 0; k < rr; ++k) acc[k & 3] += A[rr][k] * x[k];
+        const float s = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+        x[rr] = rr == lane ? 1.0f : (rr < lane ? 0.0f : -s);
     }
 #pragma unroll
     for (int j = 0; j < NB; ++j) Li[j][lane] = x[j];
@@ -567,18 +568,16 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
     const long ld = a.ld, bw = a.bw;
     long mprev = 0;
     for (long p = 0; p <= a.npad; p += NB) {
-        // the look-ahead block of this panel (step 3 of the previous one)
-        // comes into shared memory by cp.async, overlapping the staged copy;
-        // CTA 0 still holds it in A, Li and di
+        // the look-ahead block of this panel (step 3 of the previous one:
+        // L, D and 1/D) comes into shared memory by cp.async, overlapping
+        // the staged copy; CTA 0 still holds it in A and di
         const bool look = !a.dist && p > 0 && p < a.npad;
         if (look && blockIdx.x != 0) {
-            const T *lk = a.look + (int)((p / NB) & 1) * (2 * NB * NB + NB);
-            for (int e = tid; e < NB * NB; e += 256) {
-                cp_async_elem(&A[e / NB][e % NB], lk + e, true);
-                cp_async_elem(&Li[e / NB][e % NB], lk + NB * NB + e, true);
-            }
-            if (tid < NB) cp_async_elem(&di[tid], lk + 2 * NB * NB + tid, true);
+            const T *lk = a.look + (int)((p / NB) & 1) * (NB * NB + NB);
+            for (int e = tid; e < NB * NB; e += 256) cp_async_elem(&A[e / NB][e % NB], lk + e, true);
+            if (tid < NB) cp_async_elem(&di[tid], lk + NB * NB + tid, true);
         }
+        cp_async_commit();
         long m = a.npad - p - NB;
         if (m > bw) m = bw;
         if (m < 0) m = 0;
@@ -609,7 +608,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
         cp_async_commit();
         // ---- 0. staged output of the previous panel into the band (CTA 0,
         //         the look-ahead's owner, stays out when there are others) ----
-        const unsigned c0 = gridDim.x > 1 ? 1u : 0u;
+        const unsigned c0 = gridDim.x > 1 ? 1u : 0u;  // (the tile's group)
         if (p > 0 && !a.dist && blockIdx.x >= c0) {
             const long pp = p - NB;
             const int buf = (int)((pp / NB) & 1);
@@ -633,11 +632,16 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
         const int buf = (int)((p / NB) & 1);
         // ---- 1. diagonal block: LDL^T and Linv by warp 0 in registers; on
         //         the narrow path after the first panel CTA 0 has factored it
-        //         ahead (step 3) and every CTA reads its result ----
-        cp_async_wait0();  // the look-ahead block and the first tile's inputs
+        //         ahead (step 3), and every CTA forms Linv from its L while
+        //         the first tile's inputs are still on their way ----
         if (look) {
+            cp_async_wait1();  // the look-ahead block
+            __syncthreads();
+            if (warp == 0) linv32_warp(A, Li);
+            cp_async_wait0();  // the first tile's inputs
             __syncthreads();
         } else {
+            cp_async_wait0();
             for (int e = tid; e < NB * NB; e += 256) {
                 const int jj = e / NB, ii = e % NB;
                 A[ii][jj] = (ii >= jj && ii - jj <= bw) ? a.band[(p + jj) * ld + (ii - jj)] : T(0);
@@ -785,7 +789,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
         }
         // ---- 3. look-ahead (CTA 0, whose first tile (0,0) is the next panel's
         //         diagonal block, final now): factor it before the barrier,
-        //         record its pivots, stage it, publish A, Linv, 1/D ----
+        //         record its pivots, stage it, publish L, D and 1/D ----
         if (blockIdx.x == 0 && m > 0) {
             const long pn = p + NB;
             const int bn = (int)((pn / NB) & 1);
@@ -798,18 +802,17 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                 __syncthreads();
             }
             if (warp == 0) {
-                ldlt32_split(A, Li, di);
+                ldlt32_noinv(A, di);
                 record_pivots(a, pn, A[lane][lane], di[lane], lane);
             }
             __syncthreads();
             T *ds = a.dstage + bn * NB * NB;
-            T *lk = a.look + bn * (2 * NB * NB + NB);
+            T *lk = a.look + bn * (NB * NB + NB);
             for (int idx = tid; idx < NB * NB; idx += 256) {
                 ds[idx] = A[idx % NB][idx / NB];
                 lk[idx] = A[idx / NB][idx % NB];
-                lk[NB * NB + idx] = Li[idx / NB][idx % NB];
             }
-            if (tid < NB) lk[2 * NB * NB + tid] = di[tid];
+            if (tid < NB) lk[NB * NB + tid] = di[tid];
         }
         mprev = m;
         if (!grid_barrier(a.bar, gridDim.x, ep)) return;
@@ -1807,7 +1810,7 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use
     CB_CUDA(cudaMalloc(&f.flags, 2 * sizeof(int)));
     CB_CUDA(cudaMalloc(&f.bar, 2 * sizeof(GridBarrier)));  // the solve's grid and chain barriers
     CB_CUDA(cudaMalloc(&f.stage, es * 2 * NB * NB));
-    CB_CUDA(cudaMalloc(&f.look, es * 2 * (2 * NB * NB + NB)));
+    CB_CUDA(cudaMalloc(&f.look, es * 2 * (NB * NB + NB)));  // two panels of L, D and 1/D
     CB_CUDA(cudaMemset(f.bar, 0, 2 * sizeof(GridBarrier)));
     CB_CUDA(cudaMalloc(&f.fbar, sizeof(GridBarrier)));
     CB_CUDA(cudaMemset(f.fbar, 0, sizeof(GridBarrier)));
