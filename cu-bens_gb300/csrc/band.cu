@@ -746,42 +746,50 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                     Ac[q][k] = (j0 + q < m && o2 <= bw) ? a.band[(p + k) * ld + o2] : T(0);
                 }
             __syncthreads();
-            // W = X Linv^T for the row block, L = W D^-1 for the column block
-            T wv[TS * NB / 256], lv[TS * NB / 256];
+            // W = X Linv^T for the row block, L = W D^-1 for the column block:
+            // thread (warp, lane) forms row lane, columns warp + 8u, in eight
+            // independent chains (Linv's upper triangle holds zeros)
+            static_assert(TS == NB, "32 x 32 trailing tiles");
+            T wv[4] = {0, 0, 0, 0}, lv[4] = {0, 0, 0, 0};
+#pragma unroll 8
+            for (int k = 0; k < NB; ++k) {
+                const T x1 = Ar[lane][k], x2 = Ac[lane][k];
 #pragma unroll
-            for (int u = 0; u < TS * NB / 256; ++u) {
-                const int idx = tid + 256 * u, c = idx / TS, q = idx % TS;
-                T w1 = 0, w2 = 0;
-                for (int k = 0; k <= c; ++k) {
-                    const T li = Li[c][k];
-                    w1 += Ar[q][k] * li;
-                    w2 += Ac[q][k] * li;
+                for (int u = 0; u < 4; ++u) {
+                    const T li = Li[warp + 8 * u][k];
+                    wv[u] += x1 * li;
+                    lv[u] += x2 * li;
                 }
-                wv[u] = w1;
-                lv[u] = w2 * di[c];
             }
             __syncthreads();
 #pragma unroll
-            for (int u = 0; u < TS * NB / 256; ++u) {
-                const int idx = tid + 256 * u, c = idx / TS, q = idx % TS;
-                Ar[q][c] = wv[u];
-                Ac[q][c] = lv[u];
-                if (ti == tj && j0 + q < m) ls[c * m + j0 + q] = lv[u];
+            for (int u = 0; u < 4; ++u) {
+                const int c = warp + 8 * u;
+                lv[u] *= di[c];
+                Ar[lane][c] = wv[u];
+                Ac[lane][c] = lv[u];
+                if (ti == tj && j0 + lane < m) ls[c * m + j0 + lane] = lv[u];
             }
             __syncthreads();
-            // tile (0,0) is the next panel's diagonal block: with m >= 32 it is
-            // complete here, and CTA 0 keeps it in A for the look-ahead
+            // the update, row lane and columns warp + 8u of the tile; tile (0,0)
+            // is the next panel's diagonal block: with m >= 32 it is complete
+            // here, and CTA 0 keeps it in A for the look-ahead
             const bool keep = t == 0 && m >= NB;
-            for (int idx = tid; idx < TS * TS; idx += 256) {
-                const int ji = idx / TS, ri = idx % TS;
+            T acc[4] = {0, 0, 0, 0};
+#pragma unroll 8
+            for (int k = 0; k < NB; ++k) {
+                const T x = Ar[lane][k];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) acc[u] += x * Ac[warp + 8 * u][k];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int ri = lane, ji = warp + 8 * u;
                 const long rr = r0 + ri, jj = j0 + ji;
                 if (keep && ji > ri) A[ri][ji] = T(0);
                 if (rr >= m || jj >= m || jj > rr) continue;
-                T acc = 0;
-#pragma unroll 8
-                for (int k = 0; k < NB; ++k) acc += Ar[ri][k] * Ac[ji][k];
                 T *slot = a.band + (p + NB + jj) * ld + (rr - jj);
-                const T nv = (pre ? Bo[ri][ji] : *slot) - acc;
+                const T nv = (pre ? Bo[ri][ji] : *slot) - acc[u];
                 *slot = nv;
                 if (keep) A[ri][ji] = nv;
             }
@@ -831,15 +839,17 @@ __device__ __noinline__ void ldlt32_noinv(float (*A)[NB + 1], float *di)
     for (int j = 0; j < NB; ++j) r[j] = A[lane][j];
 #pragma unroll
     for (int k = 0; k < NB; ++k) {
-        const float d = __shfl_sync(0xffffffffu, r[k], k);
-        const float rd = __frcp_rn(d);  // the correctly rounded 1/d
-        const float l = lane > k ? r[k] * rd : 0.0f;
+        // row j's unscaled column-k entry c_j = l_jk d_k gives the update
+        // l_ik d_k l_jk = l_ik c_j, so the broadcasts of c_j need only the
+        // previous step's update, not this step's reciprocal
+        const float rk = r[k];
+        const float rd = __frcp_rn(__shfl_sync(0xffffffffu, rk, k));  // the correctly rounded 1/d
+        const float l = lane > k ? rk * rd : 0.0f;
         if (lane > k) r[k] = l;
-        const float ldk = l * d;
 #pragma unroll
         for (int j = k + 1; j < NB; ++j) {
-            const float ljk = __shfl_sync(0xffffffffu, l, j);
-            if (j <= lane) r[j] -= ldk * ljk;
+            const float cj = __shfl_sync(0xffffffffu, rk, j);
+            if (j <= lane) r[j] -= l * cj;
         }
     }
     float dl = 0;
