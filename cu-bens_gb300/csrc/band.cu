@@ -24,11 +24,13 @@
 // so that one solve is
 //     y_i = Linv_i b_i - Pn_i y_{i-1}[s-w:s]            (forward)
 //     x_i = Linv_i^T (y_i / D_i) - Rn_i x_{i+1}[0:w]    (backward)
-// run by one persistent cooperative kernel with 2*nblk + 2 grid barriers
-// (Linv is also kept transposed so both block-diagonal products are
-// coalesced row dots). A
-// larger s lowers the number of sequential steps while the bytes per step
-// (s*w) and per solve stay about the same.
+// run by one persistent cooperative kernel (solve_kernel). Only the w rows of
+// each block that feed the next one form the serial recurrence; they run on
+// a few CTAs with a barrier of their own, and the other rows follow in
+// grid-wide passes. Linv is also kept transposed so both block-diagonal
+// products are coalesced row dots. A larger s lowers the number of
+// sequential steps while the bytes per step (s*w) and per solve stay about
+// the same.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 

@@ -141,7 +141,7 @@ struct BandFactor {
     GridBarrier *bar = nullptr;  // persistent-solve barrier
     GridBarrier *fbar = nullptr; // persistent-factor barrier
     void *stage = nullptr;       // 2 x 32x32: staged factored diagonal blocks (FP32 factor)
-    void *look = nullptr;        // 2 x (2 x 32x32 + 32): the next panel's factored block, Linv, 1/D
+    void *look = nullptr;        // 2 x (32x32 + 32): the next panel's factored block (L, D) and 1/D
     bool fp32 = false;
     bool direct = false;         // no solve blocks: substitution with the band (one solve per factor)
     int solve_grid = 1;          // CTAs of the cooperative solve launch
