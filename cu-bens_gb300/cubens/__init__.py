@@ -264,6 +264,16 @@ class Model:
     def results_close(self):
         self._check(load().cb_results_close(self.h))
 
+    def checkpoint_save(self, path):
+        """Newmark: the converged state after the last completed time step,
+        bit for bit, to a binary file (checkPoint, misc.c:494-603)."""
+        self._check(load().cb_checkpoint_save(self.h, str(path).encode()))
+
+    def checkpoint_load(self, path):
+        """Newmark, after newmark_begin: continue from a checkpoint of the
+        same model (restartStep, misc.c:605-716)."""
+        self._check(load().cb_checkpoint_load(self.h, str(path).encode()))
+
     def newton_begin(self):
         self._check(load().cb_newton_begin(self.h))
 

@@ -233,6 +233,22 @@ int cb_results_open(cb_model *m, const char *dir);
 int cb_results_write(cb_model *m, double lam, int iterations);
 int cb_results_close(cb_model *m);
 
+/* Checkpoint and restart of the nonlinear Newmark driver (checkPoint and
+ * restartStep, misc.c:494-716). cb_checkpoint_save writes the converged
+ * state after the last completed time step to a binary file, bit for bit:
+ * velocities, accelerations, mass, d, f, coordinates, triads, deformed
+ * lengths and element forces, the next step and the time increment
+ * multiplier. cb_checkpoint_load, on a handle of the same model after
+ * cb_newmark_begin, restores it, and the following cb_newmark_step calls
+ * continue exactly as the uninterrupted run. The learned preconditioner's
+ * network is not part of the state. Errors: CB_ERR_UNSUPPORTED for other
+ * drivers, CB_ERR_STATE before cb_newmark_begin, CB_ERR_ARG when the file
+ * cannot be opened or written or belongs to a model of other sizes,
+ * CB_ERR_PARSE for a file of another format or a truncated one (the handle
+ * is unchanged then). */
+int cb_checkpoint_save(cb_model *m, const char *path);
+int cb_checkpoint_load(cb_model *m, const char *path);
+
 int cb_get_timers(const cb_model *m, cb_timers *t);
 int cb_reset_timers(cb_model *m);
 /* Enable/disable per-phase CUDA-event timing (adds event records). */
