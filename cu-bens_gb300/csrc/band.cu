@@ -845,7 +845,12 @@ __device__ __noinline__ void ldlt32_noinv(float (*A)[NB + 1], float *di)
         // l_ik d_k l_jk = l_ik c_j, so the broadcasts of c_j need only the
         // previous step's update, not this step's reciprocal
         const float rk = r[k];
-        const float rd = __frcp_rn(__shfl_sync(0xffffffffu, rk, k));  // the correctly rounded 1/d
+        // the hardware's approximate 1/d (rcp.approx.ftz, within an ulp or so):
+        // it only scales this column's L entries, so the correctly rounded
+        // reciprocal's extra steps stay off the panel's serial chain; D and
+        // 1/D themselves are exact below
+        float rd;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rd) : "f"(__shfl_sync(0xffffffffu, rk, k)));
         const float l = lane > k ? rk * rd : 0.0f;
         if (lane > k) r[k] = l;
 #pragma unroll
