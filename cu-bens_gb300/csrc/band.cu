@@ -753,14 +753,25 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
             // independent chains (Linv's upper triangle holds zeros)
             static_assert(TS == NB, "32 x 32 trailing tiles");
             T wv[4] = {0, 0, 0, 0}, lv[4] = {0, 0, 0, 0};
+            if (ti == tj) {  // a diagonal tile: its row and column blocks are the same rows
 #pragma unroll 8
-            for (int k = 0; k < NB; ++k) {
-                const T x1 = Ar[lane][k], x2 = Ac[lane][k];
+                for (int k = 0; k < NB; ++k) {
+                    const T x1 = Ar[lane][k];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const T li = Li[warp + 8 * u][k];
-                    wv[u] += x1 * li;
-                    lv[u] += x2 * li;
+                    for (int u = 0; u < 4; ++u) wv[u] += x1 * Li[warp + 8 * u][k];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) lv[u] = wv[u];
+            } else {
+#pragma unroll 8
+                for (int k = 0; k < NB; ++k) {
+                    const T x1 = Ar[lane][k], x2 = Ac[lane][k];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const T li = Li[warp + 8 * u][k];
+                        wv[u] += x1 * li;
+                        lv[u] += x2 * li;
+                    }
                 }
             }
             __syncthreads();
