@@ -662,7 +662,7 @@ def run_ours(args, world, rank, local, pg):
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                          # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the grid factor
                          # (ncu capture, profiles/factor_f32_kernel_panel64.md); the cluster factor has none
-                         "traffic": None if info.get("factor_cluster") else 39.74e6 + 3.58e6,
+                         "traffic": None if info.get("factor_cluster") else 39.74e6 + 3.65e6,
                          "traffic_source": "profiles/factor_f32_kernel_panel64.md",
                          "bytes_per_launch": bytes_ldlt, "ms_per_launch": ms_ldlt,
                          "note": "latency-bound: 780 dependent panels; bytes = the band read and written "
@@ -672,7 +672,7 @@ def run_ours(args, world, rank, local, pg):
                                "frac": achieved_solve / hbm_peak, "peak_kind": peak_kind,
                                # one launch's dram__bytes_read.sum + dram__bytes_write.sum (ncu capture of
                                # the same command with --steps 3, profiles/factor_f32_kernel_panel64.md)
-                               "traffic": 247.35e6 + 4.09e6, "traffic_source": "profiles/factor_f32_kernel_panel64.md",
+                               "traffic": 247.31e6 + 4.44e6, "traffic_source": "profiles/factor_f32_kernel_panel64.md",
                                "bytes_per_launch": bytes_solve, "ms_per_launch": ms_solve},
             "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
             "e2e": e2e,
