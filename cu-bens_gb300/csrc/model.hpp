@@ -35,6 +35,15 @@ struct cb_status_error : std::runtime_error {
 
 struct cb_results_state;
 
+// Pinned host copies of the small values the drivers read back every
+// iteration or step, so that each read is an asynchronous copy and one
+// stream synchronisation serves them all.
+struct cb_host_stage {
+    cb::GridBarrier bar[2];  // the solve's and the factor's grid barriers (err flags)
+    int flags[2];            // the factor's det and zero-pivot flags
+    double val[2];           // one reduced scalar
+};
+
 struct cb_model {
     cb::HostModel h;
     cb_options opt{};
@@ -69,6 +78,7 @@ struct cb_model {
     double learn_stall = 2.0;
     long bj_solves = 0, bj_iters = 0, learned_solves = 0, fallbacks = 0;
     cb::MsalScalars *sc = nullptr, *sc_h = nullptr;
+    cb_host_stage *hs = nullptr;  // pinned
     double *partial = nullptr;
 
     // MSAL host control state (main.c:2205-2230)

@@ -181,6 +181,8 @@ void upload_model(cb_model *m)
         m->partial = m->alloc<double>(16 * cb::kRedBlocks);
         CB_CUDA(cudaMallocHost(&m->sc_h, sizeof(cb::MsalScalars)));
         std::memset(m->sc_h, 0, sizeof(cb::MsalScalars));
+        CB_CUDA(cudaMallocHost(&m->hs, sizeof(cb_host_stage)));
+        std::memset(m->hs, 0, sizeof(cb_host_stage));
         CB_CUDA(cudaStreamSynchronize(st));
         return;
     }
@@ -207,6 +209,8 @@ void upload_model(cb_model *m)
     m->partial = m->alloc<double>(16 * cb::kRedBlocks);
     CB_CUDA(cudaMallocHost(&m->sc_h, sizeof(cb::MsalScalars)));
     std::memset(m->sc_h, 0, sizeof(cb::MsalScalars));
+    CB_CUDA(cudaMallocHost(&m->hs, sizeof(cb_host_stage)));
+    std::memset(m->hs, 0, sizeof(cb_host_stage));
     CB_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -358,7 +362,8 @@ void solve(cb_model *m, const double *rhs, double *x)
 cb::MsalScalars &pull_scalars(cb_model *m)
 {
     d2h(m->sc_h, m->sc, 1, m->st);
-    cb::GridBarrier bar[2]{};
+    cb::GridBarrier *bar = m->hs->bar;
+    bar[0].err = bar[1].err = 0;
     if (m->bf.bar) d2h(&bar[0], m->bf.bar, 1, m->st);
     if (m->bf.fbar) d2h(&bar[1], m->bf.fbar, 1, m->st);
     CB_CUDA(cudaStreamSynchronize(m->st));
@@ -372,10 +377,9 @@ double device_dot(cb_model *m, const double *a, const double *b, bool diff)
     PhaseTimer t(m, &m->tm.ms_vector);
     cb::launch_dot(a, b, m->partial, m->sc, 15, m->h.neq, m->st, diff);
     m->tm.launches += 2;
-    double v = 0;
-    d2h(&v, &m->sc->dots[15], 1, m->st);
+    d2h(&m->hs->val[0], &m->sc->dots[15], 1, m->st);
     CB_CUDA(cudaStreamSynchronize(m->st));
-    return v;
+    return m->hs->val[0];
 }
 
 double device_elem(cb_model *m, const double *v, long i)
@@ -505,10 +509,9 @@ void msal_begin(cb_model *m, cb_step *out)
     m->beta = std::sqrt((double)h.iteopt / (double)itecnt) * (m->dnormallow / m->dnorm);
     m->psi = 1;
     cb::launch_psi(m->bf.ssd, m->ssd_o, m->partial, m->sc, 14, N, st);
-    double ps = 0;
-    d2h(&ps, &m->sc->dots[14], 1, st);
+    d2h(&m->hs->val[0], &m->sc->dots[14], 1, st);
     CB_CUDA(cudaStreamSynchronize(st));
-    m->psi = ps;
+    m->psi = m->hs->val[0];
     m->errchk2 = m->subcnt = m->imagcnt = m->negcnt = 0;
     m->itecnt = itecnt;
     m->phase = 1;
@@ -547,7 +550,7 @@ void msal_step(cb_model *m, cb_step *out)
         assemble_tangent(m);
         factor(m);
         solve(m, m->q, m->ddq);
-        int flags[2] = {0, 0};
+        int *flags = m->hs->flags;
         d2h(flags, m->bf.flags, 2, st);
         CB_CUDA(cudaStreamSynchronize(st));
         if (flags[1]) throw cb_status_error(CB_ERR_NUMERIC, "singular stiffness matrix (zero pivot)");
@@ -634,10 +637,9 @@ void msal_step(cb_model *m, cb_step *out)
         m->dkc = std::fabs(out->dk);
         m->lpfc = std::fabs(m->lpf);
         cb::launch_psi(m->bf.ssd, m->ssd_o, m->partial, m->sc, 14, N, st);
-        double ps = 0;
-        d2h(&ps, &m->sc->dots[14], 1, st);
+        d2h(&m->hs->val[0], &m->sc->dots[14], 1, st);
         CB_CUDA(cudaStreamSynchronize(st));
-        m->psi = ps;
+        m->psi = m->hs->val[0];
         m->subcnt = m->imagcnt = m->negcnt = 0;
         m->itecnt = itecnt;
         out->lam = m->lpf;
@@ -725,6 +727,7 @@ int cb_model_destroy(cb_model *m)
     cb::mpnn_destroy(m->mp);
     for (void *p : m->allocs) cudaFree(p);
     if (m->sc_h) cudaFreeHost(m->sc_h);
+    if (m->hs) cudaFreeHost(m->hs);
     for (auto &e : m->ev)
         if (e) cudaEventDestroy(e);
     for (auto &e : m->marks)
