@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <thread>
 
 #include "internal.hpp"
 
@@ -474,11 +475,37 @@ void collect_tangent_pairs(const HostModel &m, std::vector<TangentPair> &all)
 }
 
 // Groups contributions by key (stable, so each list keeps the order above).
+// Large maps are split by key range into one bucket per host thread (a
+// stable scatter, so equal keys keep their order), and the buckets are
+// sorted in parallel; their concatenation is the sequential stable sort.
 template <typename Key>
 void group_pairs(std::vector<TangentPair> &all, Key key, GatherMap &g, std::vector<int64_t> &keys)
 {
-    std::stable_sort(all.begin(), all.end(),
-                     [&](const TangentPair &a, const TangentPair &b) { return key(a) < key(b); });
+    auto less = [&](const TangentPair &a, const TangentPair &b) { return key(a) < key(b); };
+    const size_t n = all.size();
+    const unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (n < (size_t)1 << 16 || nthreads == 1) {
+        std::stable_sort(all.begin(), all.end(), less);
+    } else {
+        int64_t kmax = 0;
+        for (const TangentPair &p : all) kmax = std::max(kmax, key(p));
+        const unsigned nb = nthreads;
+        auto bucket = [&](const TangentPair &p) {  // non-decreasing in the key
+            const unsigned b = (unsigned)((double)key(p) / ((double)kmax + 1.0) * nb);
+            return std::min(b, nb - 1);
+        };
+        std::vector<size_t> start(nb + 1, 0);
+        for (const TangentPair &p : all) ++start[bucket(p) + 1];
+        for (unsigned b = 0; b < nb; ++b) start[b + 1] += start[b];
+        std::vector<TangentPair> out(n);
+        std::vector<size_t> pos(start.begin(), start.end() - 1);
+        for (const TangentPair &p : all) out[pos[bucket(p)]++] = p;
+        std::vector<std::thread> pool;
+        for (unsigned b = 0; b < nb; ++b)
+            pool.emplace_back([&, b] { std::stable_sort(out.begin() + start[b], out.begin() + start[b + 1], less); });
+        for (std::thread &t : pool) t.join();
+        all.swap(out);
+    }
     g.ptr.clear();
     g.src.clear();
     keys.clear();
