@@ -465,13 +465,36 @@ void collect_tangent_pairs(const HostModel &m, std::vector<TangentPair> &all)
             for (int ie = 0; ie <= je; ++ie)
                 add(mc, ie, je, (int)(171 * E + 21 * T + packed(ie, je, 14) * F + e));
     }
-    for (long e = 0; e < E; ++e) {
-        long mc[18];
-        for (int a = 0; a < 3; ++a)
-            for (int d = 0; d < 6; ++d) mc[a * 6 + d] = m.jcode[m.sh_conn[e * 3 + a] * 7 + d];
-        for (int je = 0; je < 18; ++je)
-            for (int ie = 0; ie <= je; ++ie) add(mc, ie, je, (int)(packed(ie, je, 18) * E + e));
+    // shells, the bulk: contiguous element ranges on host threads, each into
+    // its own list, appended in range order (the same order as one loop)
+    auto shells = [&](long e0, long e1, std::vector<TangentPair> &out) {
+        for (long e = e0; e < e1; ++e) {
+            long mc[18];
+            for (int a = 0; a < 3; ++a)
+                for (int d = 0; d < 6; ++d) mc[a * 6 + d] = m.jcode[m.sh_conn[e * 3 + a] * 7 + d];
+            for (int je = 0; je < 18; ++je)
+                for (int ie = 0; ie <= je; ++ie) {
+                    if (!mc[ie] || !mc[je]) continue;
+                    out.push_back({std::max(mc[ie], mc[je]) - 1, std::min(mc[ie], mc[je]) - 1,
+                                   (int)(packed(ie, je, 18) * E + e)});
+                }
+        }
+    };
+    const unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (E < 4096 || nthreads == 1) {
+        shells(0, E, all);
+        return;
     }
+    std::vector<std::vector<TangentPair>> parts(nthreads);
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nthreads; ++t)
+        pool.emplace_back([&, t] {
+            const long e0 = E * (long)t / nthreads, e1 = E * (long)(t + 1) / nthreads;
+            parts[t].reserve((size_t)(171 * (e1 - e0)));
+            shells(e0, e1, parts[t]);
+        });
+    for (std::thread &th : pool) th.join();
+    for (const auto &part : parts) all.insert(all.end(), part.begin(), part.end());
 }
 
 // Groups contributions by key (stable, so each list keeps the order above).
