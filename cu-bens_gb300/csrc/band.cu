@@ -419,10 +419,12 @@ __global__ void __launch_bounds__(256) rn_kernel(const T *band, long ld, long bw
 // thread arrives for its CTA after a CTA barrier, with an acq_rel atomic at
 // gpu scope (releasing the CTA's writes) and polls with acquire loads (so
 // the CTA reads the others' writes after the closing CTA barrier). The wait
-// is bounded: after 2^24 polls (well over a second) the CTA records a
-// timeout in bar->err; once the flag is set no CTA waits any more. Returns
-// false when the flag is set, and the caller then leaves the kernel, so a
-// fault cannot hang the GPU; the host turns the flag into CB_ERR_TIMEOUT.
+// is bounded: after max_polls polls (the default 2^24 is well over a
+// second) the CTA records a timeout in bar->err; with max_polls < 0 a CTA
+// that is not the last to arrive records it at once, without polling. Once
+// the flag is set no CTA waits any more. Returns false when the flag is set,
+// and the caller then leaves the kernel, so a fault cannot hang the GPU; the
+// host turns the flag into CB_ERR_TIMEOUT.
 __device__ __forceinline__ unsigned barrier_arrive(unsigned *count)
 {
     unsigned old;
@@ -438,7 +440,7 @@ __device__ __forceinline__ unsigned barrier_count(const unsigned *count)
 }
 
 __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks, unsigned &epoch,
-                                             unsigned leader = 0)
+                                             long long max_polls, unsigned leader = 0)
 {
     __shared__ int failed;
     __syncthreads();
@@ -449,13 +451,13 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks,
         if (!failed) {
             const unsigned target = epoch * nblocks;
             if (barrier_arrive(&bar->count) < target) {
-                unsigned long long polls = 0;
-                while (barrier_count(&bar->count) < target) {
+                long long polls = 0;
+                while (max_polls < 0 || barrier_count(&bar->count) < target) {
                     if (*verr) {
                         failed = 1;
                         break;
                     }
-                    if (++polls > (1ull << 24)) {
+                    if (++polls > max_polls) {
                         atomicExch(&bar->err, 1);
                         failed = 1;
                         break;
@@ -484,6 +486,7 @@ struct FactorArgs {
     T *look;     // 2 * (2 * 32 * 32 + 32): the next panel's factored diagonal block, Linv, 1/D (FP32)
     GridBarrier *bar;
     int dist;    // FP32: panel rows formed once per panel (wide bands) instead of per tile
+    long long max_polls;  // bound of each grid-barrier wait (grid_barrier)
 };
 
 // Tile t of the lower triangle of an nt x nt tile grid: t = ti (ti + 1) / 2 + tj.
@@ -674,7 +677,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                 a.wbuf[lane * m + r] = w;
                 if (off <= bw) a.band[(p + lane) * ld + off] = w * di[lane];
             }
-            if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+            if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
             if (blockIdx.x == 0)
                 for (int idx = tid; idx < NB * NB; idx += 256) {
                     const int j = idx / NB, i = idx % NB;
@@ -727,7 +730,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
                 }
                 __syncthreads();
             }
-            if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+            if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
             continue;
         }
         // ---- 2. trailing tiles ----
@@ -836,7 +839,7 @@ __global__ void __launch_bounds__(256) factor_f32_kernel(FactorArgs<float> a)
             if (tid < NB) lk[NB * NB + tid] = di[tid];
         }
         mprev = m;
-        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     }
 }
 
@@ -1152,7 +1155,7 @@ __global__ void __launch_bounds__(256) factor_f64_kernel(FactorArgs<double> a)
             a.wbuf[lane * m + r] = w;
             if (off <= bw) a.band[(p + lane) * ld + off] = w * di[lane];
         }
-        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
         // ---- 3. diagonal block out, trailing update ----
         if (blockIdx.x == 0) {
             for (int e = tid; e < NB * NB; e += 256) {
@@ -1185,7 +1188,7 @@ __global__ void __launch_bounds__(256) factor_f64_kernel(FactorArgs<double> a)
             }
             __syncthreads();
         }
-        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     }
 }
 
@@ -1203,6 +1206,7 @@ struct DirectArgs {
     double *out;
     T *y;
     GridBarrier *bar;
+    long long max_polls;
 };
 
 template <typename T>
@@ -1214,7 +1218,7 @@ __global__ void __launch_bounds__(256) solve_direct_kernel(DirectArgs<T> a)
     const long ld = a.ld, bw = a.bw, npad = a.npad;
     const long gthr = blockIdx.x * 256L + tid, nthr = gridDim.x * 256L;
     for (long g = gthr; g < npad; g += nthr) a.y[g] = g < a.n ? (T)a.rhs[g] : T(0);
-    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     // forward: y_p = L_pp^-1 y_p; y_r -= L(r, p..p+31) y_p for the rows below
     for (long p = 0; p < npad; p += NB) {
         long m = npad - p - NB;
@@ -1243,10 +1247,10 @@ __global__ void __launch_bounds__(256) solve_direct_kernel(DirectArgs<T> a)
             }
             a.y[p + NB + r] -= acc;
         }
-        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     }
     for (long g = gthr; g < npad; g += nthr) a.y[g] *= a.dinv[g];
-    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     // backward: x_p = L_pp^-T z_p; z_j -= sum_i L(p+i, j) x_i for j in [p-bw, p)
     for (long p = npad - NB; p >= 0; p -= NB) {
         if (warp == 0) {
@@ -1273,7 +1277,7 @@ __global__ void __launch_bounds__(256) solve_direct_kernel(DirectArgs<T> a)
                 if (base + i <= bw) acc += a.band[j * ld + base + i] * yp[i];
             a.y[j] -= acc;
         }
-        if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+        if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     }
     for (long g = gthr; g < a.n; g += nthr) a.out[g] = (double)a.y[g];
 }
@@ -1286,6 +1290,7 @@ struct SolveArgs {
     double *out;
     T *y, *v, *z;
     GridBarrier *bar;
+    long long max_polls;
 };
 
 template <typename T>
@@ -1385,14 +1390,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) solve_kernel(Solv
 
     // A: y = blockdiag(Linv) b (b converted to T into z first)
     for (long g = gthr; g < npad; g += nthr) a.z[g] = g < a.n ? (T)a.rhs[g] : T(0);
-    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, r = row % s;
         T acc = warp_row_dot(a.linv + i * s * s + r * s, a.z + i * s, r + 1, lane);
         if (lane == 0) a.y[row] = acc;
     }
     if (in_chain && regs && crow < w && nb > 1) row_to_regs(pre, a.pn + s * w + (s - w + crow) * w, w, lane);
-    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     // B, chain rows
     if (in_chain) {
         if (own_regs && crow < w && lane + 1 < nb) own = a.y[(lane + 1) * s + s - w + crow];
@@ -1415,13 +1420,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) solve_kernel(Solv
                     if (lane == 0) a.y[i * s + s - w + r] -= acc;
                 }
             }
-            if (!grid_barrier(cbar, nchain, ep_chain, kLeader)) {
+            if (!grid_barrier(cbar, nchain, ep_chain, a.max_polls, kLeader)) {
                 chain_failed();
                 return;
             }
         }
     }
-    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     // B, the other rows, and z = y / D
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, r = row % s;
@@ -1429,7 +1434,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) solve_kernel(Solv
         if (i >= 1 && r < s - w) acc = warp_row_dot(a.pn + i * s * w + r * w, a.y + i * s - w, w, lane);
         if (lane == 0) a.z[row] = (a.y[row] - acc) * a.dinv[row];
     }
-    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     // C: v = blockdiag(Linv^T) z, warp per row of the stored transpose
     for (long row = gwarp; row < npad; row += nwarps) {
         const long i = row / s, c = row % s;
@@ -1437,7 +1442,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) solve_kernel(Solv
         if (lane == 0) a.v[row] = acc;
     }
     if (in_chain && regs && crow < w && nb > 1) row_to_regs(pre, a.rn + (nb - 2) * s * w + crow * w, w, lane);
-    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     // D, chain rows
     if (in_chain) {
         if (own_regs && crow < w && lane + 1 < nb) own = a.v[lane * s + crow];
@@ -1460,13 +1465,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) solve_kernel(Solv
                     if (lane == 0) a.v[i * s + c] -= acc;
                 }
             }
-            if (!grid_barrier(cbar, nchain, ep_chain, kLeader)) {
+            if (!grid_barrier(cbar, nchain, ep_chain, a.max_polls, kLeader)) {
                 chain_failed();
                 return;
             }
         }
     }
-    if (!grid_barrier(a.bar, gridDim.x, ep)) return;
+    if (!grid_barrier(a.bar, gridDim.x, ep, a.max_polls)) return;
     // D, the other rows, and x = v
     for (long row = gwarp; row < a.n; row += nwarps) {
         const long i = row / s, c = row % s;
@@ -1502,7 +1507,7 @@ void factor_band(BandFactor &f, cudaStream_t st, long *launches)
     // trailing triangle has many more tiles than CTAs; otherwise per tile
     const int dist = (f.fp32 && ntiles > 2L * grid) ? 1 : 0;
     FactorArgs<T> a{band, f.ld, f.bw, npad, f.n, (T *)f.dinv, f.ssd, f.flags, (T *)f.work, (T *)f.stage,
-                    (T *)f.look, f.fbar, dist};
+                    (T *)f.look, f.fbar, dist, f.max_polls};
     if constexpr (sizeof(T) == 4) {
         if (f.cluster > 0) {
             ClusterArgs ca{a, f.cluster_slots, f.cluster_nwin};
@@ -1584,7 +1589,8 @@ template <typename T>
 void solve_direct_launch(const BandFactor &f, const double *rhs, double *x, void *work, GridBarrier *bar,
                          cudaStream_t st)
 {
-    DirectArgs<T> a{(const T *)f.band, (const T *)f.dinv, f.ld, f.bw, f.nblk * f.s, f.n, rhs, x, (T *)work, bar};
+    DirectArgs<T> a{(const T *)f.band, (const T *)f.dinv, f.ld, f.bw, f.nblk * f.s, f.n, rhs, x, (T *)work, bar,
+                    f.max_polls};
     CB_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), st));
     void *args[] = {&a};
     CB_CUDA(cudaLaunchCooperativeKernel((const void *)solve_direct_kernel<T>, dim3((unsigned)f.solve_grid),
@@ -1616,6 +1622,7 @@ void solve_launch(const BandFactor &f, const double *rhs, double *x, void *work,
     a.v = a.y + npad;
     a.z = a.v + npad;
     a.bar = bar;
+    a.max_polls = f.max_polls;
     CB_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(GridBarrier), st));  // grid and chain barriers
     void *args[] = {&a};
     CB_CUDA(cudaLaunchCooperativeKernel((const void *)solve_kernel<T>, dim3((unsigned)f.solve_grid), dim3(256),

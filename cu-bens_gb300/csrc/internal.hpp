@@ -116,6 +116,9 @@ struct DevTruss {
     double *n_c = nullptr, *n_i = nullptr;      // T: axial force ef[0]
 };
 
+// Polls after which a device-side wait gives up (well over a second).
+constexpr long long kDefaultWaitPolls = 1LL << 24;
+
 // Counters of the bounded grid barrier of the persistent solve kernel.
 struct GridBarrier {
     unsigned count;
@@ -154,6 +157,7 @@ struct BandFactor {
     size_t bytes = 0;            // device memory held
     cudaGraphExec_t factor_graph = nullptr;
     long factor_launches = 0;
+    long long max_polls = kDefaultWaitPolls;  // bound of every grid-barrier wait (< 0: give up at once)
 };
 
 // direct: the factor serves one solve (Newmark's full Newton): the solve

@@ -818,6 +818,13 @@ int cb_set_timing(cb_model *m, int on)
     return CB_OK;
 }
 
+int cb_set_wait_limit(cb_model *m, long long polls)
+{
+    if (!m) return CB_ERR_ARG;
+    m->bf.max_polls = polls == 0 ? cb::kDefaultWaitPolls : (polls < 0 ? -1 : polls);
+    return CB_OK;
+}
+
 // Access to a handle's factorisation for solve_noalloc.cu.
 cb::BandFactor *cb_internal_factor(cb_model *m, cudaStream_t *st, int *device)
 {

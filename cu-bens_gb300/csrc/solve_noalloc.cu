@@ -2,13 +2,14 @@
 // memory.
 //
 // Some callers of this library may not call cudaMalloc at the point where
-// they need a solve: code running while a CUDA graph is being captured,
-// code whose device memory is owned by another allocator or a fixed pool,
-// or a real-time loop whose memory footprint must not change after start-up.
-// cb_solve_noalloc serves them. It runs the same solve kernels as
-// cb_factor_solve, but its two work vectors live in the file-scope device
-// array below instead of in memory the handle allocated, and it allocates
-// nothing: no cudaMalloc, no cudaFree, no CUDA-graph instantiation.
+// they need a solve: a host application that reserved the GPU's memory up
+// front for its own allocator or a fixed pool (cudaMalloc then fails or
+// takes memory the pool counts on), or a real-time loop whose memory
+// footprint must not change after start-up. cb_solve_noalloc serves them.
+// It runs the same solve kernels as cb_factor_solve, but its three work
+// vectors and its grid-barrier counters live in the file-scope device array
+// below instead of in memory the handle allocated, and it allocates
+// nothing: no cudaMalloc, no cudaFree.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,7 +35,9 @@ void *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on `device`, looked up once per
 // device with that device current. In host code the symbol is only a
-// host-side stand-in, so kernels must be given this address instead.
+// host-side stand-in, so kernels must be given this address instead. The
+// address is kept for the life of the process: a cudaDeviceReset of the
+// device invalidates it, and the entry point is not to be used after one.
 cudaError_t scratch_address(int device, void **out)
 {
     std::lock_guard<std::mutex> lock(g_mutex);
@@ -78,9 +81,13 @@ extern "C" int cb_solve_noalloc(cb_model *m, const double *rhs, double *x)
     int prev = 0;
     cudaGetDevice(&prev);
     if (prev != device) cudaSetDevice(device);
+    // the grid and chain barriers sit at the start of the scratch; a wait that
+    // gave up sets the grid barrier's error flag (the chain barrier's too)
+    cb::GridBarrier bar[2] = {};
     try {
         cb::band_solve_with_work(*f, rhs, x, scratch, st);
-        e = cudaStreamSynchronize(st);
+        e = cudaMemcpyAsync(bar, scratch, sizeof bar, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     } catch (const std::exception &ex) {
         cb_internal_set_error(m, ex.what());
         e = cudaErrorUnknown;
@@ -89,6 +96,10 @@ extern "C" int cb_solve_noalloc(cb_model *m, const double *rhs, double *x)
     if (e != cudaSuccess) {
         if (e != cudaErrorUnknown) cb_internal_set_error(m, cudaGetErrorString(e));
         return CB_ERR_CUDA;
+    }
+    if (bar[0].err || bar[1].err) {
+        cb_internal_set_error(m, "cb_solve_noalloc: a grid barrier of the solve timed out; x is incomplete");
+        return CB_ERR_TIMEOUT;
     }
     return CB_OK;
 }

@@ -99,6 +99,7 @@ def load(path: Path | None = None):
     L.cb_get_timers.argtypes = [vp, C.POINTER(Timers)]
     L.cb_reset_timers.argtypes = [vp]
     L.cb_set_timing.argtypes = [vp, C.c_int]
+    L.cb_set_wait_limit.argtypes = [vp, C.c_longlong]
     L.cb_event_mark.argtypes = [vp, C.c_int]
     L.cb_event_elapsed.argtypes = [vp, C.c_int, C.c_int, dp]
     L.cb_profile_kernel.argtypes = [vp, C.c_int, C.c_int, dp, dp, dp]
@@ -425,3 +426,8 @@ class Model:
 
     def set_timing(self, on: bool):
         load().cb_set_timing(self.h, 1 if on else 0)
+
+    def set_wait_limit(self, polls: int):
+        """Bound of the persistent kernels' grid-barrier waits (0: the default;
+        < 0: a CTA that is not the last to arrive gives up at once)."""
+        self._check(load().cb_set_wait_limit(self.h, polls))

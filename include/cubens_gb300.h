@@ -254,6 +254,15 @@ int cb_reset_timers(cb_model *m);
 /* Enable/disable per-phase CUDA-event timing (adds event records). */
 int cb_set_timing(cb_model *m, int on);
 
+/* Bound of every device-side wait of the handle's persistent kernels (the
+ * grid barriers of the band LDL^T and of the solves): a CTA that has polled
+ * `polls` times without seeing the other CTAs arrive records a timeout and
+ * the kernel returns early; the call that launched it then returns
+ * CB_ERR_TIMEOUT and the handle stays usable. polls = 0 restores the
+ * default (2^24 polls, well over a second); polls < 0 makes a CTA that is
+ * not the last to arrive give up at once (for tests of the timeout path). */
+int cb_set_wait_limit(cb_model *m, long long polls);
+
 /* ---- measurement hooks ---- */
 
 /* Record CUDA event `slot` (0..7) on the handle's stream. */
@@ -329,20 +338,24 @@ int cb_factor_solve(cb_model *m, const double *rhs, double *v, double *ssd, int 
 /* Solve K x = rhs with the factorisation the handle currently holds (from
  * the last arc-length increment, or from cb_factor_solve), allocating no GPU
  * memory. No counterpart in the reference: it serves callers that cannot
- * call cudaMalloc where they need the solve (during CUDA-graph capture,
- * under another allocator's memory pool, or in a loop whose footprint is
- * fixed). rhs and x are device pointers to NEQ doubles.
+ * call cudaMalloc where they need the solve, such as a host application
+ * whose allocator or fixed pool already owns the GPU's memory, or a loop
+ * whose memory footprint must not change after start-up. rhs and x are
+ * device pointers to NEQ doubles.
  *
- * The solve's work vectors and its grid-barrier counters live in one
+ * The solve's three work vectors and its grid-barrier counters live in one
  * static device array of 3 x 524288 doubles plus 256 bytes (12 MiB), held by
  * every GPU that loads the library until the process exits; models with more
- * than 524288 padded equations get CB_ERR_LIMIT. The first call on a device looks up that array's device
- * address (cudaGetSymbolAddress with the device current); make that first
- * call before any stream capture. All calls share the array, which keeps the
- * last call's contents: each call clears the barrier counters before its
- * launch (every work element is written before it is read), and calls that
- * overlap on the GPU race with each other. The call is ordered on
- * the handle's stream and returns when the solve has finished. */
+ * than 524288 padded equations get CB_ERR_LIMIT. The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress with the device
+ * current) and keeps it; make that first call before any stream capture, and
+ * do not use the entry point after a cudaDeviceReset. All calls share the
+ * array, which keeps the last call's contents: each call clears the barrier
+ * counters before its launch (every work element is written before it is
+ * read), and calls that overlap on the GPU race with each other. The call is
+ * ordered on the handle's stream and returns when the solve has finished;
+ * CB_ERR_TIMEOUT when a grid-barrier wait of the solve gave up (x is then
+ * incomplete). */
 int cb_solve_noalloc(cb_model *m, const double *rhs, double *x);
 
 #ifdef __cplusplus
