@@ -107,6 +107,8 @@ struct cb_model {
     double nm_ddt = 1;      // time increment multiplier carried between steps (main.c:3452)
 
     cb_results_state *results = nullptr;  // open results*.txt files (results.cpp)
+    // convergence history of the latest increment: lam, |dd|/|d|, |lam q - f|/|lam q| per iteration
+    std::vector<double> iter_log;
 
     // timing
     bool timing = false;

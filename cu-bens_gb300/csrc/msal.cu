@@ -188,7 +188,8 @@ void upload_model(cb_model *m)
     }
     // Newmark and full Newton-Raphson refactor every iteration and solve once
     // per factorisation: direct substitution, no solve blocks
-    cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5 || h.alg == 1, m->opt.factor_kernel == 1);
+    cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5 || h.alg == 1 || m->opt.band_solve == 1,
+                   m->opt.factor_kernel == 1);
     m->bytes += m->bf.bytes;
     cb::build_tangent_map(h, m->bf.ld, tm);
     m->tmap_n = (long)tm.dst.size();
@@ -372,6 +373,15 @@ cb::MsalScalars &pull_scalars(cb_model *m)
     return *m->sc_h;
 }
 
+// One line of the convergence history from the test's reductions
+// (dots 0, 1, 2, 6: |dd|^2, |d|^2, |lam q - f|^2, |lam q|^2).
+void log_iteration(cb_model *m, const cb::MsalScalars &s)
+{
+    m->iter_log.push_back(s.lam_t);
+    m->iter_log.push_back(s.dots[1] > 0 ? std::sqrt(s.dots[0] / s.dots[1]) : 0.0);
+    m->iter_log.push_back(s.dots[6] > 0 ? std::sqrt(s.dots[2] / s.dots[6]) : 0.0);
+}
+
 double device_dot(cb_model *m, const double *a, const double *b, bool diff)
 {
     PhaseTimer t(m, &m->tm.ms_vector);
@@ -438,6 +448,7 @@ void msal_begin(cb_model *m, cb_step *out)
     HostModel &h = m->h;
     const long N = h.neq;
     cudaStream_t st = m->st;
+    m->iter_log.clear();
     reset_to_converged(m);
     CB_CUDA(cudaMemsetAsync(m->d, 0, N * sizeof(double), st));
     CB_CUDA(cudaMemsetAsync(m->dp, 0, N * sizeof(double), st));
@@ -479,6 +490,7 @@ void msal_begin(cb_model *m, cb_step *out)
         m->tm.launches += 4;
         cb::MsalScalars &s = pull_scalars(m);
         if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+        log_iteration(m, s);
         lpf = s.lam_t;
         convchk = s.convchk;
         itecnt++;
@@ -534,6 +546,7 @@ void msal_step(cb_model *m, cb_step *out)
         return;
     }
     int attempts = 0;
+    m->iter_log.clear();
     for (;;) {
         ++attempts;
         d2d(m->dt, m->d, N, st);
@@ -593,6 +606,7 @@ void msal_step(cb_model *m, cb_step *out)
             int status = s.quad_status;
             if (status == 0) {
                 if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+                log_iteration(m, s);
                 convchk = s.convchk;
                 if (convchk == 0) {
                     m->dnorm = std::sqrt(s.dots[5]);
@@ -815,6 +829,16 @@ int cb_set_timing(cb_model *m, int on)
 {
     if (!m) return CB_ERR_ARG;
     m->timing = on != 0;
+    return CB_OK;
+}
+
+int cb_get_iteration_log(const cb_model *m, double *out, int max_iters, int *n)
+{
+    if (!m || !n) return CB_ERR_ARG;
+    const int k = (int)(m->iter_log.size() / 3);
+    *n = k;
+    if (out && max_iters > 0)
+        std::memcpy(out, m->iter_log.data(), sizeof(double) * 3 * (size_t)std::min(k, max_iters));
     return CB_OK;
 }
 

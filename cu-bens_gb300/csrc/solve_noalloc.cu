@@ -69,7 +69,8 @@ extern "C" int cb_solve_noalloc(cb_model *m, const double *rhs, double *x)
     const size_t need = cb::band_work_bytes(*f);
     if (need > sizeof(g_solve_scratch)) {
         cb_internal_set_error(m, "cb_solve_noalloc: the model needs more solve scratch than the static "
-                                 "limit of 3 x 524288 doubles (padded equations > 524288)");
+                                 "limit of 3 x 524288 doubles (padded equations > 524288 with an FP64 "
+                                 "factor, > 1048576 with an FP32 factor)");
         return CB_ERR_LIMIT;
     }
     void *scratch = nullptr;

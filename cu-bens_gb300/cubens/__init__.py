@@ -40,7 +40,7 @@ class CubensError(RuntimeError):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("use_graphs", C.c_int),
                 ("solver", C.c_int), ("krylov_restart", C.c_int), ("krylov_maxit", C.c_int),
-                ("precond", C.c_int), ("factor_kernel", C.c_int)]
+                ("precond", C.c_int), ("factor_kernel", C.c_int), ("band_solve", C.c_int)]
 
 
 class Info(C.Structure):
@@ -100,6 +100,7 @@ def load(path: Path | None = None):
     L.cb_reset_timers.argtypes = [vp]
     L.cb_set_timing.argtypes = [vp, C.c_int]
     L.cb_set_wait_limit.argtypes = [vp, C.c_longlong]
+    L.cb_get_iteration_log.argtypes = [vp, dp, C.c_int, ip]
     L.cb_event_mark.argtypes = [vp, C.c_int]
     L.cb_event_elapsed.argtypes = [vp, C.c_int, C.c_int, dp]
     L.cb_profile_kernel.argtypes = [vp, C.c_int, C.c_int, dp, dp, dp]
@@ -172,7 +173,8 @@ class Model:
 
     def __init__(self, model_def: str, precision: int = FP64, device: int = 0, use_graphs: bool = True,
                  solver: int = SOLVER_BAND, restart: int = 0, maxit: int = 0,
-                 precond: int = PRECOND_BLOCK_JACOBI, rtol: float | None = None, factor_kernel: int = 0):
+                 precond: int = PRECOND_BLOCK_JACOBI, rtol: float | None = None, factor_kernel: int = 0,
+                 band_solve: int = 0):
         L = load()
         opt = Options()
         L.cb_default_options(C.byref(opt))
@@ -184,6 +186,7 @@ class Model:
         opt.krylov_maxit = maxit
         opt.precond = precond
         opt.factor_kernel = factor_kernel
+        opt.band_solve = band_solve
         h = C.c_void_p()
         raw = model_def.encode()
         rc = L.cb_model_create(raw, len(raw), C.byref(opt), C.byref(h))
@@ -431,3 +434,13 @@ class Model:
         """Bound of the persistent kernels' grid-barrier waits (0: the default;
         < 0: a CTA that is not the last to arrive gives up at once)."""
         self._check(load().cb_set_wait_limit(self.h, polls))
+
+    def iteration_log(self):
+        """Convergence history of the latest increment: rows (lam, |dd|/|d|,
+        |lam q - f|/|lam q|), one per iteration."""
+        L = load()
+        n = C.c_int()
+        self._check(L.cb_get_iteration_log(self.h, None, 0, C.byref(n)))
+        out = np.zeros((max(1, n.value), 3))
+        self._check(L.cb_get_iteration_log(self.h, _d(out), n.value, C.byref(n)))
+        return out[:n.value]

@@ -80,6 +80,10 @@ typedef struct {
                             thread-block-cluster factor where the band's window fits a cluster's
                             distributed shared memory (measured slower on GB300: the grid factor
                             stays the default) */
+    int band_solve;      /* band LDL^T solves: 0 (default) block-bidiagonal solve with the
+                            factor's block inverses for arc-length and modified Newton-Raphson
+                            models, direct substitution for the others; 1 direct substitution
+                            with the band for every model (no block inverses are formed) */
 } cb_options;
 
 typedef struct {
@@ -263,6 +267,13 @@ int cb_set_timing(cb_model *m, int on);
  * not the last to arrive give up at once (for tests of the timeout path). */
 int cb_set_wait_limit(cb_model *m, long long polls);
 
+/* Convergence history of the latest first increment or arc-length increment:
+ * for each iteration (attempts of cut increments included, in order) three
+ * doubles, the load factor, |dd| / |d| and the FP64 equilibrium residual
+ * |lam q - f| / |lam q| after the iteration. Copies at most max_iters
+ * iterations into out (may be NULL) and the number recorded into *n. */
+int cb_get_iteration_log(const cb_model *m, double *out, int max_iters, int *n);
+
 /* ---- measurement hooks ---- */
 
 /* Record CUDA event `slot` (0..7) on the handle's stream. */
@@ -345,8 +356,9 @@ int cb_factor_solve(cb_model *m, const double *rhs, double *v, double *ssd, int 
  *
  * The solve's three work vectors and its grid-barrier counters live in one
  * static device array of 3 x 524288 doubles plus 256 bytes (12 MiB), held by
- * every GPU that loads the library until the process exits; models with more
- * than 524288 padded equations get CB_ERR_LIMIT. The first call on a device
+ * every GPU that loads the library until the process exits; FP64 factors of
+ * more than 524288 padded equations (FP32 factors of more than 1048576) get
+ * CB_ERR_LIMIT. The first call on a device
  * looks up that array's device address (cudaGetSymbolAddress with the device
  * current) and keeps it; make that first call before any stream capture, and
  * do not use the entry point after a cudaDeviceReset. All calls share the

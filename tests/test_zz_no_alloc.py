@@ -85,10 +85,11 @@ def test_noalloc_reports_a_timed_out_wait_and_recovers(golden_dir):
 
 
 def test_noalloc_rejects_models_beyond_its_limit():
-    """541,800 equations: more than the 524,288 the static array holds."""
+    """541,800 equations with an FP64 factor: more than the 524,288 padded
+    equations whose three FP64 work vectors the static array holds."""
     torch = pytest.importorskip("torch")
     spec = models.cylindrical_panel(300)
-    m = cubens.Model(spec.text, precision=cubens.MIXED)
+    m = cubens.Model(spec.text, precision=cubens.FP64, band_solve=1)
     assert m.neq > 524288
     lib = cubens.load()
     rhs = torch.zeros(m.neq, dtype=torch.float64, device="cuda")
