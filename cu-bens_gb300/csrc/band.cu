@@ -39,6 +39,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "grid_barrier.cuh"
 #include "internal.hpp"
 
 namespace cb {
@@ -412,63 +413,6 @@ __global__ void __launch_bounds__(256) rn_kernel(const T *band, long ld, long bw
 // Persistent solve
 // -------------------------------------------------------------------------
 
-// Grid barrier for a cooperative launch. bar->count is zeroed before the
-// launch and only grows: the k-th barrier of a kernel (epoch, counted by
-// every thread) is passed once count reaches k * nblocks, so a CTA arrives
-// with one atomic and nothing is reset on the critical path. The leader
-// thread arrives for its CTA after a CTA barrier, with an acq_rel atomic at
-// gpu scope (releasing the CTA's writes) and polls with acquire loads (so
-// the CTA reads the others' writes after the closing CTA barrier). The wait
-// is bounded: after max_polls polls (the default 2^24 is well over a
-// second) the CTA records a timeout in bar->err; with max_polls < 0 a CTA
-// that is not the last to arrive records it at once, without polling. Once
-// the flag is set no CTA waits any more. Returns false when the flag is set,
-// and the caller then leaves the kernel, so a fault cannot hang the GPU; the
-// host turns the flag into CB_ERR_TIMEOUT.
-__device__ __forceinline__ unsigned barrier_arrive(unsigned *count)
-{
-    unsigned old;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;\n" : "=r"(old) : "l"(count) : "memory");
-    return old + 1u;
-}
-
-__device__ __forceinline__ unsigned barrier_count(const unsigned *count)
-{
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(count) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ bool grid_barrier(GridBarrier *bar, unsigned nblocks, unsigned &epoch,
-                                             long long max_polls, unsigned leader = 0)
-{
-    __shared__ int failed;
-    __syncthreads();
-    ++epoch;
-    if (threadIdx.x == leader) {
-        volatile int *verr = &bar->err;
-        failed = *verr;
-        if (!failed) {
-            const unsigned target = epoch * nblocks;
-            if (barrier_arrive(&bar->count) < target) {
-                long long polls = 0;
-                while (max_polls < 0 || barrier_count(&bar->count) < target) {
-                    if (*verr) {
-                        failed = 1;
-                        break;
-                    }
-                    if (++polls > max_polls) {
-                        atomicExch(&bar->err, 1);
-                        failed = 1;
-                        break;
-                    }
-                }
-            }
-        }
-    }
-    __syncthreads();
-    return !failed;
-}
 
 // -------------------------------------------------------------------------
 // Persistent factorisation: one cooperative launch for the whole band
@@ -1760,6 +1704,7 @@ void band_residual64(const double *band64, long ld, long bw, long n, const doubl
 
 void band_use_factored(BandFactor &f, cudaStream_t st)
 {
+    if (f.dw) throw std::runtime_error("a double-word band is factored by band_factor only");
     const long npad = f.nblk * f.s;
     const unsigned g = (unsigned)((npad + 255) / 256);
     long dummy = 0;
@@ -1789,19 +1734,23 @@ void band_solve_with_work(const BandFactor &f, const double *rhs, double *x, voi
     // the grid-barrier counters sit in front of the work vectors
     GridBarrier *bar = (GridBarrier *)work;
     void *vecs = (unsigned char *)work + 256;
-    if (f.fp32) solve_launch<float>(f, rhs, x, vecs, bar, st);
+    if (f.dw) band_dw_solve(f, rhs, x, vecs, bar, st);
+    else if (f.fp32) solve_launch<float>(f, rhs, x, vecs, bar, st);
     else solve_launch<double>(f, rhs, x, vecs, bar, st);
     CB_CUDA(cudaGetLastError());
 }
 
 void band_profile_launch(BandFactor &f, int which, cudaStream_t st)
 {
-    if (f.fp32) profile_impl<float>(f, which, st);
+    long dummy = 0;
+    if (f.dw) {
+        if (which == 3) band_dw_factor(f, st, &dummy);
+    } else if (f.fp32) profile_impl<float>(f, which, st);
     else profile_impl<double>(f, which, st);
     CB_CUDA(cudaGetLastError());
 }
 
-void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use_cluster)
+void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use_cluster, long direct_block)
 {
     f.n = n;
     f.bw = std::max(1L, bw);
@@ -1817,7 +1766,7 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use
     // needs no blocks: the matrix is padded to a multiple of 32 only.
     long s = f.w;
     if (direct) {
-        s = NB;
+        s = direct_block > 0 ? direct_block : NB;
     } else if (fp32) {
         const double budget = 4.0e9;
         long cap = (long)(budget / ((double)es * (double)std::max(1L, n)));
@@ -1865,6 +1814,13 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use
     f.bytes = es * ((size_t)f.ld * npad + npad + blocks * (2 * f.s + 2 * f.w) + work);
 }
 
+void band_alloc_dw(BandFactor &f, long n, long bw)
+{
+    band_alloc(f, n, bw, false, true, false, band_dw_block());
+    f.dw = true;
+    band_dw_alloc(f);
+}
+
 void band_free(BandFactor &f)
 {
     if (f.factor_graph) cudaGraphExecDestroy(f.factor_graph);
@@ -1878,6 +1834,10 @@ void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches)
 {
     long dummy = 0;
     long *cnt = launches ? launches : &dummy;
+    if (f.dw) {
+        band_dw_factor(f, st, cnt);
+        return;
+    }
     if (f.fp32) factor_band<float>(f, st, cnt);
     else factor_band<double>(f, st, cnt);
     if (f.direct) return;
@@ -1903,7 +1863,8 @@ void band_factor(BandFactor &f, cudaStream_t st, bool use_graph, long *launches)
 
 void band_solve(BandFactor &f, const double *rhs, double *x, cudaStream_t st, bool /*use_graph*/, long *launches)
 {
-    if (f.fp32) solve_launch<float>(f, rhs, x, f.work, f.bar, st);
+    if (f.dw) band_dw_solve(f, rhs, x, f.work, f.bar, st);
+    else if (f.fp32) solve_launch<float>(f, rhs, x, f.work, f.bar, st);
     else solve_launch<double>(f, rhs, x, f.work, f.bar, st);
     CB_CUDA(cudaGetLastError());
     if (launches) *launches += 1;

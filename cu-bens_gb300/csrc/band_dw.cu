@@ -1,0 +1,615 @@
+// Band LDL^T and its solves in double-word ("double-float") arithmetic.
+//
+// The same factorisation as band.cu (skyfact's result in the reference's
+// equation order, solve.c:539-653: pivots ssd and the indefiniteness flag
+// det), for bands whose conditioning an FP32 factor cannot carry and whose
+// size makes native FP64 slow on GB300: the 1.58M-equation DKT panel (band
+// 3,083) takes 7.6e12 multiply-adds per factorisation. Every entry of the
+// band is a pair of floats (dw.cuh, about 48 significant bits) and all
+// arithmetic runs on the FP32 pipe.
+//
+// Factor: one persistent cooperative kernel, right-looking over 32-column
+// panels, two bounded grid barriers per panel:
+//   1. the panel's factored diagonal block (L below, D on the diagonal) and
+//      1/D come from the look-ahead buffer (CTA 0 factored the block during
+//      the previous panel; for the first panel every CTA factors it);
+//   2. one warp per panel row r forms W_r (W_r L_pp^T = A_r, by
+//      substitution, so W_r = L_r D) and L_r = W_r D^-1 into the band, and W
+//      and L into a k-major buffer;
+//   -- grid barrier --
+//   3. the trailing lower triangle of the band window in 64 x 64 tiles,
+//      A_ij -= sum_k W_ik L_jk, each thread a 4 x 4 block of accumulators;
+//      CTA 0 takes only tile (0,0), which holds the next panel's diagonal
+//      block, and factors that block right after its update while the other
+//      CTAs work through the rest of the triangle;
+//   -- grid barrier --
+// Then inv_block_kernel forms, for every 128-row block of the matrix, the
+// inverse X_i of its unit-lower diagonal block: its ten lower 32 x 32 tiles,
+// once row-major and once column-major.
+//
+// Solve: one cooperative kernel over 128-row blocks, forward and backward,
+// one grid barrier per block each way. Every CTA forms the block's solution
+// y_i = X_i t_i (or x_i = X_i^T u_i) from the block inverse in shared memory
+// and applies it to 32 of the band's rows (columns) below (above) the
+// block. Nothing a step reads besides the solution's 128 values depends on
+// the solution: each CTA copies the next block's inverse into shared memory
+// (cp.async) and each thread the next step's band values into registers
+// before the barrier that ends a step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <stdexcept>
+#include <string>
+
+#include "dw.cuh"
+#include "grid_barrier.cuh"
+#include "internal.hpp"
+
+#define CB_CUDA_DW(x)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (x);                                                              \
+        if (e_ != cudaSuccess)                                                             \
+            throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + \
+                                     " at " __FILE__ ":" + std::to_string(__LINE__));      \
+    } while (0)
+
+namespace cb {
+
+namespace {
+
+constexpr int NB = 32;        // panel width of the factor, tile size of the block inverses
+constexpr int TW = 64;        // tile of the factor's trailing update (4 x 4 accumulators per thread)
+constexpr int SB = 128;       // block size of the solve
+constexpr int kTiles = (SB / NB) * (SB / NB + 1) / 2;  // lower 32 x 32 tiles of a block
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ dw dw_zero() { return dw{0.0f, 0.0f}; }
+
+__device__ __forceinline__ dw shfl_dw(dw v, int src)
+{
+    return dw{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+struct DwFactorArgs {
+    dw *band;       // ld * npad, L(i, j) at band[j * ld + (i - j)]
+    long ld, bw, npad, n;
+    dw *dinv;       // npad: 1/D
+    double *ssd;    // n pivots
+    int *flags;     // [0] a pivot <= 0, [1] a zero pivot
+    dw *wl;         // 2 * 32 * bw: W (row r of column k at k * m + r), then L at offset 32 * bw
+    dw *look;       // the next panel's factored block (32 x 32) and 1/D (32)
+    GridBarrier *bar;
+    long long max_polls;
+};
+
+// LDL^T of the 32 x 32 block in A (lower triangle) by all threads of the CTA,
+// one CTA barrier per column: every thread forms 1/D_k itself from the final
+// pivot, the update uses the unscaled column (W = L D), and the columns are
+// scaled by 1/D at the end. On return L below the diagonal, D on it, di = 1/D.
+__device__ void ldlt32_dw(dw (*A)[NB + 1], dw *di)
+{
+    const int tid = threadIdx.x;
+    for (int k = 0; k < NB; ++k) {
+        const dw dk = dw_recip(A[k][k]);
+        for (int e = tid; e < NB * NB; e += kThreads) {
+            const int j = e / NB, i = e % NB;
+            if (j > k && i >= j) A[i][j] = dw_sub(A[i][j], dw_mul(dw_mul(A[i][k], dk), A[j][k]));
+        }
+        if (tid == 0) di[k] = dk;
+        __syncthreads();
+    }
+    for (int e = tid; e < NB * NB; e += kThreads) {
+        const int j = e / NB, i = e % NB;
+        if (i > j) A[i][j] = dw_mul(A[i][j], di[j]);
+    }
+    __syncthreads();
+}
+
+// The factored block of panel p into the band, 1/D, the FP64 pivots and the flags.
+__device__ void record_block(const DwFactorArgs &a, long p, const dw (*A)[NB + 1], const dw *di)
+{
+    const int tid = threadIdx.x;
+    for (int e = tid; e < NB * NB; e += kThreads) {
+        const int j = e / NB, i = e % NB;
+        if (i >= j && i - j <= a.bw) a.band[(p + j) * a.ld + (i - j)] = A[i][j];
+    }
+    if (tid < NB) {
+        a.dinv[p + tid] = di[tid];
+        const long g = p + tid;
+        if (g < a.n) {
+            const double d = dw_to_double(A[tid][tid]);
+            a.ssd[g] = d;
+            if (!(d > 0.0)) atomicOr(&a.flags[0], 1);
+            if (d == 0.0) atomicOr(&a.flags[1], 1);
+        }
+    }
+}
+
+__device__ void load_block(const DwFactorArgs &a, long p, dw (*A)[NB + 1])
+{
+    for (int e = threadIdx.x; e < NB * NB; e += kThreads) {
+        const int j = e / NB, i = e % NB;
+        A[i][j] = (i >= j && i - j <= a.bw) ? a.band[(p + j) * a.ld + (i - j)] : dw_zero();
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads) factor_dw_kernel(DwFactorArgs a)
+{
+    unsigned ep = 0;  // grid barriers passed
+    __shared__ dw A[NB][NB + 1];   // factored diagonal block of the panel
+    __shared__ dw di[NB];          // 1/D
+    __shared__ dw Wt[NB][TW];      // W of a tile's rows, k-major
+    __shared__ dw Lt[NB][TW];      // L of a tile's columns, k-major
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    const long ld = a.ld, bw = a.bw;
+    const unsigned G = gridDim.x;
+    for (long p = 0; p < a.npad; p += NB) {
+        long m = a.npad - p - NB;
+        if (m > bw) m = bw;
+        if (m < 0) m = 0;
+        // ---- 1. the factored diagonal block ----
+        if (p == 0) {
+            load_block(a, 0, A);
+            ldlt32_dw(A, di);
+            if (blockIdx.x == 0) record_block(a, 0, A, di);
+        } else {
+            for (int e = tid; e < NB * NB; e += kThreads) A[e / NB][e % NB] = a.look[e];
+            if (tid < NB) di[tid] = a.look[NB * NB + tid];
+        }
+        __syncthreads();
+        // ---- 2. panel rows by substitution (one warp per row) ----
+        dw *wbuf = a.wl, *lbuf = a.wl + (long)NB * bw;
+        for (long r = blockIdx.x * 8L + warp; r < m; r += G * 8L) {
+            const long off = NB + r - lane;
+            dw w = off <= bw ? a.band[(p + lane) * ld + off] : dw_zero();
+            for (int k = 0; k < NB - 1; ++k) {
+                const dw wk = shfl_dw(w, k);
+                if (lane > k) w = dw_sub(w, dw_mul(wk, A[lane][k]));
+            }
+            const dw l = dw_mul(w, di[lane]);
+            wbuf[lane * m + r] = w;
+            lbuf[lane * m + r] = l;
+            if (off <= bw) a.band[(p + lane) * ld + off] = l;
+        }
+        if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
+        // ---- 3. trailing triangle; CTA 0: tile (0,0), then the next block ----
+        const long nt = (m + TW - 1) / TW;
+        const long ntiles = nt * (nt + 1) / 2;
+        const int tx = tid % 16, ty = tid / 16;
+        auto tile = [&](long t) {
+            // tile (ti, tj) of the lower triangle, t = ti (ti + 1) / 2 + tj
+            long ti = (long)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+            while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+            while (ti * (ti + 1) / 2 > t) --ti;
+            const long tj = t - ti * (ti + 1) / 2;
+            const long r0 = ti * TW, j0 = tj * TW;
+            for (int e = tid; e < NB * TW; e += kThreads) {
+                const int k = e / TW, q = e % TW;
+                Wt[k][q] = r0 + q < m ? wbuf[k * m + r0 + q] : dw_zero();
+                Lt[k][q] = j0 + q < m ? lbuf[k * m + j0 + q] : dw_zero();
+            }
+            // the band values the tile updates, loaded ahead of the products:
+            // rows r0 + tx + 16 i, columns j0 + ty + 16 j
+            dw old[4][4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const long rr = r0 + tx + 16 * i, jj = j0 + ty + 16 * j;
+                    old[i][j] = (rr < m && jj <= rr) ? a.band[(p + NB + jj) * ld + (rr - jj)] : dw_zero();
+                }
+            __syncthreads();
+            dw_acc acc[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc_zero(acc[i][j]);
+#pragma unroll 2
+            for (int k = 0; k < NB; ++k) {
+                dw w[4], l[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    w[i] = Wt[k][tx + 16 * i];
+                    l[i] = Lt[k][ty + 16 * i];
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc_fma(acc[i][j], w[i], l[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const long rr = r0 + tx + 16 * i, jj = j0 + ty + 16 * j;
+                    if (rr < m && jj <= rr)
+                        a.band[(p + NB + jj) * ld + (rr - jj)] = dw_sub(old[i][j], acc_value(acc[i][j]));
+                }
+            __syncthreads();
+        };
+        if (blockIdx.x == 0) {
+            // tile (0,0) holds the next panel's diagonal block (rows and columns
+            // 0..31 of the window); band rows below the window, for a band
+            // narrower than a panel, take no update from this panel
+            if (ntiles > 0) tile(0);
+            if (p + NB < a.npad) {
+                const long pn = p + NB;
+                load_block(a, pn, A);
+                ldlt32_dw(A, di);
+                record_block(a, pn, A, di);
+                for (int e = tid; e < NB * NB; e += kThreads) a.look[e] = A[e / NB][e % NB];
+                if (tid < NB) a.look[NB * NB + tid] = di[tid];
+            }
+            if (G == 1)
+                for (long t = 1; t < ntiles; ++t) tile(t);
+        } else {
+            for (long t = blockIdx.x; t < ntiles; t += G - 1) tile(t);
+        }
+        if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
+    }
+}
+
+// Lower tile (I, J), J <= I, of a block inverse: index I (I + 1) / 2 + J.
+__host__ __device__ constexpr int tile_index(int I, int J) { return I * (I + 1) / 2 + J; }
+
+// X_i = inverse of the unit-lower diagonal block i (rows and columns
+// 128 i .. 128 i + 127) of the factored band, one CTA per block, by 32 x 32
+// tiles: X_II = T_I (the inverse of tile L_II, by forward elimination on the
+// identity), X_IJ = -T_I sum_{K=J}^{I-1} L_IK X_KJ. Tile (I, J) is written
+// row-major to xr and column-major to xc (kTiles * 1024 pairs per block).
+__global__ void __launch_bounds__(kThreads) inv_block_kernel(const dw *band, long ld, long bw, dw *xr, dw *xc)
+{
+    __shared__ dw T[NB][NB + 1];  // T_I
+    __shared__ dw L[NB][NB + 1];  // a tile L_IK
+    __shared__ dw X[NB][NB + 1];  // a tile X_KJ, then the tile sum S
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    const long p0 = (long)blockIdx.x * SB;
+    dw *Xr = xr + (long)blockIdx.x * kTiles * NB * NB, *Xc = xc + (long)blockIdx.x * kTiles * NB * NB;
+    auto lval = [&](long r, long c) -> dw {  // L(p0 + r, p0 + c), r > c; 0 outside the band
+        const long off = r - c;
+        return off <= bw ? band[(p0 + c) * ld + off] : dw_zero();
+    };
+    auto store = [&](int I, int J, const dw v[2][2]) {
+        dw *tr = Xr + tile_index(I, J) * NB * NB, *tc = Xc + tile_index(I, J) * NB * NB;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int r = tx + 16 * i, c = ty + 16 * j;
+                tr[r * NB + c] = v[i][j];
+                tc[c * NB + r] = v[i][j];
+            }
+    };
+    for (int I = 0; I < SB / NB; ++I) {
+        // T = L_II^-1: row k of T is final after step k
+        for (int e = tid; e < NB * NB; e += kThreads) {
+            const int i = e / NB, j = e % NB;
+            T[i][j] = i == j ? dw{1.0f, 0.0f} : dw_zero();
+            L[i][j] = i > j ? lval(NB * I + i, NB * I + j) : dw_zero();
+        }
+        __syncthreads();
+        for (int k = 0; k < NB - 1; ++k) {
+            for (int e = tid; e < NB * NB; e += kThreads) {
+                const int j = e / NB, i = e % NB;
+                if (i > k && j <= k) T[i][j] = dw_sub(T[i][j], dw_mul(L[i][k], T[k][j]));
+            }
+            __syncthreads();
+        }
+        {
+            dw v[2][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) v[i][j] = T[tx + 16 * i][ty + 16 * j];
+            store(I, I, v);
+        }
+        for (int J = 0; J < I; ++J) {
+            dw_acc acc[2][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) acc_zero(acc[i][j]);
+            for (int K = J; K < I; ++K) {
+                __syncthreads();
+                const dw *xk = Xr + tile_index(K, J) * NB * NB;
+                for (int e = tid; e < NB * NB; e += kThreads) {
+                    const int i = e / NB, j = e % NB;
+                    L[i][j] = lval(NB * I + i, NB * K + j);
+                    X[i][j] = xk[e];
+                }
+                __syncthreads();
+#pragma unroll 4
+                for (int k = 0; k < NB; ++k) {
+                    const dw l0 = L[tx][k], l1 = L[tx + 16][k], x0 = X[k][ty], x1 = X[k][ty + 16];
+                    acc_fma(acc[0][0], l0, x0);
+                    acc_fma(acc[0][1], l0, x1);
+                    acc_fma(acc[1][0], l1, x0);
+                    acc_fma(acc[1][1], l1, x1);
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) X[tx + 16 * i][ty + 16 * j] = acc_value(acc[i][j]);
+            __syncthreads();
+            dw v[2][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    dw_acc s;
+                    acc_zero(s);
+                    const int r = tx + 16 * i, c = ty + 16 * j;
+                    for (int k = 0; k <= r; ++k) acc_fma(s, T[r][k], X[k][c]);
+                    v[i][j] = dw_neg(acc_value(s));
+                }
+            store(I, J, v);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+struct DwSolveArgs {
+    const dw *band, *dinv, *xr, *xc;
+    long ld, bw, npad, n;
+    const double *rhs;
+    double *out;
+    dw *t, *y;  // npad each: the right-hand side being reduced, the solution
+    GridBarrier *bar;
+    long long max_polls;
+};
+
+constexpr int kCols = SB / 8;  // columns (rows) of the block per warp in a step's update
+constexpr int kBlockElems = kTiles * NB * NB;
+// dynamic shared memory of the solve: two block inverses
+constexpr size_t kSolveSmem = 2 * sizeof(dw) * kBlockElems;
+
+// CTA b of the solve applies a block's solution to rows (columns) 32 b ..
+// 32 b + 31 of the block's reach: thread (lane, warp) sums the 16 products
+// of its row (column) with warp's 16 entries of the block.
+__global__ void __launch_bounds__(kThreads, 1) solve_dw_kernel(DwSolveArgs a)
+{
+    extern __shared__ __align__(16) unsigned char dyn[];
+    dw *xs = (dw *)dyn;                // [2][kBlockElems]
+    __shared__ dw ts[SB], ys[SB];      // the block's right-hand side and solution
+    __shared__ dw part[2][SB];         // halves of the block product
+    __shared__ dw red[8][NB + 1];      // per-warp partial sums of the update
+    unsigned ep = 0;
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    const long ld = a.ld, bw = a.bw, npad = a.npad;
+    const long gthr = blockIdx.x * (long)kThreads + tid, nthr = gridDim.x * (long)kThreads;
+    const unsigned G = gridDim.x;
+    const long nb = npad / SB;
+    const bool active = NB * (long)blockIdx.x < bw;  // this CTA's rows (columns) are in a block's reach
+    auto fetch_inv = [&](const dw *src, long blk, int buf) {
+        const char *g = (const char *)(src + blk * kBlockElems);
+        char *sm = (char *)(xs + buf * kBlockElems);
+        for (int e = tid; e < kBlockElems * (int)sizeof(dw) / 16; e += kThreads) cp_async16(sm + 16 * e, g + 16 * e);
+        cp_async_commit();
+    };
+    dw v[kCols];  // this thread's band values for a step
+    // forward: row r = p + 128 + 32 b + lane takes L(r, p + 16 warp + k), k < 16
+    auto load_row = [&](long p) {
+        const long r = p + SB + NB * (long)blockIdx.x + lane;
+#pragma unroll
+        for (int k = 0; k < kCols; ++k) {
+            const long col = p + kCols * warp + k, off = r - col;
+            v[k] = (active && r < npad && off <= bw) ? a.band[col * ld + off] : dw_zero();
+        }
+    };
+    // backward: column c = p - 32 (b + 1) + lane takes L(p + 16 warp + i, c), i < 16
+    auto load_col = [&](long p) {
+        const long c = p - NB * ((long)blockIdx.x + 1) + lane;
+#pragma unroll
+        for (int i = 0; i < kCols; ++i) {
+            const long off = p + kCols * warp + i - c;
+            v[i] = (active && c >= 0 && off <= bw) ? a.band[c * ld + off] : dw_zero();
+        }
+    };
+    // the products of this thread, summed over the warps into row (column) g
+    auto apply = [&](long g, bool valid) {
+        dw_acc acc;
+        acc_zero(acc);
+#pragma unroll
+        for (int k = 0; k < kCols; ++k) acc_fma(acc, v[k], ys[kCols * warp + k]);
+        red[warp][lane] = acc_value(acc);
+        __syncthreads();
+        if (warp == 0 && valid) {
+            dw s = red[0][lane];
+            for (int w = 1; w < 8; ++w) s = dw_add(s, red[w][lane]);
+            a.t[g] = dw_sub(a.t[g], s);
+        }
+    };
+    const int h = tid / SB, r = tid % SB;  // half of the block product, row (column) of the block
+    for (long g = gthr; g < npad; g += nthr) a.t[g] = g < a.n ? dw_from_double(a.rhs[g]) : dw_zero();
+    fetch_inv(a.xc, 0, 0);
+    load_row(0);
+    if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
+    for (long i = 0; i < nb; ++i) {
+        const long p = i * SB;
+        const int buf = (int)(i & 1);
+        if (tid < SB) ts[tid] = a.t[p + tid];
+        cp_async_wait_all();
+        __syncthreads();
+        // y_i = X_i t_i: thread (h, r) sums k in [64 h, 64 h + 64), k <= r
+        {
+            const dw *xb = xs + buf * kBlockElems;
+            dw_acc acc;
+            acc_zero(acc);
+            const int I = r / NB, rr = r % NB;
+            for (int J = 2 * h; J < 2 * h + 2 && J <= I; ++J) {
+                const dw *tile = xb + tile_index(I, J) * NB * NB + rr;  // column-major: (rr, kk) at kk * 32 + rr
+                const int kend = J < I ? NB : rr + 1;
+                for (int kk = 0; kk < kend; ++kk) acc_fma(acc, tile[kk * NB], ts[NB * J + kk]);
+            }
+            part[h][r] = acc_value(acc);
+        }
+        __syncthreads();
+        if (tid < SB) {
+            const dw yv = dw_add(part[0][tid], part[1][tid]);
+            ys[tid] = yv;
+            if (blockIdx.x == 0) a.y[p + tid] = yv;
+        }
+        __syncthreads();
+        if (i + 1 < nb) fetch_inv(a.xc, i + 1, buf ^ 1);
+        const long row = p + SB + NB * (long)blockIdx.x + lane;
+        apply(row, active && row < npad);
+        if (i + 1 < nb) load_row(p + SB);
+        if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
+    }
+    // z = D^-1 y into t (the backward right-hand side)
+    for (long g = gthr; g < npad; g += nthr) a.t[g] = dw_mul(a.y[g], a.dinv[g]);
+    fetch_inv(a.xr, nb - 1, (int)((nb - 1) & 1));
+    load_col(npad - SB);
+    if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
+    for (long i = nb - 1; i >= 0; --i) {
+        const long p = i * SB;
+        const int buf = (int)(i & 1);
+        if (tid < SB) ts[tid] = a.t[p + tid];
+        cp_async_wait_all();
+        __syncthreads();
+        // x_i = X_i^T u_i: thread (h, c = r) sums rows k in [64 h, 64 h + 64), k >= c
+        {
+            const dw *xb = xs + buf * kBlockElems;
+            dw_acc acc;
+            acc_zero(acc);
+            const int J = r / NB, cc = r % NB;
+            for (int I = 2 * h; I < 2 * h + 2; ++I) {
+                if (I < J) continue;
+                const dw *tile = xb + tile_index(I, J) * NB * NB + cc;  // row-major: (kk, cc) at kk * 32 + cc
+                const int kbeg = I > J ? 0 : cc;
+                for (int kk = kbeg; kk < NB; ++kk) acc_fma(acc, tile[kk * NB], ts[NB * I + kk]);
+            }
+            part[h][r] = acc_value(acc);
+        }
+        __syncthreads();
+        if (tid < SB) {
+            const dw xv = dw_add(part[0][tid], part[1][tid]);
+            ys[tid] = xv;
+            if (blockIdx.x == 0) a.y[p + tid] = xv;
+        }
+        __syncthreads();
+        if (i > 0) fetch_inv(a.xr, i - 1, buf ^ 1);
+        const long c = p - NB * ((long)blockIdx.x + 1) + lane;
+        apply(c, active && c >= 0);
+        if (i > 0) load_col(p - SB);
+        if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
+    }
+    for (long g = gthr; g < a.n; g += nthr) a.out[g] = dw_to_double(a.y[g]);
+}
+
+// band[dst[i]] = the FP64 sum of slot i's contributions, split into a pair
+__global__ void gather_band_dw_kernel(const int *__restrict__ ptr, const int *__restrict__ src,
+                                      const int64_t *__restrict__ dst, const double *__restrict__ in,
+                                      dw *__restrict__ band, long n)
+{
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) s += in[src[k]];
+    band[dst[i]] = dw_from_double(s);
+}
+
+__global__ void pad_identity_dw_kernel(dw *band, long ld, long n, long npad)
+{
+    const long g = n + blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (g < npad) band[g * ld] = dw{1.0f, 0.0f};
+}
+
+template <typename K>
+int coop_grid(K kernel, int per_sm_cap, size_t dyn_smem = 0)
+{
+    int dev = 0, sms = 0, per = 0;
+    CB_CUDA_DW(cudaGetDevice(&dev));
+    CB_CUDA_DW(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CB_CUDA_DW(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, dyn_smem));
+    return std::max(1, sms * std::min(per, per_sm_cap));
+}
+
+}  // namespace
+
+long band_dw_block() { return SB; }
+
+size_t band_dw_extra_bytes(long n, long bw)
+{
+    const long nblk = (n + SB - 1) / SB;
+    (void)bw;
+    return sizeof(dw) * 2 * (size_t)nblk * kBlockElems;
+}
+
+void band_dw_alloc(BandFactor &f)
+{
+    const long npad = f.nblk * f.s;
+    if (f.s != SB) throw std::runtime_error("the double-word band is padded to 128-row blocks");
+    const size_t inv = sizeof(dw) * (size_t)(npad / SB) * kBlockElems;
+    CB_CUDA_DW(cudaMalloc(&f.linv, inv));
+    CB_CUDA_DW(cudaMalloc(&f.linvt, inv));
+    f.factor_grid = coop_grid(factor_dw_kernel, 2);
+    static const bool smem_ok = [] {
+        return cudaFuncSetAttribute(solve_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSolveSmem) == cudaSuccess;
+    }();
+    if (!smem_ok) throw std::runtime_error("the double-word solve needs 160 KB of shared memory per CTA");
+    const int sgrid = coop_grid(solve_dw_kernel, 1, kSolveSmem);
+    // the solve gives each 32 rows (columns) of a block's reach a CTA of its own
+    const long need = (f.bw + NB - 1) / NB;
+    if (need > sgrid) throw std::runtime_error("band too wide for the double-word solve's cooperative grid");
+    f.solve_grid = (int)std::max(1L, need);
+    f.solve_grid_full = f.solve_grid;
+    f.bytes += band_dw_extra_bytes(f.n, f.bw);
+}
+
+void band_dw_gather(const int *ptr, const int *src, const int64_t *dst, const double *kel, BandFactor &f,
+                    long nslots, cudaStream_t st)
+{
+    if (nslots > 0)
+        gather_band_dw_kernel<<<(unsigned)((nslots + 255) / 256), 256, 0, st>>>(ptr, src, dst, kel, (dw *)f.band,
+                                                                               nslots);
+    CB_CUDA_DW(cudaGetLastError());
+}
+
+void band_dw_factor(BandFactor &f, cudaStream_t st, long *launches)
+{
+    const long npad = f.nblk * f.s;
+    dw *band = (dw *)f.band;
+    if (npad > f.n) {
+        pad_identity_dw_kernel<<<(unsigned)((npad - f.n + 127) / 128), 128, 0, st>>>(band, f.ld, f.n, npad);
+        ++*launches;
+    }
+    CB_CUDA_DW(cudaMemsetAsync(f.flags, 0, 2 * sizeof(int), st));
+    CB_CUDA_DW(cudaMemsetAsync(f.fbar, 0, sizeof(GridBarrier), st));
+    const long tiles = ((f.bw + TW - 1) / TW) * ((f.bw + TW - 1) / TW + 1) / 2;
+    const int grid = (int)std::max(1L, std::min<long>(f.factor_grid, std::max(tiles + 1, (f.bw + 7) / 8)));
+    DwFactorArgs a{band, f.ld, f.bw, npad, f.n, (dw *)f.dinv, f.ssd, f.flags, (dw *)f.work, (dw *)f.look, f.fbar,
+                   f.max_polls};
+    void *args[] = {&a};
+    CB_CUDA_DW(cudaLaunchCooperativeKernel((const void *)factor_dw_kernel, dim3((unsigned)grid), dim3(kThreads),
+                                           args, 0, st));
+    inv_block_kernel<<<(unsigned)(npad / SB), kThreads, 0, st>>>(band, f.ld, f.bw, (dw *)f.linv, (dw *)f.linvt);
+    CB_CUDA_DW(cudaGetLastError());
+    *launches += 2;
+}
+
+void band_dw_solve(const BandFactor &f, const double *rhs, double *x, void *work, GridBarrier *bar,
+                   cudaStream_t st)
+{
+    const long npad = f.nblk * f.s;
+    DwSolveArgs a{(const dw *)f.band, (const dw *)f.dinv, (const dw *)f.linv, (const dw *)f.linvt, f.ld, f.bw,
+                  npad, f.n, rhs, x, (dw *)work, (dw *)work + npad, bar, f.max_polls};
+    CB_CUDA_DW(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), st));
+    void *args[] = {&a};
+    CB_CUDA_DW(cudaLaunchCooperativeKernel((const void *)solve_dw_kernel, dim3((unsigned)f.solve_grid),
+                                           dim3(kThreads), args, kSolveSmem, st));
+}
+
+}  // namespace cb

@@ -146,6 +146,7 @@ struct BandFactor {
     void *stage = nullptr;       // 2 x 32x32: staged factored diagonal blocks (FP32 factor)
     void *look = nullptr;        // 2 x (32x32 + 32): the next panel's factored block (L, D) and 1/D
     bool fp32 = false;
+    bool dw = false;             // double-word band (pairs of floats, band_dw.cu); always direct
     bool direct = false;         // no solve blocks: substitution with the band (one solve per factor)
     int solve_grid = 1;          // CTAs of the cooperative solve launch
     int solve_grid_full = 1;     // ... when the handle has the GPU to itself
@@ -162,8 +163,23 @@ struct BandFactor {
 
 // direct: the factor serves one solve (Newmark's full Newton): the solve
 // substitutes with the band itself and no solve blocks are formed
-void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct = false, bool use_cluster = false);
+// direct_block: the padding block of a direct band (0: one 32-row panel)
+void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct = false, bool use_cluster = false,
+                long direct_block = 0);
 void band_free(BandFactor &f);
+// Double-word band (band_dw.cu): entries are pairs of floats (about 48
+// significant bits), the factor and its solves run on the FP32 pipe.
+// band_alloc_dw allocates the band and the block inverses of the solve; the
+// tangent is gathered from FP64 element matrices by band_dw_gather.
+void band_alloc_dw(BandFactor &f, long n, long bw);
+void band_dw_alloc(BandFactor &f);
+size_t band_dw_extra_bytes(long n, long bw);
+long band_dw_block();  // rows of the solve's blocks (the band is padded to a multiple)
+void band_dw_gather(const int *ptr, const int *src, const int64_t *dst, const double *kel, BandFactor &f,
+                    long nslots, cudaStream_t st);
+void band_dw_factor(BandFactor &f, cudaStream_t st, long *launches);
+void band_dw_solve(const BandFactor &f, const double *rhs, double *x, void *work, GridBarrier *bar,
+                   cudaStream_t st);
 // The band already holds an LDL^T factor (L below, D on the diagonal): form
 // 1/d and the solve blocks so that band_solve can use it.
 void band_use_factored(BandFactor &f, cudaStream_t st);

@@ -165,6 +165,7 @@ void upload_model(cb_model *m)
     h2d(m->fmap_ptr, fm.ptr.data(), fm.ptr.size(), st);
     h2d(m->fmap_src, fm.src.data(), fm.src.size(), st);
     const bool fp32 = m->opt.precision == CB_MIXED;
+    const bool dwp = m->opt.precision == CB_FP32X2;
     if (m->opt.solver == CB_SOLVER_FGMRES) {
         // FP64 matrix and Krylov vectors; mixed precision stores the
         // preconditioner in FP32
@@ -188,8 +189,11 @@ void upload_model(cb_model *m)
     }
     // Newmark and full Newton-Raphson refactor every iteration and solve once
     // per factorisation: direct substitution, no solve blocks
-    cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5 || h.alg == 1 || m->opt.band_solve == 1,
-                   m->opt.factor_kernel == 1);
+    if (dwp)
+        cb::band_alloc_dw(m->bf, N, h.bw);
+    else
+        cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5 || h.alg == 1 || m->opt.band_solve == 1,
+                       m->opt.factor_kernel == 1);
     m->bytes += m->bf.bytes;
     cb::build_tangent_map(h, m->bf.ld, tm);
     m->tmap_n = (long)tm.dst.size();
@@ -330,7 +334,8 @@ void assemble_tangent_t(cb_model *m, TangentState which)
         cb::launch_frame_tangent<K>(fr, conv ? fr.c_c : fr.c_ip, conv ? fr.ef_c : fr.ef_ip,
                                     conv ? fr.len_c : fr.len_ip, m->fr_lref, k + 171 * E + 21 * T, F, m->st);
     }
-    cb::launch_gather_band<K>(m->tmap_ptr, m->tmap_src, m->tmap_dst, k, (K *)bf.band, m->tmap_n, m->st);
+    if (bf.dw) cb::band_dw_gather(m->tmap_ptr, m->tmap_src, m->tmap_dst, (const double *)k, bf, m->tmap_n, m->st);
+    else cb::launch_gather_band<K>(m->tmap_ptr, m->tmap_src, m->tmap_dst, k, (K *)bf.band, m->tmap_n, m->st);
     m->tm.launches += 1 + (E ? 1 : 0) + (T ? 1 : 0) + (F ? 1 : 0);
 }
 
@@ -709,6 +714,16 @@ int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb
         *out = m;
         return CB_ERR_UNSUPPORTED;
     }
+    if (m->opt.precision != CB_FP64 && m->opt.precision != CB_MIXED && m->opt.precision != CB_FP32X2) {
+        m->err = "unknown precision";
+        *out = m;
+        return CB_ERR_ARG;
+    }
+    if (m->opt.precision == CB_FP32X2 && (m->opt.solver != CB_SOLVER_BAND || m->h.alg == 5)) {
+        m->err = "the double-word band serves the band solver of arc-length and Newton-Raphson models";
+        *out = m;
+        return CB_ERR_UNSUPPORTED;
+    }
     if (m->opt.precond != CB_PRECOND_BLOCK_JACOBI && m->opt.precond != CB_PRECOND_LEARNED) {
         m->err = "unknown preconditioner";
         *out = m;
@@ -1055,6 +1070,11 @@ int cb_eval_tangent(cb_model *m, const double *x, const double *c_sh, const doub
             d2h(bfl.data(), (const float *)bf.band, bfl.size(), st);
             CB_CUDA(cudaStreamSynchronize(st));
             for (size_t i = 0; i < bfl.size(); ++i) band[i] = bfl[i];
+        } else if (bf.dw) {
+            std::vector<float> pairs(2 * (size_t)bf.ld * npad);
+            d2h(pairs.data(), (const float *)bf.band, pairs.size(), st);
+            CB_CUDA(cudaStreamSynchronize(st));
+            for (size_t i = 0; i < band.size(); ++i) band[i] = (double)pairs[2 * i] + (double)pairs[2 * i + 1];
         } else {
             d2h(band.data(), (const double *)bf.band, band.size(), st);
             CB_CUDA(cudaStreamSynchronize(st));

@@ -24,6 +24,7 @@ STATUS = {0: "ok", 1: "bad argument", 2: "parse error", 3: "CUDA error", 4: "uns
 
 FP64 = 0
 MIXED = 1
+FP32X2 = 2
 
 K_SOLVE, K_SHELL_FORCE, K_FACTOR, K_BAND_LDLT, K_SOLVE_BLOCKS, K_FRAME_FORCE, K_SPMV = range(7)
 

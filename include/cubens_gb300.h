@@ -47,7 +47,11 @@ typedef struct cb_model cb_model;
  * FP64 in both modes. */
 enum cb_precision {
     CB_FP64 = 0,   /* plain path: FP64 tangent and FP64 LDL^T (parity with the reference) */
-    CB_MIXED = 1   /* FP32 tangent and FP32 LDL^T; the modified-Newton loop refines in FP64 */
+    CB_MIXED = 1,  /* FP32 tangent and FP32 LDL^T; the modified-Newton loop refines in FP64 */
+    CB_FP32X2 = 2  /* FP64 tangent assembled into a band of float pairs (about 48 significant
+                      bits); the LDL^T and its direct solves in double-word arithmetic on the
+                      FP32 pipe. For bands whose conditioning an FP32 factor cannot carry
+                      (arc-length and Newton-Raphson models; band solver) */
 };
 
 /* Linear solver of the equilibrium iterations. */
