@@ -1,22 +1,26 @@
 #!/usr/bin/env python3
 """Converged arc-length steps per second on one GB300 (or N replicas).
 
-Workload: the hinged cylindrical DKT shell panel (R 2540, L 508, theta 0.2
-rad, t 12.7, E 3102.75, nu 0.3) on a 64 x 64 quad mesh: 8192 triangles, 4225
-joints, 24,960 equations, centre point load, modified spherical arc length.
-One "step" is one converged arc-length increment (main.c:2647-3134): tangent,
-LDL^T, predictor and the modified-Newton corrector iterations to the
-reference's own convergence test.
+Default workload: the hinged cylindrical DKT shell panel (R 2540, L 508,
+theta 0.2 rad, t 12.7, E 3102.75, nu 0.3) on a 512 x 512 quad mesh: 524,288
+triangles, 263,169 joints, 1,575,936 equations (band 3,083), a seeded
+four-mode radial imperfection of 0.05 t, centre point load, modified
+spherical arc length. One "step" is one converged arc-length increment
+(main.c:2647-3134): tangent, LDL^T, predictor and the modified-Newton
+corrector iterations to the reference's own convergence test. The headline
+leg factors and solves the band in double-word FP32 arithmetic (CB_FP32X2);
+the plain FP64 band leg runs beside it on the first increments.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload panel|frame]
+                    [--workload panel512|panel64|frame|batch]
 
---workload frame measures the nonlinear Newmark workload instead: the
-20 x 20 bay, 30 storey steel frame building (13,671 joints, 38,430
-co-rotational 14-DOF members, warping fixed: NEQ 79,380), seeded
-band-limited lateral floor forces, dt 0.005 s; a step is one time step
-(main.c:3449-3953: full Newton, the effective stiffness factored every
-iteration).
+--workload panel64 measures the 64 x 64 panel (NEQ 24,960) with the FP32
+band; --workload frame the nonlinear Newmark workload: the 20 x 20 bay, 30
+storey steel frame building (13,671 joints, 38,430 co-rotational 14-DOF
+members, warping fixed: NEQ 79,380), seeded band-limited lateral floor
+forces, dt 0.005 s; a step is one time step (main.c:3449-3953: full Newton,
+the effective stiffness factored every iteration); --workload batch the
+batched imperfection sweep.
 
 Under torchrun with N > 1 every rank runs an independent replica of the
 analysis on its own GPU (the analysis does not shard); value is the total
@@ -41,6 +45,11 @@ sys.path.insert(0, str(ROOT / "cu-bens_gb300"))
 
 METRIC = "converged load steps/s at 1e-8 residual: learned+mixed vs plain FP64 GPU"
 WORKLOAD = "DKT cylindrical panel 64x64 (8192 shells, 4225 joints, NEQ 24960), MSAL"
+LARGE_WORKLOAD = ("DKT cylindrical panel 512x512 (524,288 shells, 263,169 joints, NEQ 1,575,936, band 3,083), "
+                  "seeded 4-mode imperfection 0.05 t, MSAL")
+LARGE_N, LARGE_SEED, LARGE_IMP = 512, 5, 0.05
+LARGE_CONTROLS = ("dk -0.2 at the centre joint, alpha 1, psi 0.1, iteopt 6, itemax 100, toldisp 1e-5; force and "
+                  "energy criteria off: the reference formulation's residual floor on the imperfect panel")
 
 
 def panel_text(n: int = 64):
@@ -48,6 +57,14 @@ def panel_text(n: int = 64):
     c = models.MsalControls(joint=n // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.2, toldisp=1e-5,
                             tolforc=1.0, tolener=1.0, itemax=100)
     return models.cylindrical_panel(n, controls=c).text, c
+
+
+def large_text(n: int = LARGE_N):
+    """The 512 x 512 panel (or the same panel on an n x n mesh) with its controls."""
+    from cubens import models
+    c = models.MsalControls(joint=n // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.2, toldisp=1e-5,
+                            tolforc=1.0, tolener=1.0, itemax=100)
+    return models.cylindrical_panel(n, seed=LARGE_SEED, imperfection=LARGE_IMP, controls=c).text
 
 
 def peaks():
@@ -683,17 +700,216 @@ def run_ours(args, world, rank, local, pg):
     return line
 
 
+def large_cpu_sample(n_sample: int = 128, steps: int = 2):
+    """The oracle port (single thread, the reference is serial) on the same
+    panel at n_sample x n_sample: the first increment untimed, then `steps`
+    arc-length steps timed; scaled to the 512 x 512 panel by the skyline
+    factorisation work n bw^2 (the factorisation dominates a step once the
+    band is wide: three or four iterations per step here). A step of the
+    full panel takes about an hour and a half on one core, so it is
+    extrapolated."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    o = oracle.OracleModel(large_text(n_sample))
+    t0 = time.perf_counter()
+    r = o.msal_timed(1 + steps)
+    if len(r["t"]) < 1 + steps:
+        raise RuntimeError(f"oracle stopped early: {r['error']}")
+    secs = r["t"][-1] - r["t"][0]
+    wall = time.perf_counter() - t0
+
+    def neq_bw(n):
+        # hinged straight edges: 3 translations of 2 (n + 1) joints fixed; row-major joint numbering
+        return 6 * (n + 1) ** 2 - 6 * (n + 1), 6 * (n + 2) - 1
+
+    ns, bs = neq_bw(n_sample)
+    nf, bf = neq_bw(LARGE_N)
+    scale = (nf * bf ** 2) / (ns * bs ** 2)
+    per_step = secs / steps * scale
+    return {"value": 1.0 / per_step, "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"oracle port (C restatement of the reference, gcc -O2, 1 thread): the same panel on a "
+                      f"{n_sample}x{n_sample} mesh (NEQ {ns}), first increment untimed, {steps} arc-length steps "
+                      f"in {secs:.1f} s ({[int(x) for x in r['its'][1:]]} iterations), scaled by n bw^2 to NEQ "
+                      f"{nf} (x{scale:.0f}): extrapolated, {per_step / 3600:.2f} h per step",
+            "total_s": wall}
+
+
+def run_large(args, world, rank, local, pg):
+    """The 512 x 512 panel: the double-word FP32 band (headline), the plain
+    FP64 band on the first increments, end to end through the public API."""
+    import cubens
+    device = local if world > 1 else 0
+    hbm_peak, peak_kind = peaks()
+    text = large_text()
+    total = 1 + args.warmup + args.steps
+    # ---- headline: created from the model_def text (the end-to-end clock starts), first
+    #      increment, warm-up, the timed steps; d read back after every increment ----
+    barrier(pg)
+    w_e2e = time.perf_counter()
+    m = cubens.Model(text, precision=cubens.FP32X2, device=device, band_solve=1)
+    info = m.info
+    recs = []
+
+    def record(r):
+        d, lam = m.displacements()
+        recs.append({"lam": r.lam, "its": r.iterations, "res": r.residual, "dk": r.dk, "d": d})
+
+    record(m.begin())
+    for _ in range(args.warmup):
+        record(m.step())
+    clocks = ClockSampler(device)
+    barrier(pg)
+    clocks.start()
+    l0 = m.timers()["launches"]
+    m.mark(0)
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = m.step()
+        if r.done:
+            raise RuntimeError("analysis limits reached inside the timed region")
+        record(r)
+    m.mark(1)
+    dev_ms = m.elapsed_ms(0, 1)
+    wall_ms = (time.perf_counter() - w0) * 1e3
+    launches = m.timers()["launches"] - l0
+    e2e_s = time.perf_counter() - w_e2e
+    clk = clocks.stop()
+    barrier(pg)
+    t_max = allmax(pg, wall_ms)
+    value = world * args.steps / (t_max / 1e3)
+    d2h = sum(x["d"].nbytes + 8 for x in recs)
+    e2e = {"value": world * total / allmax(pg, e2e_s), "unit": "steps/s",
+           "h2d_bytes_per_step": info["h2d_bytes"] / total, "d2h_bytes_per_step": d2h / total,
+           "includes": "model_def parse + upload, first increment, warm-up and timed increments, d read back "
+                       "after every increment (host buffers, C ABI through ctypes)"}
+    # per-phase times of one more increment, then the dominant kernels alone
+    m.reset_timers()
+    m.set_timing(True)
+    m.step()
+    m.set_timing(False)
+    tm = m.timers()
+    ms_solve, bytes_solve, _ = m.profile_kernel(cubens.K_SOLVE, reps=5)
+    ms_force, bytes_force, flops_force = m.profile_kernel(cubens.K_SHELL_FORCE, reps=20)
+    ms_ldlt, bytes_ldlt, flops_ldlt = m.profile_kernel(cubens.K_BAND_LDLT, reps=1)
+    m.close()
+    # ---- plain FP64 band on the first increments (a step is about half a minute) ----
+    k64 = max(1, min(args.steps, args.fp64_steps))
+    p = cubens.Model(text, precision=cubens.FP64, device=device, band_solve=1)
+    p64 = [p.begin()]
+    d64 = [p.displacements()[0]]
+    w0 = time.perf_counter()
+    for _ in range(k64):
+        p64.append(p.step())
+        d64.append(p.displacements()[0])
+    wall64 = (time.perf_counter() - w0) * 1e3
+    p.reset_timers()
+    p.set_timing(True)
+    p.step()
+    p.set_timing(False)
+    tm64 = p.timers()
+    p.close()
+    if rank != 0:
+        return None
+    # per-increment error of the headline leg against the FP64 leg (same increments)
+    err = []
+    for k, (rr, dd) in enumerate(zip(p64, d64)):
+        x = recs[k]
+        err.append({"increment": k, "iterations_fp32x2": x["its"], "iterations_fp64": rr.iterations,
+                    "lam_rel_err": abs(x["lam"] - rr.lam) / abs(rr.lam),
+                    "d_rel_err": float(np.linalg.norm(x["d"] - dd) / np.linalg.norm(dd))})
+    cpu = large_cpu_sample() if world == 1 and not args.skip_cpu else None
+    timed = recs[1 + args.warmup:]
+    n, bw = info["neq"], info["bandwidth"]
+    fma = n * bw * bw / 2.0                        # band LDL^T multiply-adds per factorisation
+    fp32_ops = fma * 12.0                          # a double-word multiply-add: 12 FP32 instructions
+    fp32_peak = 152 * 128 * 2.07e9                 # FP32 lanes x clock (nominal), instructions/s
+    achieved = bytes_ldlt / (ms_ldlt * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 forces/residual/arc-length; f64 tangent; band LDL^T and solves in double-word f32 (~48-bit)",
+        "data": "synthetic",
+        "config": {"workload": LARGE_WORKLOAD, "neq": n, "bandwidth": bw, "seed": LARGE_SEED,
+                   "imperfection": f"{LARGE_IMP} t, modes (1,1),(1,2),(2,1),(2,2)", "controls": LARGE_CONTROLS,
+                   "parallelism": f"replicas x{world}",
+                   "l2": f"working set > L2: {info['device_bytes'] / 1e9:.1f} GB on the device (the band "
+                         f"{8 * n * (bw + 5) / 1e9:.1f} GB), streamed by every factorisation and solve",
+                   "iterations_per_step": [x["its"] for x in timed],
+                   "max_rel_residual": max(x["res"] for x in timed),
+                   "residual_per_step": [x["res"] for x in timed],
+                   "lam_per_step": [x["lam"] for x in timed],
+                   "device_ms_timed": dev_ms,
+                   "error_vs_fp64_gpu": err,
+                   "fp64_plain": {"value": k64 / (wall64 / 1e3), "ms_per_step": wall64 / k64, "steps": k64,
+                                  "iterations_per_step": [x.iterations for x in p64[1:]],
+                                  "max_rel_residual": max(x.residual for x in p64[1:]),
+                                  "phase_ms_one_step": {k: round(v, 1) for k, v in tm64.items()
+                                                        if k.startswith("ms_")}},
+                   "fp32x2_over_fp64": (args.steps / (wall_ms / 1e3)) / (k64 / (wall64 / 1e3)),
+                   "phase_ms_one_step": {k: round(v, 1) for k, v in tm.items() if k.startswith("ms_")},
+                   "band_ldlt_ms": ms_ldlt, "band_ldlt_fma_per_s": fma / (ms_ldlt * 1e-3),
+                   "solve_ms": ms_solve, "shell_force_ms": ms_force,
+                   "shell_force_GBps": bytes_force / (ms_force * 1e-3) / 1e9,
+                   "fp32_band_ldlt": "diverges at this size (first increment: lambda 615 after the first solve "
+                                     "against 81.45, no convergence in 100 iterations); not a leg"},
+        "roofline": {"kernel": "factor_dw_kernel (persistent band LDL^T, double-word FP32, two grid barriers per "
+                               "32-column panel)",
+                     "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                     "traffic": (TRAFFIC_DW_256 * (n * (bw + 5)) / (394752 * 1552)) if TRAFFIC_DW_256 else None,
+                     "traffic_source": "profiles/factor_dw_kernel_panel256.md (one launch on the 256 x 256 panel, "
+                                       "scaled by n ld)",
+                     "bytes_per_launch": bytes_ldlt, "ms_per_launch": ms_ldlt,
+                     "note": "compute-bound on the FP32 pipe: bytes = the band read and written once; the pipe "
+                             "figure is in roofline_compute"},
+        "roofline_compute": {"kernel": "factor_dw_kernel", "bound": "fp32 pipe",
+                             "achieved": fp32_ops / (ms_ldlt * 1e-3) / 1e12, "peak": fp32_peak / 1e12,
+                             "unit": "T FP32 instructions/s", "frac": fp32_ops / (ms_ldlt * 1e-3) / fp32_peak,
+                             "peak_kind": "nominal (152 SMs x 128 FP32 lanes x 2.07 GHz)",
+                             "work": f"n bw^2 / 2 = {fma:.3e} double-word multiply-adds x 12 FP32 instructions"},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
+        "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_reference_large(args, world, rank, pg):
+    """The reference's CPU path (the oracle port) on the host, extrapolated
+    from the same panel on a 128 x 128 mesh (a step of the 512 x 512 panel is
+    about an hour and a half on one core)."""
+    if rank != 0:
+        return
+    cpu = large_cpu_sample()
+    line = {"metric": METRIC, "value": cpu["value"], "unit": "steps/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cpu["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": LARGE_WORKLOAD, "controls": LARGE_CONTROLS},
+            "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cpu["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one factor_dw_kernel launch on the 256 x 256
+# panel (NEQ 394,752, ld 1,552), from profiles/factor_dw_kernel_panel256.md
+TRAFFIC_DW_256 = None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample (profiling runs)")
     ap.add_argument("--skip-e2e", action="store_true", help="omit the end-to-end leg (profiling runs)")
-    ap.add_argument("--workload", choices=["panel", "frame", "batch"], default="panel",
-                    help="panel: MSAL DKT panel 64x64 (default); frame: nonlinear Newmark frame building; "
-                         "batch: the batched imperfection sweep")
+    ap.add_argument("--workload", choices=["panel512", "panel64", "frame", "batch"], default="panel512",
+                    help="panel512: MSAL DKT panel 512x512, 1.58M equations (default); panel64: the 64x64 "
+                         "panel; frame: nonlinear Newmark frame building; batch: the batched imperfection sweep")
+    ap.add_argument("--fp64-steps", type=int, default=2,
+                    help="panel512: timed increments of the plain FP64 leg (about half a minute each)")
     ap.add_argument("--batch", type=int, default=48, help="instances of the batch workload")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup(args.gpus)
@@ -707,10 +923,15 @@ def main():
             run_reference_frame(args, world, rank, pg)
         else:
             run_frame(args, world, rank, local, pg)
+    elif args.workload == "panel64":
+        if args.impl == "reference":
+            run_reference(args, world, rank, pg)
+        else:
+            run_ours(args, world, rank, local, pg)
     elif args.impl == "reference":
-        run_reference(args, world, rank, pg)
+        run_reference_large(args, world, rank, pg)
     else:
-        run_ours(args, world, rank, local, pg)
+        run_large(args, world, rank, local, pg)
     if pg:
         pg.destroy_process_group()
 
