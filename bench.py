@@ -896,7 +896,7 @@ def run_reference_large(args, world, rank, pg):
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one factor_dw_kernel launch on the 256 x 256
 # panel (NEQ 394,752, ld 1,552), from profiles/factor_dw_kernel_panel256.md
-TRAFFIC_DW_256 = None
+TRAFFIC_DW_256 = 4.972161e9 + 4.856823e9
 
 
 def main():
@@ -910,10 +910,21 @@ def main():
     ap.add_argument("--workload", choices=["panel512", "panel64", "frame", "batch"], default="panel512",
                     help="panel512: MSAL DKT panel 512x512, 1.58M equations (default); panel64: the 64x64 "
                          "panel; frame: nonlinear Newmark frame building; batch: the batched imperfection sweep")
+    ap.add_argument("--factor-only", type=int, default=0, metavar="N",
+                    help="profiling: the FP32x2 band LDL^T of the same panel on an N x N mesh (first increment, "
+                         "then one factorisation alone), no JSON line")
     ap.add_argument("--fp64-steps", type=int, default=2,
                     help="panel512: timed increments of the plain FP64 leg (about half a minute each)")
     ap.add_argument("--batch", type=int, default=48, help="instances of the batch workload")
     args = ap.parse_args()
+    if args.factor_only:
+        import cubens
+        m = cubens.Model(large_text(args.factor_only), precision=cubens.FP32X2, band_solve=1)
+        m.begin()
+        ms, _, fl = m.profile_kernel(cubens.K_BAND_LDLT, reps=1)
+        print(f"band LDL^T, NEQ {m.neq}, band {m.info['bandwidth']}: {ms:.1f} ms, "
+              f"{fl / 2 / (ms * 1e-3) / 1e12:.3f} T double-word multiply-adds/s", flush=True)
+        return
     world, rank, local, pg = dist_setup(args.gpus)
     if args.workload == "batch":
         if args.impl == "reference":

@@ -87,3 +87,43 @@ def test_fp32x2_refused_for_newmark():
     with pytest.raises(cubens.CubensError) as e:
         cubens.Model(f.text, precision=cubens.FP32X2)
     assert e.value.code == 4
+
+
+def _bench_controls(n):
+    # the controls of the 1.58M-equation benchmark panel (bench.large_text)
+    c = models.MsalControls(joint=n // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.05, toldisp=1e-5,
+                            tolforc=1.0, tolener=1.0, itemax=100)
+    return models.cylindrical_panel(n, seed=5, imperfection=0.05, controls=c).text
+
+
+def test_fp32x2_benchmark_window_matches_oracle():
+    """The benchmark's controls and imperfection on a 64 x 64 mesh, over as
+    many increments as the benchmark takes (first increment, 3 warm-up and 5
+    timed): the oracle's iteration counts, lambda and d to 1e-6 at every one."""
+    text = _bench_controls(64)
+    steps = 1 + 3 + 5
+    o = oracle.OracleModel(text).msal(steps)
+    assert o["rc"] == steps, o["error"]
+    g = cubens.Model(text, precision=cubens.FP32X2).run(steps)
+    np.testing.assert_array_equal(g["its"], o["its"])
+    assert _rel(g["lam"], o["lam"]) < 1e-6
+    for k in range(steps):
+        assert np.linalg.norm(g["d"][k] - o["d"][k]) / np.linalg.norm(o["d"][k]) < 1e-6, k
+
+
+def test_fp32x2_large_panel_matches_fp64_gpu():
+    """The benchmark panel itself (512 x 512, 1,575,936 equations): the
+    FP32x2 band against the FP64 band on the first two increments (an FP64
+    increment takes about half a minute)."""
+    text = _bench_controls(512)
+    out = []
+    for prec in (cubens.FP64, cubens.FP32X2):
+        m = cubens.Model(text, precision=prec, band_solve=1)
+        assert m.neq == 1575936
+        out.append(m.run(2))
+        m.close()
+    f64, x2 = out
+    np.testing.assert_array_equal(x2["its"], f64["its"])
+    assert _rel(x2["lam"], f64["lam"]) < 1e-6
+    for k in range(2):
+        assert np.linalg.norm(x2["d"][k] - f64["d"][k]) / np.linalg.norm(f64["d"][k]) < 1e-6, k

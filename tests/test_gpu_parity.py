@@ -97,22 +97,29 @@ def test_msal_panel32_matches_oracle():
     assert _rel(g["d"][-1], o["d"][-1]) < 1e-6
 
 
+def _curve_err(g, o):
+    """Largest |lambda - lambda_ref(d_k)| / |lambda_ref| of the run g against
+    the oracle curve o, at matched control displacement."""
+    k = int(np.argmax(np.abs(o["d"][0])))  # the control DOF carries the largest displacement
+    dk_o, lam_o = o["d"][:, k], o["lam"]
+    order = np.argsort(dk_o)
+    errs = [abs(lam - np.interp(dk, dk_o[order], lam_o[order])) / abs(np.interp(dk, dk_o[order], lam_o[order]))
+            for dk, lam in zip(g["d"][:, k], g["lam"]) if dk_o.min() <= dk <= dk_o.max()]
+    return max(errs)
+
+
 def test_mixed_precision_path_tracks_fp64_curve():
-    """FP32 tangent and factor: the same load-displacement curve within 1e-5."""
+    """FP32 tangent and factor on the 16 x 16 panel: the oracle's curve
+    lambda(d_k) within 1e-5 and the displacements within 1e-5 at every
+    increment (measured: 5e-10 and 2e-7, the same iteration counts)."""
     m = _panel(16)
     steps = 8
     o = oracle.OracleModel(m.text).msal(steps)
     g = cubens.Model(m.text, precision=cubens.MIXED).run(steps)
-    # the first increment is displacement controlled: same d_k, compare lambda
     assert abs(g["lam"][0] - o["lam"][0]) / abs(o["lam"][0]) < 1e-5
-    # later increments: compare lambda against the oracle curve lambda(d_k)
-    k = int(np.argmax(np.abs(o["d"][0])))  # the control DOF carries the largest displacement
-    dk_o, lam_o = o["d"][:, k], o["lam"]
-    order = np.argsort(dk_o)
-    for dk, lam in zip(g["d"][:, k], g["lam"]):
-        if dk_o.min() <= dk <= dk_o.max():
-            ref = np.interp(dk, dk_o[order], lam_o[order])
-            assert abs(lam - ref) / abs(ref) < 1e-3
+    assert _curve_err(g, o) < 1e-5
+    for k in range(steps):
+        assert np.linalg.norm(g["d"][k] - o["d"][k]) / np.linalg.norm(o["d"][k]) < 1e-5, k
     assert np.all(g["res"] < 1e-2)
 
 
@@ -140,6 +147,21 @@ def test_benchmark_panel64_matches_oracle():
     mx = cubens.Model(text, precision=cubens.MIXED).run(steps)
     np.testing.assert_array_equal(mx["its"], o["its"])
     assert _rel(mx["lam"], o["lam"]) < 1e-5
+
+
+def test_mixed_panel64_curve_within_1e5_over_14_increments():
+    """The FP32 factor on the 64 x 64 panel keeps the oracle's curve within
+    1e-5 (at matched control displacement) for the first 14 increments;
+    past them, near the limit point, it departs by up to 2e-4 (measured over
+    26 increments), which is why the large-panel benchmark factors in FP32x2
+    (tests/test_gpu_fp32x2.py holds that path to 1e-6)."""
+    import bench
+    text, _ = bench.panel_text(64)
+    steps = 14
+    o = oracle.OracleModel(text).msal(steps)
+    assert o["rc"] == steps, o["error"]
+    mx = cubens.Model(text, precision=cubens.MIXED).run(steps)
+    assert _curve_err(mx, o) < 1e-5
 
 
 def test_cluster_factor_matches_grid_factor_and_oracle():
