@@ -61,12 +61,14 @@ def panel_text(n: int = 64):
     return models.cylindrical_panel(n, controls=c).text, c
 
 
-def large_text(n: int = LARGE_N, toldisp: float = 1e-5):
-    """The 512 x 512 panel (or the same panel on an n x n mesh) with its controls."""
+def large_text(n: int = LARGE_N, toldisp: float = 1e-5, n_axial: int | None = None):
+    """The 512 x 512 panel (or the same panel on an n x n mesh, or n_axial x n)
+    with its controls."""
     from cubens import models
-    c = models.MsalControls(joint=n // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.05, toldisp=toldisp,
+    na = n if n_axial is None else n_axial
+    c = models.MsalControls(joint=na // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.05, toldisp=toldisp,
                             tolforc=1.0, tolener=1.0, itemax=100)
-    return models.cylindrical_panel(n, seed=LARGE_SEED, imperfection=LARGE_IMP, controls=c).text
+    return models.cylindrical_panel(n, seed=LARGE_SEED, imperfection=LARGE_IMP, controls=c, n_axial=n_axial).text
 
 
 def peaks():
@@ -910,16 +912,19 @@ def main():
     ap.add_argument("--workload", choices=["panel512", "panel64", "frame", "batch"], default="panel512",
                     help="panel512: MSAL DKT panel 512x512, 1.58M equations (default); panel64: the 64x64 "
                          "panel; frame: nonlinear Newmark frame building; batch: the batched imperfection sweep")
-    ap.add_argument("--factor-only", type=int, default=0, metavar="N",
-                    help="profiling: the FP32x2 band LDL^T of the same panel on an N x N mesh (first increment, "
-                         "then one factorisation alone), no JSON line")
+    ap.add_argument("--factor-only", default="", metavar="N[xA]",
+                    help="profiling: the FP32x2 band LDL^T of the same panel on an N x N mesh, or A axial by N "
+                         "circumferential divisions (the band of the N x N panel with fewer equations): first "
+                         "increment, then one factorisation alone; no JSON line")
     ap.add_argument("--fp64-steps", type=int, default=2,
                     help="panel512: timed increments of the plain FP64 leg (about half a minute each)")
     ap.add_argument("--batch", type=int, default=48, help="instances of the batch workload")
     args = ap.parse_args()
     if args.factor_only:
         import cubens
-        m = cubens.Model(large_text(args.factor_only), precision=cubens.FP32X2, band_solve=1)
+        nf, _, na = args.factor_only.partition("x")
+        m = cubens.Model(large_text(int(nf), n_axial=int(na) if na else None), precision=cubens.FP32X2,
+                         band_solve=1)
         m.begin()
         ms, _, fl = m.profile_kernel(cubens.K_BAND_LDLT, reps=1)
         print(f"band LDL^T, NEQ {m.neq}, band {m.info['bandwidth']}: {ms:.1f} ms, "

@@ -8,7 +8,7 @@
 // band is a pair of floats (dw.cuh, about 48 significant bits) and all
 // arithmetic runs on the FP32 pipe.
 //
-// Factor: one persistent cooperative kernel, right-looking over 32-column
+// Factor: one persistent cooperative kernel, right-looking over 64-column
 // panels, two bounded grid barriers per panel:
 //   1. the panel's factored diagonal block (L below, D on the diagonal) and
 //      1/D come from the look-ahead buffer (CTA 0 factored the block during
@@ -19,7 +19,7 @@
 //   -- grid barrier --
 //   3. the trailing lower triangle of the band window in 64 x 64 tiles,
 //      A_ij -= sum_k W_ik L_jk, each thread a 4 x 4 block of accumulators;
-//      CTA 0 takes only tile (0,0), which holds the next panel's diagonal
+//      CTA 0 takes only tile (0,0), which is the next panel's diagonal
 //      block, and factors that block right after its update while the other
 //      CTAs work through the rest of the triangle;
 //   -- grid barrier --
@@ -57,7 +57,8 @@ namespace cb {
 
 namespace {
 
-constexpr int NB = 32;        // panel width of the factor, tile size of the block inverses
+constexpr int NB = 32;        // tile size of the block inverses
+constexpr int PW = 64;        // panel width of the factor
 constexpr int TW = 64;        // tile of the factor's trailing update (4 x 4 accumulators per thread)
 constexpr int SB = 128;       // block size of the solve
 constexpr int kTiles = (SB / NB) * (SB / NB + 1) / 2;  // lower 32 x 32 tiles of a block
@@ -76,44 +77,64 @@ struct DwFactorArgs {
     dw *dinv;       // npad: 1/D
     double *ssd;    // n pivots
     int *flags;     // [0] a pivot <= 0, [1] a zero pivot
-    dw *wl;         // 2 * 32 * bw: W (row r of column k at k * m + r), then L at offset 32 * bw
-    dw *look;       // the next panel's factored block (32 x 32) and 1/D (32)
+    dw *wl;         // 2 * 64 * (bw + 1): W (row r of column k at k * ms + r, ms = m rounded up to
+                    // even), then L at offset 64 * (bw + 1)
+    dw *look;       // the next panel's factored block (64 x 64) and 1/D (64)
     GridBarrier *bar;
     long long max_polls;
 };
 
-// LDL^T of the 32 x 32 block in A (lower triangle) by all threads of the CTA,
+// shared memory of the factor: the diagonal block (and 1/D), W and L of a tile
+constexpr int KH = PW / 2;  // depth of one stage of a tile's update (half the panel)
+struct DwFactorSmem {
+    dw A[PW][PW + 1];     // factored diagonal block of the panel: L below, D on the diagonal
+    dw di[PW];            // 1/D
+    dw Wt[2][KH][TW];     // W of a tile's rows for one stage, k-major, two buffers
+    dw Lt[2][KH][TW];     // L of a tile's columns for one stage
+};
+
+__device__ __forceinline__ void cp_async16_zfill(void *smem, const void *gmem, bool valid)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+    const int n = valid ? 16 : 0;  // 0: the 16 bytes are zero-filled, nothing is read
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_f() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_f() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// LDL^T of the 64 x 64 block in A (lower triangle) by all threads of the CTA,
 // one CTA barrier per column: every thread forms 1/D_k itself from the final
 // pivot, the update uses the unscaled column (W = L D), and the columns are
 // scaled by 1/D at the end. On return L below the diagonal, D on it, di = 1/D.
-__device__ void ldlt32_dw(dw (*A)[NB + 1], dw *di)
+__device__ void ldlt_block_dw(dw (*A)[PW + 1], dw *di)
 {
     const int tid = threadIdx.x;
-    for (int k = 0; k < NB; ++k) {
+    for (int k = 0; k < PW; ++k) {
         const dw dk = dw_recip(A[k][k]);
-        for (int e = tid; e < NB * NB; e += kThreads) {
-            const int j = e / NB, i = e % NB;
+        for (int e = tid; e < PW * PW; e += kThreads) {
+            const int j = e / PW, i = e % PW;
             if (j > k && i >= j) A[i][j] = dw_sub(A[i][j], dw_mul(dw_mul(A[i][k], dk), A[j][k]));
         }
         if (tid == 0) di[k] = dk;
         __syncthreads();
     }
-    for (int e = tid; e < NB * NB; e += kThreads) {
-        const int j = e / NB, i = e % NB;
+    for (int e = tid; e < PW * PW; e += kThreads) {
+        const int j = e / PW, i = e % PW;
         if (i > j) A[i][j] = dw_mul(A[i][j], di[j]);
     }
     __syncthreads();
 }
 
 // The factored block of panel p into the band, 1/D, the FP64 pivots and the flags.
-__device__ void record_block(const DwFactorArgs &a, long p, const dw (*A)[NB + 1], const dw *di)
+__device__ void record_block(const DwFactorArgs &a, long p, const dw (*A)[PW + 1], const dw *di)
 {
     const int tid = threadIdx.x;
-    for (int e = tid; e < NB * NB; e += kThreads) {
-        const int j = e / NB, i = e % NB;
+    for (int e = tid; e < PW * PW; e += kThreads) {
+        const int j = e / PW, i = e % PW;
         if (i >= j && i - j <= a.bw) a.band[(p + j) * a.ld + (i - j)] = A[i][j];
     }
-    if (tid < NB) {
+    if (tid < PW) {
         a.dinv[p + tid] = di[tid];
         const long g = p + tid;
         if (g < a.n) {
@@ -125,126 +146,169 @@ __device__ void record_block(const DwFactorArgs &a, long p, const dw (*A)[NB + 1
     }
 }
 
-__device__ void load_block(const DwFactorArgs &a, long p, dw (*A)[NB + 1])
+__device__ void load_block(const DwFactorArgs &a, long p, dw (*A)[PW + 1])
 {
-    for (int e = threadIdx.x; e < NB * NB; e += kThreads) {
-        const int j = e / NB, i = e % NB;
+    for (int e = threadIdx.x; e < PW * PW; e += kThreads) {
+        const int j = e / PW, i = e % PW;
         A[i][j] = (i >= j && i - j <= a.bw) ? a.band[(p + j) * a.ld + (i - j)] : dw_zero();
     }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads) factor_dw_kernel(DwFactorArgs a)
+__global__ void __launch_bounds__(kThreads, 1) factor_dw_kernel(DwFactorArgs a)
 {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    DwFactorSmem &sm = *reinterpret_cast<DwFactorSmem *>(dyn);
+    auto &A = sm.A;
+    auto &di = sm.di;
+    auto &Wt = sm.Wt;
+    auto &Lt = sm.Lt;
     unsigned ep = 0;  // grid barriers passed
-    __shared__ dw A[NB][NB + 1];   // factored diagonal block of the panel
-    __shared__ dw di[NB];          // 1/D
-    __shared__ dw Wt[NB][TW];      // W of a tile's rows, k-major
-    __shared__ dw Lt[NB][TW];      // L of a tile's columns, k-major
     const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
     const long ld = a.ld, bw = a.bw;
     const unsigned G = gridDim.x;
-    for (long p = 0; p < a.npad; p += NB) {
-        long m = a.npad - p - NB;
+    for (long p = 0; p < a.npad; p += PW) {
+        long m = a.npad - p - PW;
         if (m > bw) m = bw;
         if (m < 0) m = 0;
         // ---- 1. the factored diagonal block ----
         if (p == 0) {
             load_block(a, 0, A);
-            ldlt32_dw(A, di);
+            ldlt_block_dw(A, di);
             if (blockIdx.x == 0) record_block(a, 0, A, di);
         } else {
-            for (int e = tid; e < NB * NB; e += kThreads) A[e / NB][e % NB] = a.look[e];
-            if (tid < NB) di[tid] = a.look[NB * NB + tid];
+            for (int e = tid; e < PW * PW; e += kThreads) A[e / PW][e % PW] = a.look[e];
+            if (tid < PW) di[tid] = a.look[PW * PW + tid];
         }
         __syncthreads();
-        // ---- 2. panel rows by substitution (one warp per row) ----
-        dw *wbuf = a.wl, *lbuf = a.wl + (long)NB * bw;
+        // ---- 2. panel rows by substitution (one warp per row, lane: columns lane and lane + 32) ----
+        // W and L of the panel, k-major with an even row stride (16-byte rows for cp.async)
+        const long ms = (m + 1) & ~1L;
+        dw *wbuf = a.wl, *lbuf = a.wl + (long)PW * (bw + 1);
+        if (ms > m && blockIdx.x == 0 && tid < PW) {
+            wbuf[tid * ms + m] = dw_zero();
+            lbuf[tid * ms + m] = dw_zero();
+        }
         for (long r = blockIdx.x * 8L + warp; r < m; r += G * 8L) {
-            const long off = NB + r - lane;
-            dw w = off <= bw ? a.band[(p + lane) * ld + off] : dw_zero();
-            for (int k = 0; k < NB - 1; ++k) {
-                const dw wk = shfl_dw(w, k);
-                if (lane > k) w = dw_sub(w, dw_mul(wk, A[lane][k]));
+            const long off0 = PW + r - lane, off1 = off0 - 32;
+            dw w0 = off0 <= bw ? a.band[(p + lane) * ld + off0] : dw_zero();
+            dw w1 = off1 <= bw ? a.band[(p + 32 + lane) * ld + off1] : dw_zero();
+            for (int k = 0; k < 32; ++k) {
+                const dw wk = shfl_dw(w0, k);
+                if (lane > k) w0 = dw_sub(w0, dw_mul(wk, A[lane][k]));
+                w1 = dw_sub(w1, dw_mul(wk, A[32 + lane][k]));
             }
-            const dw l = dw_mul(w, di[lane]);
-            wbuf[lane * m + r] = w;
-            lbuf[lane * m + r] = l;
-            if (off <= bw) a.band[(p + lane) * ld + off] = l;
+            for (int k = 0; k < 31; ++k) {
+                const dw wk = shfl_dw(w1, k);
+                if (lane > k) w1 = dw_sub(w1, dw_mul(wk, A[32 + lane][32 + k]));
+            }
+            const dw l0 = dw_mul(w0, di[lane]), l1 = dw_mul(w1, di[32 + lane]);
+            wbuf[lane * ms + r] = w0;
+            wbuf[(32 + lane) * ms + r] = w1;
+            lbuf[lane * ms + r] = l0;
+            lbuf[(32 + lane) * ms + r] = l1;
+            if (off0 <= bw) a.band[(p + lane) * ld + off0] = l0;
+            if (off1 <= bw) a.band[(p + 32 + lane) * ld + off1] = l1;
         }
         if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
         // ---- 3. trailing triangle; CTA 0: tile (0,0), then the next block ----
         const long nt = (m + TW - 1) / TW;
         const long ntiles = nt * (nt + 1) / 2;
         const int tx = tid % 16, ty = tid / 16;
-        auto tile = [&](long t) {
-            // tile (ti, tj) of the lower triangle, t = ti (ti + 1) / 2 + tj
-            long ti = (long)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-            while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-            while (ti * (ti + 1) / 2 > t) --ti;
-            const long tj = t - ti * (ti + 1) / 2;
-            const long r0 = ti * TW, j0 = tj * TW;
-            for (int e = tid; e < NB * TW; e += kThreads) {
-                const int k = e / TW, q = e % TW;
-                Wt[k][q] = r0 + q < m ? wbuf[k * m + r0 + q] : dw_zero();
-                Lt[k][q] = j0 + q < m ? lbuf[k * m + j0 + q] : dw_zero();
-            }
-            // the band values the tile updates, loaded ahead of the products:
-            // rows r0 + tx + 16 i, columns j0 + ty + 16 j
-            dw old[4][4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const long rr = r0 + tx + 16 * i, jj = j0 + ty + 16 * j;
-                    old[i][j] = (rr < m && jj <= rr) ? a.band[(p + NB + jj) * ld + (rr - jj)] : dw_zero();
+        // the tiles t = first, first + stride, ... (< last) in stages of half the
+        // panel's depth; the next stage's W and L come in by cp.async while
+        // the current one computes
+        auto tiles = [&](long first, long stride, long last) {
+            if (first >= last) return;
+            const long nst = 2 * ((last - first + stride - 1) / stride);
+            auto coords = [&](long t, long &r0, long &j0) {
+                long ti = (long)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+                while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+                while (ti * (ti + 1) / 2 > t) --ti;
+                r0 = ti * TW;
+                j0 = (t - ti * (ti + 1) / 2) * TW;
+            };
+            auto fetch = [&](long st) {
+                long r0, j0;
+                coords(first + (st / 2) * stride, r0, j0);
+                const int h = (int)(st & 1), b = (int)(st & 1);
+                // 2 pairs per 16-byte chunk: KH x TW / 2 chunks per matrix
+                for (int e = tid; e < KH * TW / 2; e += kThreads) {
+                    const int k = e / (TW / 2), q = 2 * (e % (TW / 2));
+                    const long kk = KH * h + k;
+                    cp_async16_zfill(&Wt[b][k][q], wbuf + kk * ms + r0 + q, r0 + q < m);
+                    cp_async16_zfill(&Lt[b][k][q], lbuf + kk * ms + j0 + q, j0 + q < m);
                 }
-            __syncthreads();
+                cp_async_commit_f();
+            };
             dw_acc acc[4][4];
+            long r0 = 0, j0 = 0;
+            fetch(0);
+            for (long st = 0; st < nst; ++st) {
+                const int b = (int)(st & 1);
+                if (st + 1 < nst) fetch(st + 1);
+                if ((st & 1) == 0) {
+                    // a new tile: rows r0 + tx + 16 i, columns j0 + ty + 16 j
+                    coords(first + (st / 2) * stride, r0, j0);
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+                    for (int j = 0; j < 4; ++j)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc_zero(acc[i][j]);
+                        for (int i = 0; i < 4; ++i) acc_zero(acc[i][j]);
+                }
+                if (st + 1 < nst) cp_async_wait_f<1>();
+                else cp_async_wait_f<0>();
+                __syncthreads();
 #pragma unroll 2
-            for (int k = 0; k < NB; ++k) {
-                dw w[4], l[4];
+                for (int k = 0; k < KH; ++k) {
+                    dw w[4], l[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    w[i] = Wt[k][tx + 16 * i];
-                    l[i] = Lt[k][ty + 16 * i];
+                    for (int i = 0; i < 4; ++i) {
+                        w[i] = Wt[b][k][tx + 16 * i];
+                        l[i] = Lt[b][k][ty + 16 * i];
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc_fma(acc[i][j], w[i], l[j]);
                 }
+                __syncthreads();  // the buffer is refilled by the stage after next
+                if (st & 1) {
+                    dw old[4][4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
+                    for (int j = 0; j < 4; ++j)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) acc_fma(acc[i][j], w[i], l[j]);
+                        for (int i = 0; i < 4; ++i) {
+                            const long rr = r0 + tx + 16 * i, jj = j0 + ty + 16 * j;
+                            old[i][j] = (rr < m && jj <= rr) ? a.band[(p + PW + jj) * ld + (rr - jj)] : dw_zero();
+                        }
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const long rr = r0 + tx + 16 * i, jj = j0 + ty + 16 * j;
+                            if (rr < m && jj <= rr)
+                                a.band[(p + PW + jj) * ld + (rr - jj)] = dw_sub(old[i][j], acc_value(acc[i][j]));
+                        }
+                }
             }
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const long rr = r0 + tx + 16 * i, jj = j0 + ty + 16 * j;
-                    if (rr < m && jj <= rr)
-                        a.band[(p + NB + jj) * ld + (rr - jj)] = dw_sub(old[i][j], acc_value(acc[i][j]));
-                }
-            __syncthreads();
+            __syncthreads();  // the tiles' band values are written before the caller reads them
         };
         if (blockIdx.x == 0) {
-            // tile (0,0) holds the next panel's diagonal block (rows and columns
-            // 0..31 of the window); band rows below the window, for a band
+            // tile (0,0) is the next panel's diagonal block (rows and columns
+            // 0..63 of the window); band rows below the window, for a band
             // narrower than a panel, take no update from this panel
-            if (ntiles > 0) tile(0);
-            if (p + NB < a.npad) {
-                const long pn = p + NB;
+            tiles(0, 1, ntiles > 0 ? 1 : 0);
+            if (p + PW < a.npad) {
+                const long pn = p + PW;
                 load_block(a, pn, A);
-                ldlt32_dw(A, di);
+                ldlt_block_dw(A, di);
                 record_block(a, pn, A, di);
-                for (int e = tid; e < NB * NB; e += kThreads) a.look[e] = A[e / NB][e % NB];
-                if (tid < NB) a.look[NB * NB + tid] = di[tid];
+                for (int e = tid; e < PW * PW; e += kThreads) a.look[e] = A[e / PW][e % PW];
+                if (tid < PW) a.look[PW * PW + tid] = di[tid];
             }
-            if (G == 1)
-                for (long t = 1; t < ntiles; ++t) tile(t);
+            if (G == 1) tiles(1, 1, ntiles);
         } else {
-            for (long t = blockIdx.x; t < ntiles; t += G - 1) tile(t);
+            tiles(blockIdx.x, G - 1, ntiles);
         }
         if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
     }
@@ -554,7 +618,18 @@ void band_dw_alloc(BandFactor &f)
     const size_t inv = sizeof(dw) * (size_t)(npad / SB) * kBlockElems;
     CB_CUDA_DW(cudaMalloc(&f.linv, inv));
     CB_CUDA_DW(cudaMalloc(&f.linvt, inv));
-    f.factor_grid = coop_grid(factor_dw_kernel, 2);
+    // the factor's W/L buffer (2 * 64 * bw) and look-ahead block (64 x 64 + 64)
+    const size_t wl = std::max((size_t)3 * npad, (size_t)2 * PW * (f.bw + 1) + PW);
+    CB_CUDA_DW(cudaFree(f.work));
+    CB_CUDA_DW(cudaMalloc(&f.work, sizeof(dw) * wl));
+    CB_CUDA_DW(cudaFree(f.look));
+    CB_CUDA_DW(cudaMalloc(&f.look, sizeof(dw) * (PW * PW + PW)));
+    static const bool fsmem_ok = [] {
+        return cudaFuncSetAttribute(factor_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(DwFactorSmem)) == cudaSuccess;
+    }();
+    if (!fsmem_ok) throw std::runtime_error("the double-word factor needs 97 KB of shared memory per CTA");
+    f.factor_grid = coop_grid(factor_dw_kernel, 1, sizeof(DwFactorSmem));
     static const bool smem_ok = [] {
         return cudaFuncSetAttribute(solve_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kSolveSmem) == cudaSuccess;
@@ -594,7 +669,7 @@ void band_dw_factor(BandFactor &f, cudaStream_t st, long *launches)
                    f.max_polls};
     void *args[] = {&a};
     CB_CUDA_DW(cudaLaunchCooperativeKernel((const void *)factor_dw_kernel, dim3((unsigned)grid), dim3(kThreads),
-                                           args, 0, st));
+                                           args, sizeof(DwFactorSmem), st));
     inv_block_kernel<<<(unsigned)(npad / SB), kThreads, 0, st>>>(band, f.ld, f.bw, (dw *)f.linv, (dw *)f.linvt);
     CB_CUDA_DW(cudaGetLastError());
     *launches += 2;

@@ -96,17 +96,24 @@ __device__ __forceinline__ void acc_zero(dw_acc &a)
     a.c = 0.0f;
 }
 
-// a += x * y
+// a += x * y. Every operation is a fused multiply-add: a sum u + v is formed
+// as fma(u, 1, v) and a difference u - v as fma(v, -1, u), which round
+// exactly as the add does, so the products, Knuth's two-sum and the error
+// terms all issue as FFMA.
 __device__ __forceinline__ void acc_fma(dw_acc &a, dw x, dw y)
 {
-    const float p = __fmul_rn(x.hi, y.hi);
+    const float p = __fmaf_rn(x.hi, y.hi, -0.0f);
     float e = __fmaf_rn(x.hi, y.hi, -p);
     e = __fmaf_rn(x.hi, y.lo, e);
     e = __fmaf_rn(x.lo, y.hi, e);
-    float s, t;
-    two_sum(a.s, p, s, t);
+    const float s = __fmaf_rn(a.s, 1.0f, p);
+    const float bb = __fmaf_rn(a.s, -1.0f, s);   // s - a.s
+    const float t1 = __fmaf_rn(bb, -1.0f, s);    // s - bb
+    const float t2 = __fmaf_rn(t1, -1.0f, a.s);  // a.s - t1
+    const float t3 = __fmaf_rn(bb, -1.0f, p);    // p - bb
+    const float t = __fmaf_rn(t2, 1.0f, t3);
     a.s = s;
-    a.c = __fadd_rn(a.c, __fadd_rn(t, e));
+    a.c = __fmaf_rn(a.c, 1.0f, __fmaf_rn(t, 1.0f, e));
 }
 
 __device__ __forceinline__ dw acc_value(const dw_acc &a)

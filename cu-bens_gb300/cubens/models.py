@@ -184,8 +184,12 @@ def cylindrical_panel(n: int = 64, seed: int | None = None, imperfection: float 
                       load: float = -1.0, controls: MsalControls | None = None,
                       radius: float = PANEL_R, length: float = PANEL_L,
                       theta: float = PANEL_THETA, thick: float = PANEL_T,
-                      emod: float = PANEL_E, nu: float = PANEL_NU) -> ModelSpec:
+                      emod: float = PANEL_E, nu: float = PANEL_NU, n_axial: int | None = None) -> ModelSpec:
     """Hinged cylindrical DKT shell panel on an n x n quad grid (2 n^2 triangles).
+
+    With ``n_axial`` the grid has n_axial divisions along the axis and n
+    around it (the band of the equations, set by the n + 1 joints of an
+    axial station, stays that of the n x n panel).
 
     Joints are (x_i, R sin a_j, R cos a_j - R) with x_i = L i/n along the axis and
     a_j = -theta/2 + theta j/n; joint (i, j) is number i*(n+1)+j+1. Each quad
@@ -198,9 +202,10 @@ def cylindrical_panel(n: int = 64, seed: int | None = None, imperfection: float 
     amps = np.zeros(4)
     if seed is not None and imperfection > 0:
         amps = imperfection_amplitudes(seed, imperfection)
+    na = n if n_axial is None else n_axial
     nodes = []
-    for i in range(n + 1):
-        x = length * i / n
+    for i in range(na + 1):
+        x = length * i / na
         for j in range(n + 1):
             a = -theta / 2 + theta * j / n
             w = 0.0
@@ -213,17 +218,17 @@ def cylindrical_panel(n: int = 64, seed: int | None = None, imperfection: float 
         return i * (n + 1) + j + 1
 
     tris = []
-    for i in range(n):
+    for i in range(na):
         for j in range(n):
             a, b, c, d = idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)
             tris.append((a, b, c))
             tris.append((a, c, d))
     cons = []
-    for i in range(n + 1):
+    for i in range(na + 1):
         for j in (0, n):
             for dr in (1, 2, 3):
                 cons.append(f"{idx(i, j)},{dr}")
-    centre = idx(n // 2, n // 2)
+    centre = idx(na // 2, n // 2)
     if controls is None:
         controls = MsalControls(joint=centre, direction=3, dk=-0.5)
     out = ["2", _alg(controls), "0", "1", str(len(nodes)), f"0,0,{len(tris)},0,0"]
