@@ -19,12 +19,14 @@
 // gradients as per-chunk partials summed in chunk order), so training is
 // bit-reproducible. The edge messages are recomputed in the backward pass
 // from the node arrays (P, Q, c), so nothing per edge is stored.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
+#include <stdexcept>
 #include <vector>
 
 #include "internal.hpp"
@@ -163,59 +165,104 @@ struct DenseArgs {
     const KrylovCtl *ctl;
 };
 
-constexpr int kDenseNodes = 32;
+// The dense products run on the tensor cores: BF16 operands (the float32
+// activations and weights rounded to nearest), FP32 accumulation, with
+// mma.sync.m16n8k16 (row-major A, column-major B).
+__device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                         unsigned b0, unsigned b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
 
-// 32 nodes per block; X tile and W (as [k][o]) staged in shared memory; each
-// thread computes O/8 outputs of one node (fixed k order).
-__global__ void mp_dense_kernel(DenseArgs a)
+__device__ __forceinline__ unsigned ld_pair(const __nv_bfloat16 *p) { return *(const unsigned *)p; }
+
+constexpr int kTcNodes = 64;    // nodes per CTA of the dense kernel: 4 warps x 16 rows
+constexpr int kTcThreads = 128;
+
+// Y = act(sum_t X_t W_t^T + bias) (+ res) for 64 nodes per CTA: X and W in
+// shared memory as BF16 (K padded to a multiple of 16, O to NT * 8), warp w
+// computes rows 16 w .. 16 w + 15 and all NT column tiles.
+template <int NT>
+__global__ void __launch_bounds__(kTcThreads) mp_dense_tc_kernel(DenseArgs a, int Kp)
 {
     if (a.ctl && a.ctl->done) return;
-    extern __shared__ float sm[];
-    const int O = a.O;
-    int Ktot = 0;
-    for (int t = 0; t < a.nin; ++t) Ktot += a.in[t].K;
-    float *Ws = sm;                      // [Ktot][O]
-    float *Xs = sm + (size_t)Ktot * O;   // [32][Ktot]
-    const long n0 = blockIdx.x * (long)kDenseNodes;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    const int ldx = Kp + 8;  // row stride (bf16): 16-byte rows, conflict-free fragment loads
+    __nv_bfloat16 *Xs = (__nv_bfloat16 *)dsm;           // [64][ldx]
+    __nv_bfloat16 *Ws = Xs + kTcNodes * ldx;            // [NT*8][ldx]
+    const int O = a.O, tid = threadIdx.x;
+    const long n0 = blockIdx.x * (long)kTcNodes;
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
     int kb = 0;
     for (int t = 0; t < a.nin; ++t) {
         const DenseIn &in = a.in[t];
-        for (int e = threadIdx.x; e < in.K * O; e += blockDim.x) {
-            const int k = e / O, o = e % O;
-            Ws[(kb + k) * O + o] = in.trans ? in.W[(size_t)k * O + o] : in.W[(size_t)o * in.K + k];
-        }
-        for (int e = threadIdx.x; e < kDenseNodes * in.K; e += blockDim.x) {
+        for (int e = tid; e < kTcNodes * in.K; e += kTcThreads) {
             const int r = e / in.K, k = e % in.K;
             const long node = n0 + r;
-            Xs[r * Ktot + kb + k] = node < a.n ? in.X[node * in.K + k] : 0.f;
+            Xs[r * ldx + kb + k] = __float2bfloat16_rn(node < a.n ? in.X[node * in.K + k] : 0.f);
+        }
+        for (int e = tid; e < O * in.K; e += kTcThreads) {
+            const int o = e / in.K, k = e % in.K;
+            Ws[o * ldx + kb + k] = __float2bfloat16_rn(in.trans ? in.W[(size_t)k * O + o] : in.W[(size_t)o * in.K + k]);
         }
         kb += in.K;
     }
-    __syncthreads();
-    const int r = threadIdx.x >> 3, og = threadIdx.x & 7;  // node row, output group
-    const long node = n0 + r;
-    if (node >= a.n) return;
-    for (int o = og; o < O; o += 8) {
-        float acc = a.bias ? a.bias[o] : 0.f;
-        for (int k = 0; k < Ktot; ++k) acc = fmaf(Xs[r * Ktot + k], Ws[k * O + o], acc);
-        if (a.relu) acc = fmaxf(acc, 0.f);
-        if (a.Yres) {
-            a.Y[node * O + o] = acc;
-            a.Yres[node * O + o] = acc + a.res[node * O + o];
-            continue;
-        }
-        if (a.res) acc += a.res[node * O + o];
-        float *y = a.Y + node * O + o;
-        *y = a.accum ? *y + acc : acc;
+    for (int e = tid; e < kTcNodes * (Kp - kb); e += kTcThreads) Xs[(e / (Kp - kb)) * ldx + kb + e % (Kp - kb)] = zero;
+    for (int e = tid; e < NT * 8 * Kp; e += kTcThreads) {
+        const int o = e / Kp, k = e % Kp;
+        if (o >= O || k >= kb) Ws[o * ldx + k] = zero;
     }
+    __syncthreads();
+    const int warp = tid / 32, lane = tid % 32, g = lane >> 2, q = lane & 3;
+    float acc[NT][4];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const __nv_bfloat16 *xr0 = Xs + (16 * warp + g) * ldx, *xr1 = xr0 + 8 * ldx;
+    for (int k0 = 0; k0 < Kp; k0 += 16) {
+        const unsigned a0 = ld_pair(xr0 + k0 + 2 * q), a1 = ld_pair(xr1 + k0 + 2 * q);
+        const unsigned a2 = ld_pair(xr0 + k0 + 8 + 2 * q), a3 = ld_pair(xr1 + k0 + 8 + 2 * q);
+#pragma unroll
+        for (int j = 0; j < NT; ++j) {
+            const __nv_bfloat16 *wr = Ws + (8 * j + g) * ldx + k0 + 2 * q;
+            mma_bf16(acc[j], a0, a1, a2, a3, ld_pair(wr), ld_pair(wr + 8));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const long node = n0 + 16 * warp + g + (e >= 2 ? 8 : 0);
+            const int o = 8 * j + 2 * q + (e & 1);
+            if (node >= a.n || o >= O) continue;
+            float v = acc[j][e] + (a.bias ? a.bias[o] : 0.f);
+            if (a.relu) v = fmaxf(v, 0.f);
+            if (a.Yres) {
+                a.Y[node * O + o] = v;
+                a.Yres[node * O + o] = v + a.res[node * O + o];
+                continue;
+            }
+            if (a.res) v += a.res[node * O + o];
+            float *y = a.Y + node * O + o;
+            *y = a.accum ? *y + v : v;
+        }
 }
+
+size_t dense_smem(int Kp, int NT) { return sizeof(__nv_bfloat16) * (size_t)(kTcNodes + NT * 8) * (Kp + 8); }
 
 void dense(const DenseArgs &a, cudaStream_t st)
 {
     int Ktot = 0;
     for (int t = 0; t < a.nin; ++t) Ktot += a.in[t].K;
-    const size_t smem = sizeof(float) * ((size_t)Ktot * a.O + (size_t)kDenseNodes * Ktot);
-    mp_dense_kernel<<<(unsigned)((a.n + kDenseNodes - 1) / kDenseNodes), kT, smem, st>>>(a);
+    const int Kp = (Ktot + 15) / 16 * 16;
+    const unsigned grid = (unsigned)((a.n + kTcNodes - 1) / kTcNodes);
+    if (a.O <= 64)
+        mp_dense_tc_kernel<8><<<grid, kTcThreads, dense_smem(Kp, 8), st>>>(a, Kp);
+    else
+        mp_dense_tc_kernel<16><<<grid, kTcThreads, dense_smem(Kp, 16), st>>>(a, Kp);
 }
 
 // ---- edge aggregation: a_i = mean_j relu(P_i + Q_j + c) ----
@@ -362,46 +409,65 @@ __global__ void mp_mask_kernel(const float *__restrict__ dh, const float *__rest
 
 // ---- weight gradients: dW[o][k] = sum_n dZ[n][o] X[n][k], db[o] = sum_n dZ[n][o] ----
 
-// per chunk of kWChunk nodes: part[blk][o*(K+1) + k] (k == K: the bias sum)
-__global__ void mp_wgrad_parts_kernel(const float *__restrict__ dZ, int O, const float *__restrict__ X, int K,
-                                      float *__restrict__ part, long n)
+// per chunk of kWChunk nodes: part[blk][o*(K+1) + k] (k == K: the bias sum),
+// on the tensor cores: A = dZ^T (O x nodes), B = [X 1] (nodes x (K+1)), both
+// as BF16 in shared memory, FP32 accumulation over the chunk's 128 nodes.
+// Warp w takes row tiles w, w + 4, ... (RT of them) and all NT column tiles.
+template <int RT, int NT>
+__global__ void __launch_bounds__(kTcThreads) mp_wgrad_tc_kernel(const float *__restrict__ dZ, int O,
+                                                                 const float *__restrict__ X, int K,
+                                                                 float *__restrict__ part, long n)
 {
-    __shared__ float dzs[32][128];
-    __shared__ float xs[32][65];
+    constexpr int kSub = 64;          // nodes staged at a time
+    constexpr int kld = kSub + 8;     // row stride (bf16) over those nodes
+    __shared__ __align__(16) __nv_bfloat16 As[4 * RT * 16][kld];  // [o][node]
+    __shared__ __align__(16) __nv_bfloat16 Bs[NT * 8][kld];       // [k][node]
+    const int tid = threadIdx.x;
     const long c0 = blockIdx.x * (long)kWChunk;
     const int KK = K + 1, tot = O * KK;
-    float acc[33];
+    const int warp = tid / 32, lane = tid % 32, g = lane >> 2, q = lane & 3;
+    float acc[RT][NT][4];
 #pragma unroll
-    for (int u = 0; u < 33; ++u) acc[u] = 0.f;
-    for (int s = 0; s < kWChunk; s += 32) {
-        for (int e = threadIdx.x; e < 32 * O; e += blockDim.x) {
-            const int r = e / O, o = e % O;
-            const long node = c0 + s + r;
-            dzs[r][o] = node < n ? dZ[node * O + o] : 0.f;
+    for (int i = 0; i < RT; ++i)
+#pragma unroll
+        for (int j = 0; j < NT; ++j) acc[i][j][0] = acc[i][j][1] = acc[i][j][2] = acc[i][j][3] = 0.f;
+    for (int s0 = 0; s0 < kWChunk; s0 += kSub) {
+        for (int e = tid; e < 4 * RT * 16 * kSub; e += kTcThreads) {
+            const int o = e / kSub, r = e % kSub;
+            const long node = c0 + s0 + r;
+            As[o][r] = __float2bfloat16_rn((o < O && node < n) ? dZ[node * O + o] : 0.f);
         }
-        for (int e = threadIdx.x; e < 32 * KK; e += blockDim.x) {
-            const int r = e / KK, k = e % KK;
-            const long node = c0 + s + r;
-            xs[r][k] = node < n ? (k < K ? X[node * K + k] : 1.f) : 0.f;
+        for (int e = tid; e < NT * 8 * kSub; e += kTcThreads) {
+            const int k = e / kSub, r = e % kSub;
+            const long node = c0 + s0 + r;
+            const float v = node < n ? (k < K ? X[node * K + k] : (k == K ? 1.f : 0.f)) : 0.f;
+            Bs[k][r] = __float2bfloat16_rn(v);
         }
         __syncthreads();
+        for (int k0 = 0; k0 < kSub; k0 += 16) {
 #pragma unroll
-        for (int u = 0; u < 33; ++u) {
-            const int idx = threadIdx.x + u * kT;
-            if (idx < tot) {
-                const int o = idx / KK, k = idx % KK;
-                float a = acc[u];
-                for (int r = 0; r < 32; ++r) a = fmaf(dzs[r][o], xs[r][k], a);
-                acc[u] = a;
+            for (int i = 0; i < RT; ++i) {
+                const int row = 16 * (warp + 4 * i) + g;
+                const unsigned a0 = ld_pair(&As[row][k0 + 2 * q]), a1 = ld_pair(&As[row + 8][k0 + 2 * q]);
+                const unsigned a2 = ld_pair(&As[row][k0 + 8 + 2 * q]), a3 = ld_pair(&As[row + 8][k0 + 8 + 2 * q]);
+#pragma unroll
+                for (int j = 0; j < NT; ++j)
+                    mma_bf16(acc[i][j], a0, a1, a2, a3, ld_pair(&Bs[8 * j + g][k0 + 2 * q]),
+                             ld_pair(&Bs[8 * j + g][k0 + 8 + 2 * q]));
             }
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int u = 0; u < 33; ++u) {
-        const int idx = threadIdx.x + u * kT;
-        if (idx < tot) part[(size_t)blockIdx.x * tot + idx] = acc[u];
-    }
+    for (int i = 0; i < RT; ++i)
+#pragma unroll
+        for (int j = 0; j < NT; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int o = 16 * (warp + 4 * i) + g + (e >= 2 ? 8 : 0);
+                const int k = 8 * j + 2 * q + (e & 1);
+                if (o < O && k < KK) part[(size_t)blockIdx.x * tot + o * KK + k] = acc[i][j][e];
+            }
 }
 
 // grad += sum over chunks (in chunk order); bias sums for the first nbias outputs
@@ -583,7 +649,10 @@ void wgrad(Mpnn &mp, const float *dZ, int O, const float *X, int K, float *gW, f
            cudaStream_t st)
 {
     const int nparts = (int)((mp.nj + kWChunk - 1) / kWChunk);
-    mp_wgrad_parts_kernel<<<nparts, kT, 0, st>>>(dZ, O, X, K, mp.wpart, mp.nj);
+    // O <= 64: one row tile per warp; O = 128: two. K + 1 <= 72 (nine column tiles) or <= 16
+    if (K + 1 <= 16) mp_wgrad_tc_kernel<1, 2><<<nparts, kTcThreads, 0, st>>>(dZ, O, X, K, mp.wpart, mp.nj);
+    else if (O <= 64) mp_wgrad_tc_kernel<1, 9><<<nparts, kTcThreads, 0, st>>>(dZ, O, X, K, mp.wpart, mp.nj);
+    else mp_wgrad_tc_kernel<2, 9><<<nparts, kTcThreads, 0, st>>>(dZ, O, X, K, mp.wpart, mp.nj);
     mp_wgrad_reduce_kernel<<<nb((long)O * (K + 1)), kT, 0, st>>>(mp.wpart, nparts, O, K, gW, gb, nbias);
 }
 
@@ -666,6 +735,13 @@ void adam_step(Mpnn &mp, cudaStream_t st)
 
 Mpnn *mpnn_create(const HostModel &h, unsigned seed, int capacity, cudaStream_t st)
 {
+    static const bool smem_ok = [] {
+        return cudaFuncSetAttribute(mp_dense_tc_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)dense_smem(128, 8)) == cudaSuccess &&
+               cudaFuncSetAttribute(mp_dense_tc_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)dense_smem(128, 16)) == cudaSuccess;
+    }();
+    if (!smem_ok) throw std::runtime_error("the network's dense kernel needs 52 KB of shared memory per CTA");
     Mpnn *mp = new Mpnn();
     std::vector<int> node_eq, ptr, adj;
     build_joint_graph(h, node_eq, ptr, adj);

@@ -115,26 +115,42 @@ def _rms(v):
     return float(np.sqrt(np.mean(v * v)))
 
 
-def forward(theta, g: Graph, r, p):
-    """Returns z and the saved activations."""
+def bf16(x):
+    """x rounded as the GPU rounds a float32 operand of its BF16 tensor-core
+    products: to float32 first, then to the nearest bfloat16 (ties to even)."""
+    f = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+    u = f.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _ident(x):
+    return x
+
+
+def forward(theta, g: Graph, r, p, bf=False):
+    """Returns z and the saved activations. With bf, the operands of the
+    dense products (not the decoder's) are rounded as the GPU's BF16
+    tensor-core layers round them."""
+    q = bf16 if bf else _ident
     P = unpack(theta.astype(np.float64))
     sr, sp = _rms(r), _rms(p)
     if sr == 0 or sp == 0:
         return p.copy(), None
     x = np.concatenate([_gather(g, r) / sr, _gather(g, p) / sp], axis=1)
-    S = x @ P["W0"].T + P["b0"]
+    S = q(x) @ q(P["W0"]).T + P["b0"]
     h = np.maximum(S, 0)
     cache = dict(x=x, S=S, sp=sp, layers=[])
     for l in range(LAYERS):
-        Pn = h @ P[f"A{l}"].T
-        Qn = h @ P[f"B{l}"].T
+        Pn = q(h) @ q(P[f"A{l}"]).T
+        Qn = q(h) @ q(P[f"B{l}"]).T
         pre = Pn[g.src] + Qn[g.adj] + P[f"c{l}"]
         msg = np.maximum(pre, 0)
         a = np.zeros_like(h)
         np.add.at(a, g.src, msg)
         deg = np.maximum(g.deg, 1)[:, None]
         a = a / deg
-        T = h @ P[f"U{l}"].T + a @ P[f"V{l}"].T + P[f"d{l}"]
+        T = q(h) @ q(P[f"U{l}"]).T + q(a) @ q(P[f"V{l}"]).T + P[f"d{l}"]
         cache["layers"].append(dict(h=h, pre=pre, a=a, T=T))
         h = h + np.maximum(T, 0)
     y = h @ P["Wd"].T + P["bd"]
@@ -145,10 +161,14 @@ def forward(theta, g: Graph, r, p):
     return z, cache
 
 
-def loss_and_grad(theta, g: Graph, b, t, p):
-    """Loss |P(b) - t|^2 / |t|^2 and its gradient (float64)."""
+def loss_and_grad(theta, g: Graph, b, t, p, bf=False):
+    """Loss |P(b) - t|^2 / |t|^2 and its gradient (float64); with bf the
+    operands of every product the GPU forms on its BF16 tensor cores (dense
+    layers forward and backward, weight and bias gradients) are rounded as
+    it rounds them."""
+    q = bf16 if bf else _ident
     P = unpack(theta.astype(np.float64))
-    z, c = forward(theta, g, b, p)
+    z, c = forward(theta, g, b, p, bf=bf)
     tt = float(t @ t)
     e = z - t
     L = float(e @ e) / tt
@@ -158,32 +178,32 @@ def loss_and_grad(theta, g: Graph, b, t, p):
     dz = 2 * e / tt
     dy = c["sp"] * _gather(g, dz)
     h = c["h_last"]
-    grads["Wd"] = dy.T @ h
-    grads["bd"] = dy.sum(0)
-    dh = dy @ P["Wd"]
+    grads["Wd"] = q(dy).T @ q(h)
+    grads["bd"] = q(dy).sum(0)
+    dh = q(dy) @ q(P["Wd"])
     deg = np.maximum(g.deg, 1)[:, None]
     for l in reversed(range(LAYERS)):
         L_ = c["layers"][l]
         hin, a, T, pre = L_["h"], L_["a"], L_["T"], L_["pre"]
         dT = dh * (T > 0)
-        grads[f"U{l}"] = dT.T @ hin
-        grads[f"V{l}"] = dT.T @ a
-        grads[f"d{l}"] = dT.sum(0)
-        da = dT @ P[f"V{l}"]
-        dh_in = dh + dT @ P[f"U{l}"]
+        grads[f"U{l}"] = q(dT).T @ q(hin)
+        grads[f"V{l}"] = q(dT).T @ q(a)
+        grads[f"d{l}"] = q(dT).sum(0)
+        da = q(dT) @ q(P[f"V{l}"])
+        dh_in = dh + q(dT) @ q(P[f"U{l}"])
         gm = (da / deg)[g.src] * (pre > 0)
         dPn = np.zeros_like(hin)
         np.add.at(dPn, g.src, gm)
         dQn = np.zeros_like(hin)
         np.add.at(dQn, g.adj, gm)
-        grads[f"c{l}"] = gm.sum(0)
-        grads[f"A{l}"] = dPn.T @ hin
-        grads[f"B{l}"] = dQn.T @ hin
-        dh_in += dPn @ P[f"A{l}"] + dQn @ P[f"B{l}"]
+        grads[f"c{l}"] = q(dPn).sum(0) if bf else gm.sum(0)
+        grads[f"A{l}"] = q(dPn).T @ q(hin)
+        grads[f"B{l}"] = q(dQn).T @ q(hin)
+        dh_in += q(dPn) @ q(P[f"A{l}"]) + q(dQn) @ q(P[f"B{l}"])
         dh = dh_in
     dS = dh * (c["S"] > 0)
-    grads["W0"] = dS.T @ c["x"]
-    grads["b0"] = dS.sum(0)
+    grads["W0"] = q(dS).T @ q(c["x"])
+    grads["b0"] = q(dS).sum(0)
     flat = np.concatenate([grads[name].ravel() for name, _ in layout()])
     return L, flat
 

@@ -8,9 +8,15 @@ relative residual with either preconditioner, so the Newmark path keeps the
 oracle's iteration counts and a 1e-6 relative displacement history; what the
 network changes is the Krylov work, which the last test reports.
 
-Tolerances: the network runs in float32, so its output is compared at 1e-4
-of the network's own contribution, the gradient per parameter block at 1e-3
-(relative norm), the Adam step at 1e-6 absolute (learning rate 1e-3).
+Tolerances: the dense products run on BF16 tensor cores (operands rounded
+to bfloat16, FP32 accumulation) and the CPU definition rounds the same
+operands the same way (mpnn_ref.bf16), so what remains is the float32
+arithmetic and the accumulation order, plus operands within an ulp of a
+bfloat16 rounding tie that the two sides round apart: the output is compared
+at 1e-3 of the network's own contribution, the gradient per parameter block
+at 5e-3 (relative norm), the Adam step at 1e-6 absolute (learning rate
+1e-3). Against the unrounded float64 network the output agrees to a few
+1e-2 of its contribution (bfloat16 has 8 significant bits).
 """
 import numpy as np
 import pytest
@@ -41,16 +47,18 @@ def test_network_forward_gradient_and_adam_match_the_cpu_definition():
     z, loss = m.mpnn_eval(r, p, t)
     _, grad = m.mpnn_params()
     t64 = th.astype(np.float64)
-    zr, _ = M.forward(t64, g, r, p)
-    Lr, gr = M.loss_and_grad(t64, g, r, t, p)
-    assert np.max(np.abs(z - zr)) <= 1e-4 * np.max(np.abs(zr - p))
-    assert abs(loss - Lr) <= 1e-5 * Lr
+    zr, _ = M.forward(t64, g, r, p, bf=True)
+    Lr, gr = M.loss_and_grad(t64, g, r, t, p, bf=True)
+    assert np.max(np.abs(z - zr)) <= 1e-3 * np.max(np.abs(zr - p))
+    assert abs(loss - Lr) <= 1e-4 * Lr
+    z64, _ = M.forward(t64, g, r, p)  # the unrounded network
+    assert np.max(np.abs(z - z64)) <= 5e-2 * np.max(np.abs(z64 - p))
     o = 0
     for name, shape in M.layout():
         k = int(np.prod(shape))
         ref = gr[o:o + k]
         err = np.linalg.norm(grad[o:o + k] - ref) / max(np.linalg.norm(ref), 1e-30)
-        assert err < 1e-3, (name, err)
+        assert err < 5e-3, (name, err)
         o += k
     # one Adam step from the same parameters uses the same gradient
     m.set_mpnn_params(th)
