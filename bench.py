@@ -813,6 +813,7 @@ def run_large(args, world, rank, local, pg):
     p.set_timing(False)
     tm64 = p.timers()
     p.close()
+    krylov = krylov_legs(device, args.krylov_maxit) if args.krylov_maxit > 0 else None
     if rank != 0:
         return None
     # per-increment error of the headline leg against the FP64 leg (same increments)
@@ -852,6 +853,7 @@ def run_large(args, world, rank, local, pg):
                                   "phase_ms_one_step": {k: round(v, 1) for k, v in tm64.items()
                                                         if k.startswith("ms_")}},
                    "fp32x2_over_fp64": (args.steps / (wall_ms / 1e3)) / (k64 / (wall64 / 1e3)),
+                   "fgmres_legs": krylov,
                    "phase_ms_one_step": {k: round(v, 1) for k, v in tm.items() if k.startswith("ms_")},
                    "band_ldlt_ms": ms_ldlt, "band_ldlt_fma_per_s": fma / (ms_ldlt * 1e-3),
                    "solve_ms": ms_solve, "shell_force_ms": ms_force,
@@ -878,6 +880,45 @@ def run_large(args, world, rank, local, pg):
     }
     print(json.dumps(line), flush=True)
     return line
+
+
+def krylov_legs(device: int, maxit: int):
+    """The FGMRES(50) legs on the 512 x 512 panel's first increment, with a
+    bounded Arnoldi budget per solve: nodal block-Jacobi in FP64, and the
+    learned preconditioner with the mixed-precision inner solver. Neither
+    can converge there (the DKT panel's bending makes the block-Jacobi-scaled
+    tangent's condition number grow as n^4), so each leg reports how far its
+    solves get instead of a step rate, and the learned+mixed over plain FP64
+    ratio stays undefined."""
+    import cubens
+    from cubens import models
+    n = LARGE_N
+    c = models.MsalControls(joint=n // 2 * (n + 1) + n // 2 + 1, direction=3, dk=-0.05, toldisp=1e-5,
+                            tolforc=1.0, tolener=1.0, itemax=2, submax=0)
+    text = models.cylindrical_panel(n, seed=LARGE_SEED, imperfection=LARGE_IMP, controls=c).text
+    out = {"arnoldi_limit_per_solve": maxit, "restart": 50,
+           "controls": "the config's first increment with itemax 2 (two corrector iterations) and no subdivision"}
+    for name, kw in (("fp64_block_jacobi", dict(precision=cubens.FP64)),
+                     ("mixed_learned", dict(precision=cubens.MIXED, precond=cubens.PRECOND_LEARNED))):
+        w0 = time.perf_counter()
+        m = cubens.Model(text, solver=cubens.SOLVER_FGMRES, maxit=maxit, device=device, **kw)
+        w1 = time.perf_counter()
+        try:
+            r = m.begin()
+            status = f"first increment converged in {r.iterations} iterations"
+        except cubens.CubensError as e:
+            status = f"first increment not converged ({e})"
+        w2 = time.perf_counter()
+        s = m.krylov_stats()
+        m.close()
+        out[name] = {"status": status, "create_s": round(w1 - w0, 2), "first_increment_s": round(w2 - w1, 2),
+                     "solves": s["solves"], "arnoldi_steps": s["iterations"],
+                     "inner_fp32_steps": s["inner_iterations"], "unconverged_solves": s["unconverged"],
+                     "last_solve_rel_residual": s["last_residual"],
+                     "train_steps": s["train_steps"], "train_loss": s["train_loss"],
+                     "learned_solves": s["learned_solves"]}
+    out["learned_mixed_over_plain_fp64"] = None
+    return out
 
 
 def run_reference_large(args, world, rank, pg):
@@ -919,6 +960,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2,
                     help="panel512: timed increments of the plain FP64 leg (about half a minute each)")
     ap.add_argument("--batch", type=int, default=48, help="instances of the batch workload")
+    ap.add_argument("--krylov-maxit", type=int, default=1000,
+                    help="Arnoldi steps per solve of the panel512 FGMRES legs (0: omit them)")
     args = ap.parse_args()
     if args.factor_only:
         import cubens

@@ -297,6 +297,8 @@ void krylov_setup_block_jacobi(KrylovSolver &ks, cudaStream_t st);
 // Solve A x = b to rtol (relative to |b|); returns the Arnoldi steps taken.
 int krylov_solve(KrylovSolver &ks, const double *b, double *x, cudaStream_t st, bool use_graph,
                  KrylovPrecond pc, long *launches);
+// piv = pivots of the LDL^T of every joint block's diagonal block (n values)
+void krylov_block_pivots(const KrylovSolver &ks, double *piv, cudaStream_t st);
 // y = A x (one CSR product; isolated timing)
 void krylov_spmv(const KrylovSolver &ks, const double *x, double *y, cudaStream_t st);
 // After a solve: t = z_k of the last cycle's preconditioned basis, b = A z_k

@@ -662,6 +662,45 @@ void krylov_setup_block_jacobi(KrylovSolver &ks, cudaStream_t st)
     if (ks.nested) kry_to_f32_kernel<<<nb(ks.nnz), kKT, 0, st>>>(ks.val, ks.valf, ks.nnz);
 }
 
+namespace {
+
+// piv[s0 + r] = r-th pivot of the LDL^T (no pivoting) of joint block b's
+// diagonal block of the matrix: the arc-length driver's substitute for the
+// global factor's pivots (ssd) when it solves with FGMRES
+__global__ void kry_block_pivots_kernel(const int *__restrict__ rowptr, const int *__restrict__ col,
+                                        const double *__restrict__ val, const int *__restrict__ blk_start,
+                                        double *__restrict__ piv, long nblk)
+{
+    const long b = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (b >= nblk) return;
+    const int s0 = blk_start[b], bs = blk_start[b + 1] - s0;
+    double A[8][8];
+    for (int r = 0; r < bs; ++r)
+        for (int c = 0; c < bs; ++c) A[r][c] = 0;
+    for (int r = 0; r < bs; ++r)
+        for (int k = rowptr[s0 + r]; k < rowptr[s0 + r + 1]; ++k) {
+            const int c = col[k] - s0;
+            if (c >= 0 && c < bs) A[r][c] = val[k];
+        }
+    for (int k = 0; k < bs; ++k) {
+        const double d = A[k][k];
+        piv[s0 + k] = d;
+        if (d == 0.0) continue;
+        for (int i = k + 1; i < bs; ++i) {
+            const double l = A[i][k] / d;
+            for (int j = k + 1; j <= i; ++j) A[i][j] -= l * A[j][k];
+        }
+    }
+}
+
+}  // namespace
+
+void krylov_block_pivots(const KrylovSolver &ks, double *piv, cudaStream_t st)
+{
+    kry_block_pivots_kernel<<<nb(ks.nblk, 128), 128, 0, st>>>(ks.rowptr, ks.col, ks.val, ks.blk_start, piv, ks.nblk);
+    CB_CUDA(cudaGetLastError());
+}
+
 void krylov_basis_pair(const KrylovSolver &ks, int k, double *b, double *t, cudaStream_t st)
 {
     const double *z = ks.Z + (size_t)k * ks.n;

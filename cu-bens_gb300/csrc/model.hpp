@@ -109,6 +109,10 @@ struct cb_model {
     cb_results_state *results = nullptr;  // open results*.txt files (results.cpp)
     // convergence history of the latest increment: lam, |dd|/|d|, |lam q - f|/|lam q| per iteration
     std::vector<double> iter_log;
+    // arc-length with FGMRES: pivots of the LDL^T of each joint's diagonal
+    // block (psi), and the converged increments so far (learning schedule)
+    double *bpiv = nullptr;
+    long msal_incs = 0;
 
     // timing
     bool timing = false;
@@ -211,5 +215,7 @@ void solve(cb_model *m, const double *rhs, double *x);
 cb::MsalScalars &pull_scalars(cb_model *m);
 double device_dot(cb_model *m, const double *a, const double *b, bool diff = false);
 double device_elem(cb_model *m, const double *v, long i);
+// FGMRES solve with the block-Jacobi or learned preconditioner (newmark.cu)
+void krylov_solve_learned(cb_model *m, const double *rhs, double *x, bool training);
 
 }  // namespace drv

@@ -178,6 +178,7 @@ void upload_model(cb_model *m)
             m->bytes += cb::mpnn_bytes(m->mp);
         }
         m->kel = m->alloc<double>(171 * E + 21 * T + 105 * F);
+        if (h.alg == 3) m->bpiv = m->alloc<double>(N);
         m->sc = m->alloc<cb::MsalScalars>(1);
         m->partial = m->alloc<double>(16 * cb::kRedBlocks);
         CB_CUDA(cudaMallocHost(&m->sc_h, sizeof(cb::MsalScalars)));
@@ -334,15 +335,28 @@ void assemble_tangent_t(cb_model *m, TangentState which)
         cb::launch_frame_tangent<K>(fr, conv ? fr.c_c : fr.c_ip, conv ? fr.ef_c : fr.ef_ip,
                                     conv ? fr.len_c : fr.len_ip, m->fr_lref, k + 171 * E + 21 * T, F, m->st);
     }
+    m->tm.launches += 1 + (E ? 1 : 0) + (T ? 1 : 0) + (F ? 1 : 0);
+    if (m->ks) {
+        // arc-length with FGMRES: the CSR gather, the nodal block-Jacobi
+        // inverses and the nodal blocks' pivots (psi's substitute for ssd)
+        cb::krylov_assemble(*m->ks, (const double *)k, m->st);
+        cb::krylov_setup_block_jacobi(*m->ks, m->st);
+        cb::krylov_block_pivots(*m->ks, m->bpiv, m->st);
+        m->tm.launches += 2;
+        return;
+    }
     if (bf.dw) cb::band_dw_gather(m->tmap_ptr, m->tmap_src, m->tmap_dst, (const double *)k, bf, m->tmap_n, m->st);
     else cb::launch_gather_band<K>(m->tmap_ptr, m->tmap_src, m->tmap_dst, k, (K *)bf.band, m->tmap_n, m->st);
-    m->tm.launches += 1 + (E ? 1 : 0) + (T ? 1 : 0) + (F ? 1 : 0);
 }
 
 // tangent into the band (stiff_tr + stiff_fr + stiff_sh)
 void assemble_tangent(cb_model *m, TangentState which)
 {
     PhaseTimer t(m, &m->tm.ms_tangent);
+    if (m->ks) {
+        assemble_tangent_t<double>(m, which);
+        return;
+    }
     cb::BandFactor &bf = m->bf;
     const size_t es = bf.fp32 ? 4 : 8;
     CB_CUDA(cudaMemsetAsync(bf.band, 0, es * (size_t)bf.ld * bf.nblk * bf.s, m->st));
@@ -352,6 +366,7 @@ void assemble_tangent(cb_model *m, TangentState which)
 
 void factor(cb_model *m)
 {
+    if (m->ks) return;  // FGMRES: the block-Jacobi inverses were formed with the tangent
     PhaseTimer t(m, &m->tm.ms_factor);
     cb::band_factor(m->bf, m->st, m->opt.use_graphs != 0, &m->tm.launches);
     m->tm.factorizations++;
@@ -359,6 +374,13 @@ void factor(cb_model *m)
 
 void solve(cb_model *m, const double *rhs, double *x)
 {
+    if (m->ks) {
+        // arc-length with FGMRES: the first increments train a learned
+        // preconditioner (when the handle has one), later ones use it
+        const long train = m->learn_steps >= 0 ? m->learn_steps : 5;
+        krylov_solve_learned(m, rhs, x, m->msal_incs < train);
+        return;
+    }
     PhaseTimer t(m, &m->tm.ms_solve);
     cb::band_solve(m->bf, rhs, x, m->st, m->opt.use_graphs != 0, &m->tm.launches);
     m->tm.solves++;
@@ -410,6 +432,10 @@ double device_elem(cb_model *m, const double *v, long i)
 namespace {
 
 using namespace drv;
+
+// The pivots psi compares step to step: the band factor's (skyfact's ssd),
+// or with FGMRES those of the joints' diagonal blocks.
+const double *pivots(cb_model *m) { return m->ks ? m->bpiv : m->bf.ssd; }
 
 // Push the host-side scalars the device kernels read.
 void push_scalars(cb_model *m, double lam_t, double a, double intener1)
@@ -463,7 +489,7 @@ void msal_begin(cb_model *m, cb_step *out)
     assemble_tangent(m);
     factor(m);
     solve(m, m->q, m->ddq);
-    d2d(m->ssd_o, m->bf.ssd, N, st);
+    d2d(m->ssd_o, pivots(m), N, st);
     double ddq_k = device_elem(m, m->ddq, h.dkdof);
     double lpf = h.dk / ddq_k;
     // d = dd = lpf ddq; intener1 = dd . (lpf q)
@@ -525,13 +551,14 @@ void msal_begin(cb_model *m, cb_step *out)
     m->dnormallow = h.alpha * nd;
     m->beta = std::sqrt((double)h.iteopt / (double)itecnt) * (m->dnormallow / m->dnorm);
     m->psi = 1;
-    cb::launch_psi(m->bf.ssd, m->ssd_o, m->partial, m->sc, 14, N, st);
+    cb::launch_psi(pivots(m), m->ssd_o, m->partial, m->sc, 14, N, st);
     d2h(&m->hs->val[0], &m->sc->dots[14], 1, st);
     CB_CUDA(cudaStreamSynchronize(st));
     m->psi = m->hs->val[0];
     m->errchk2 = m->subcnt = m->imagcnt = m->negcnt = 0;
     m->itecnt = itecnt;
     m->phase = 1;
+    m->msal_incs = 1;
 }
 
 // ---- one arc-length increment (main.c:2647-3134) ----
@@ -568,11 +595,19 @@ void msal_step(cb_model *m, cb_step *out)
         assemble_tangent(m);
         factor(m);
         solve(m, m->q, m->ddq);
-        int *flags = m->hs->flags;
-        d2h(flags, m->bf.flags, 2, st);
-        CB_CUDA(cudaStreamSynchronize(st));
-        if (flags[1]) throw cb_status_error(CB_ERR_NUMERIC, "singular stiffness matrix (zero pivot)");
-        const int det = flags[0];
+        int det = 0;
+        if (m->ks) {
+            // FGMRES gives no pivots: K is taken as indefinite when q . K^-1 q <= 0
+            // (the sign of the current stiffness parameter), the predictor
+            // direction that skyfact's det gives when one eigenvalue has crossed
+            det = device_dot(m, m->q, m->ddq) <= 0.0 ? 1 : 0;
+        } else {
+            int *flags = m->hs->flags;
+            d2h(flags, m->bf.flags, 2, st);
+            CB_CUDA(cudaStreamSynchronize(st));
+            if (flags[1]) throw cb_status_error(CB_ERR_NUMERIC, "singular stiffness matrix (zero pivot)");
+            det = flags[0];
+        }
         double a = m->psi >= h.psi_thresh ? m->qq + device_dot(m, m->ddq, nullptr) : device_dot(m, m->ddq, nullptr);
         double dlpf = det == 0 ? m->arc * std::sqrt(1 / a) : -m->arc * std::sqrt(1 / a);
         lam_t += dlpf;
@@ -655,7 +690,7 @@ void msal_step(cb_model *m, cb_step *out)
         out->dk = device_elem(m, m->d, h.dkdof);
         m->dkc = std::fabs(out->dk);
         m->lpfc = std::fabs(m->lpf);
-        cb::launch_psi(m->bf.ssd, m->ssd_o, m->partial, m->sc, 14, N, st);
+        cb::launch_psi(pivots(m), m->ssd_o, m->partial, m->sc, 14, N, st);
         d2h(&m->hs->val[0], &m->sc->dots[14], 1, st);
         CB_CUDA(cudaStreamSynchronize(st));
         m->psi = m->hs->val[0];
@@ -665,6 +700,7 @@ void msal_step(cb_model *m, cb_step *out)
         out->iterations = itecnt;
         out->attempts = attempts;
         out->residual = true_residual(m, m->lpf, m->f);
+        m->msal_incs++;
         return;
     }
 }
@@ -707,9 +743,8 @@ int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb
         *out = m;
         return CB_ERR_ARG;
     }
-    if (m->opt.solver == CB_SOLVER_FGMRES && m->h.alg != 5) {
-        m->err = "the FGMRES solver serves the nonlinear Newmark driver (its effective stiffness is "
-                 "mass-shifted); MSAL needs the pivots of a factorisation (det, ssd), and static "
+    if (m->opt.solver == CB_SOLVER_FGMRES && m->h.alg != 5 && m->h.alg != 3) {
+        m->err = "the FGMRES solver serves the nonlinear Newmark and arc-length drivers; static "
                  "Newton-Raphson keeps the direct solve";
         *out = m;
         return CB_ERR_UNSUPPORTED;
@@ -720,7 +755,8 @@ int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb
         return CB_ERR_ARG;
     }
     if (m->opt.precision == CB_FP32X2 && (m->opt.solver != CB_SOLVER_BAND || m->h.alg == 5)) {
-        m->err = "the double-word band serves the band solver of arc-length and Newton-Raphson models";
+        m->err = "the double-word band factor serves the band solver of arc-length and Newton-Raphson "
+                 "models (it has no FGMRES form and no Newmark driver)";
         *out = m;
         return CB_ERR_UNSUPPORTED;
     }

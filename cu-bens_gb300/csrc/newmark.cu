@@ -20,6 +20,70 @@
 #include "internal.hpp"
 #include "model.hpp"
 
+namespace drv {
+
+// K x = rhs with FGMRES on the handle's current matrix and block-Jacobi
+// preconditioner. With the learned preconditioner: while `training`, solve
+// with block-Jacobi and train the network on the solve's (rhs, x) pair and
+// three pairs from inside its last Arnoldi cycle; afterwards solve with the
+// network, capped at stall_factor times the block-Jacobi average of Arnoldi
+// steps, and redo a stalled solve with block-Jacobi.
+void krylov_solve_learned(cb_model *m, const double *rhs, double *x, bool training)
+{
+    cb::KrylovSolver &ks = *m->ks;
+    const bool graphs = m->opt.use_graphs != 0;
+    auto bj_solve = [&] {
+        PhaseTimer t(m, &m->tm.ms_solve);
+        const int it = cb::krylov_solve(ks, rhs, x, m->st, graphs, cb::KrylovPrecond::block_jacobi,
+                                        &m->tm.launches);
+        m->tm.solves++;
+        return it;
+    };
+    if (!m->mp) {
+        bj_solve();
+        return;
+    }
+    if (training) {
+        // the block-Jacobi work per solve: Arnoldi steps, inner ones included
+        const long inner0 = ks.inner_iterations;
+        m->bj_iters += bj_solve() + (ks.inner_iterations - inner0);
+        m->bj_solves++;
+        PhaseTimer t(m, &m->tm.ms_train);
+        // the solve's own pair and three from inside its last Arnoldi cycle
+        // (the vectors the preconditioner is applied to)
+        cb::mpnn_push_pair(*m->mp, rhs, x, m->st);
+        const int nc = ks.ctl_h->ncols;
+        for (int k : {0, nc / 2, nc - 1}) {
+            if (k < 0 || nc <= 0) continue;
+            double *b = nullptr, *tt = nullptr;
+            cb::mpnn_slot(*m->mp, &b, &tt);
+            cb::krylov_basis_pair(ks, k, b, tt, m->st);
+            cb::mpnn_commit_pair(*m->mp);
+        }
+        cb::mpnn_train(*m->mp, ks, m->learn_adam, m->st);
+        return;
+    }
+    const double avg = m->bj_solves ? (double)m->bj_iters / (double)m->bj_solves : (double)ks.maxit;
+    const int cap = std::max(10, (int)(m->learn_stall * avg));
+    const int saved = ks.maxit;
+    ks.maxit = std::min(cap, saved);
+    {
+        PhaseTimer t(m, &m->tm.ms_solve);
+        cb::krylov_solve(ks, rhs, x, m->st, graphs, cb::KrylovPrecond::learned, &m->tm.launches);
+        m->tm.solves++;
+    }
+    ks.maxit = saved;
+    m->learned_solves++;
+    if (ks.ctl_h->status == 1) {
+        // stalled: the unconverged count is the fallback's business
+        ks.unconverged--;
+        m->fallbacks++;
+        bj_solve();
+    }
+}
+
+}  // namespace drv
+
 namespace {
 
 using namespace drv;
@@ -85,10 +149,8 @@ void newmark_begin(cb_model *m)
 }
 
 // Keff dd = Reff with FGMRES: the preconditioner from the current matrix,
-// then the solve (m->r -> m->dd).
-// With the learned preconditioner: the first time steps solve with
-// block-Jacobi and train the network on each solve's (Reff, dd) pair; later
-// solves use the network and fall back to block-Jacobi when one stalls.
+// then the solve (m->r -> m->dd). With the learned preconditioner the first
+// time steps train the network (drv::krylov_solve_learned).
 void krylov_newmark_solve(cb_model *m)
 {
     cb::KrylovSolver &ks = *m->ks;
@@ -98,56 +160,8 @@ void krylov_newmark_solve(cb_model *m)
         m->tm.launches += 1;
         m->tm.factorizations++;
     }
-    const bool graphs = m->opt.use_graphs != 0;
-    auto bj_solve = [&] {
-        PhaseTimer t(m, &m->tm.ms_solve);
-        const int it = cb::krylov_solve(ks, m->r, m->dd, m->st, graphs, cb::KrylovPrecond::block_jacobi,
-                                        &m->tm.launches);
-        m->tm.solves++;
-        return it;
-    };
-    if (!m->mp) {
-        bj_solve();
-        return;
-    }
     const long train = m->learn_steps >= 0 ? m->learn_steps : std::max(1L, m->h.nsteps / 10);
-    if (m->nm_k < train) {
-        // the block-Jacobi work per solve: Arnoldi steps, inner ones included
-        const long inner0 = ks.inner_iterations;
-        m->bj_iters += bj_solve() + (ks.inner_iterations - inner0);
-        m->bj_solves++;
-        PhaseTimer t(m, &m->tm.ms_train);
-        // the solve's own pair and three from inside its last Arnoldi cycle
-        // (the vectors the preconditioner is applied to)
-        cb::mpnn_push_pair(*m->mp, m->r, m->dd, m->st);
-        const int nc = ks.ctl_h->ncols;
-        for (int k : {0, nc / 2, nc - 1}) {
-            if (k < 0 || nc <= 0) continue;
-            double *b = nullptr, *tt = nullptr;
-            cb::mpnn_slot(*m->mp, &b, &tt);
-            cb::krylov_basis_pair(ks, k, b, tt, m->st);
-            cb::mpnn_commit_pair(*m->mp);
-        }
-        cb::mpnn_train(*m->mp, ks, m->learn_adam, m->st);
-        return;
-    }
-    const double avg = m->bj_solves ? (double)m->bj_iters / (double)m->bj_solves : (double)ks.maxit;
-    const int cap = std::max(10, (int)(m->learn_stall * avg));
-    const int saved = ks.maxit;
-    ks.maxit = std::min(cap, saved);
-    {
-        PhaseTimer t(m, &m->tm.ms_solve);
-        cb::krylov_solve(ks, m->r, m->dd, m->st, graphs, cb::KrylovPrecond::learned, &m->tm.launches);
-        m->tm.solves++;
-    }
-    ks.maxit = saved;
-    m->learned_solves++;
-    if (ks.ctl_h->status == 1) {
-        // stalled: the unconverged count is the fallback's business
-        ks.unconverged--;
-        m->fallbacks++;
-        bj_solve();
-    }
+    krylov_solve_learned(m, m->r, m->dd, m->nm_k < train);
 }
 
 // one Newton iteration of main.c:3543-3745; returns the scalar block

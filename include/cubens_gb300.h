@@ -59,7 +59,9 @@ enum cb_solver {
     CB_SOLVER_BAND = 0,   /* band LDL^T in the reference's equation order (skyfact/skysolve's
                              result; pivots give det and ssd) */
     CB_SOLVER_FGMRES = 1  /* FGMRES(m) with a nodal block-Jacobi preconditioner over a CSR
-                             product (nonlinear Newmark only: MSAL needs det and ssd). In
+                             product, for nonlinear Newmark and MSAL models (not for static
+                             Newton-Raphson). MSAL takes det from the sign of q . K^-1 q and
+                             psi from the pivots of the joints' diagonal blocks. In
                              CB_MIXED precision each FP64 Arnoldi step is preconditioned by
                              an FP32 FGMRES(30) solve to 1e-4 with FP32 matrix and blocks */
 };
@@ -209,13 +211,14 @@ int cb_set_krylov_tolerance(cb_model *m, double rtol);
 int cb_get_krylov_stats(const cb_model *m, cb_krylov_stats *s);
 
 /* Learned preconditioner (solver CB_SOLVER_FGMRES, precond CB_PRECOND_LEARNED).
- * Online schedule: the time steps k < train_steps solve with block-Jacobi
- * and store each solve's (effective residual, FP64 correction) pair; after
+ * Online schedule: the time steps (MSAL: arc-length increments) k <
+ * train_steps solve with block-Jacobi and store each solve's (right-hand
+ * side, FP64 solution) pair; after
  * each such solve the network takes adam_per_solve Adam steps (learning rate
  * lr) on the stored pairs. Later solves use the network; one that has not
  * converged after stall_factor times the block-Jacobi average of Arnoldi
  * steps (at least 10) is redone with block-Jacobi. train_steps < 0 keeps the
- * default (a tenth of the time steps, at least one). */
+ * default (Newmark: a tenth of the time steps, at least one; MSAL: 5). */
 int cb_set_learning(cb_model *m, int train_steps, int adam_per_solve, double lr, double stall_factor);
 /* The network itself, for checks against a CPU definition. Parameters are
  * cb_mpnn_param_count() float32 values (layout in cu-bens_gb300/csrc/mpnn.cu).

@@ -18,6 +18,8 @@ at 5e-3 (relative norm), the Adam step at 1e-6 absolute (learning rate
 1e-3). Against the unrounded float64 network the output agrees to a few
 1e-2 of its contribution (bfloat16 has 8 significant bits).
 """
+import time
+
 import numpy as np
 import pytest
 
@@ -94,15 +96,69 @@ def test_learned_preconditioner_keeps_the_newmark_path():
     assert m2.krylov_stats()["iterations"] == s["iterations"]
 
 
-def test_what_the_network_gains_over_block_jacobi(record_property):
-    """Krylov steps per solve after training, learned vs block-Jacobi (the
-    same solves to the same tolerance); recorded, and the learned run must
-    stay within its stall budget (fallbacks are counted, not hidden)."""
+def _window(m, step, first, total):
+    """Krylov work of the increments (or time steps) after the first ones:
+    Arnoldi steps per solve, solves, learned solves, fallbacks, wall seconds."""
+    for _ in range(first):
+        step()
+    s0 = m.krylov_stats()
+    t0 = time.perf_counter()
+    for _ in range(total - first):
+        step()
+    sec = time.perf_counter() - t0
+    s1 = m.krylov_stats()
+    d = {k: s1[k] - s0[k] for k in ("solves", "iterations", "learned_solves", "fallbacks")}
+    d["per_solve"] = d["iterations"] / d["solves"]
+    d["seconds"] = sec
+    return d
+
+
+def _arc_length(text, learned):
+    kw = dict(precond=cubens.PRECOND_LEARNED) if learned else {}
+    m = cubens.Model(text, solver=cubens.SOLVER_FGMRES, **kw)
+    if learned:
+        m.set_learning(train_steps=10, adam_per_solve=32, lr=1e-3, stall_factor=2.0)
+    m.begin()
+    return m, _window(m, m.step, 9, 39)
+
+
+def test_what_the_network_gains_over_block_jacobi(golden_dir, record_property):
+    """What the trained network does to FGMRES against block-Jacobi alone, on
+    the same solves to the same 1e-12 tolerance: the config-1 space truss on
+    the arc-length path (trained on its first 10 increments, applied on the
+    next 30) and the frame building on the Newmark path (trained on 20 time
+    steps, applied on 20). Measured on GB300: the network does not gain on
+    either. Truss: 179 Arnoldi steps per solve against 118 (1.52x), 6.7x the
+    wall time, training loss 0.99 (it learns almost nothing of K^-1 beyond
+    the joint blocks: the solves are dominated by the structure's smooth,
+    global modes, which a three-hop message-passing network cannot reach).
+    Newmark: 56 against 46 steps per solve (1.22x), the training loss 0.12.
+    The asserted brackets pin these figures so that a change shows; the
+    fallbacks are counted, not hidden."""
+    text = str(np.load(golden_dir / "run_truss_c1.npz")["model_def"])
+    _, bj = _arc_length(text, False)
+    ml, ln = _arc_length(text, True)
+    record_property("arc_length_block_jacobi", bj)
+    record_property("arc_length_learned", ln)
+    assert ln["solves"] == bj["solves"]                     # the same Newton path
+    assert ln["learned_solves"] == ln["solves"] and ln["fallbacks"] == 0
+    ratio = ln["per_solve"] / bj["per_solve"]
+    assert 1.2 <= ratio <= 2.0, ratio                       # measured 1.52
+    assert ln["seconds"] > 2 * bj["seconds"]                # measured 6.7x
+    assert ml.krylov_stats()["train_loss"] > 0.9            # measured 0.99
+
     spec = models.frame_building(4, 3, 6, steps=40, dt=0.005, seed=11)
-    bj, _ = _newmark(spec, 40, False)
-    ln, _ = _newmark(spec, 40, True, train=20)
-    sb, sl = bj.krylov_stats(), ln.krylov_stats()
-    record_property("bj_iterations_per_solve", sb["iterations"] / sb["solves"])
-    record_property("learned_stats", sl)
-    assert sl["learned_solves"] > 0
-    assert sl["fallbacks"] <= sl["learned_solves"]
+    nb = cubens.Model(spec.text, solver=cubens.SOLVER_FGMRES)
+    nb.newmark_begin()
+    bjn = _window(nb, nb.newmark_step, 20, 40)
+    nl, _ = _learned(spec)
+    nl.set_learning(train_steps=20, adam_per_solve=8, lr=1e-3, stall_factor=2.0)
+    nl.newmark_begin()
+    lnn = _window(nl, nl.newmark_step, 20, 40)
+    record_property("newmark_block_jacobi", bjn)
+    record_property("newmark_learned", lnn)
+    assert lnn["solves"] == bjn["solves"] and lnn["learned_solves"] == lnn["solves"]
+    ratio = lnn["per_solve"] / bjn["per_solve"]
+    assert 1.0 <= ratio <= 1.6, ratio                       # measured 1.22
+    loss = nl.krylov_stats()["train_loss"]
+    assert 0.02 < loss < 0.5, loss                          # measured 0.12
