@@ -14,6 +14,23 @@ namespace cb {
 // ---------------------------------------------------------------------------
 // Host-side model: what main() builds during setup (main.c:330-1648)
 // ---------------------------------------------------------------------------
+// Input values the solver does not use but the reference echoes to
+// results1.txt while it reads the model_def (struc model.c:381-390, prop_tr
+// truss.c:48-70, prop_fr frame.c:171-181, prop_sh shell.c:51-100, load
+// model.c:1316-1319, arc.c:52-53).
+struct InputEcho {
+    int ana = 2;
+    std::vector<int> wrp;                      // NJ warping restraint flags ("j,7,r")
+    std::vector<double> tr_dens, tr_yield;     // NE_TR
+    std::vector<double> sh_dens, sh_yield;     // NE_SH
+    std::vector<double> fr_yield;              // NE_FR*3: yield stress, plastic moduli (strong, weak)
+    std::vector<long> load_jt;                 // static joint loads in input order (1-based joints)
+    std::vector<int> load_dir;
+    std::vector<double> load_mag;
+    long dk_jt = 0;                            // MSAL initially prescribed displacement
+    int dk_dir = 0;
+};
+
 struct HostModel {
     long nj = 0, ne_tr = 0, ne_fr = 0, ne_sh = 0, neq = 0, lss = 0, bw = 0;
     std::vector<long> jcode;   // NJ*7, 1-based equation numbers, 0 = fixed
@@ -40,7 +57,13 @@ struct HostModel {
     double dk = 0, alpha = 1, psi_thresh = 0.1, lpfmax = 0, dkimax = 0;
     double toldisp = 1, tolforc = 1, tolener = 1;
     int iteopt = 6, itemax = 20, submax = 10, imagmax = 10, negmax = 10;
+    InputEcho echo;
 };
+
+// The text the reference writes to results1.txt from the start of the run to
+// the end of input processing (the input echo, main.c:386-433 through the
+// MSAL parameters).
+std::string input_echo(const HostModel &m);
 
 // Parse a model_def text; returns an empty string on success, else the reason.
 std::string parse_model_def(const char *text, size_t len, HostModel &m, int &status);
@@ -378,7 +401,7 @@ struct MsalScalars {
     int psi_ge;          // psi >= psi_thresh
     int quad_status;     // 0 ok, 2 imaginary roots, 3 both gammas <= 0 (arc.c:70-157)
     int convchk;         // misc.c:187-250
-    int test_err;        // 1 when a denominator of the test is zero
+    int test_err;        // a zero denominator: 1 displacements, 2 force increment, 3 energy increment
     double toldisp, tolforc, tolener, intener1;
     int intener_first;   // the test takes intener1 from this iteration's dd . (qtot - f_ip) (static NR)
 };

@@ -107,6 +107,10 @@ struct cb_model {
     double nm_ddt = 1;      // time increment multiplier carried between steps (main.c:3452)
 
     cb_results_state *results = nullptr;  // open results*.txt files (results.cpp)
+    // the reference's results1.txt messages of the run (its lines after the
+    // input echo), in order; the results writer appends them
+    std::vector<std::string> ofp0;
+    bool ofp0_closed = false;  // the run's closing line has been logged
     // convergence history of the latest increment: lam, |dd|/|d|, |lam q - f|/|lam q| per iteration
     std::vector<double> iter_log;
     // arc-length with FGMRES: pivots of the LDL^T of each joint's diagonal
@@ -196,6 +200,37 @@ int guarded(cb_model *m, F &&fn)
         m->err = e.what();
         return CB_ERR_CUDA;
     }
+}
+
+// A line of the reference's results1.txt messages.
+inline void ref_message(cb_model *m, const char *text) { m->ofp0.push_back(text); }
+
+// The run's successful end (main.c:2155, 3139, 3957), logged once.
+inline void ref_success(cb_model *m, const char *text)
+{
+    if (m->ofp0_closed) return;
+    m->ofp0_closed = true;
+    m->ofp0.push_back(text);
+}
+
+// A failure that ends the reference's run: its message, then closeio's
+// "Solution failed" (misc.c:474), and the status error for the caller.
+[[noreturn]] inline void fail_run(cb_model *m, int code, const std::string &msg, const char *ref)
+{
+    if (!m->ofp0_closed) {
+        m->ofp0_closed = true;
+        m->ofp0.push_back(ref);
+        m->ofp0.push_back("\nSolution failed\n");
+    }
+    throw cb_status_error(code, msg);
+}
+
+// test()'s message for a zero denominator (misc.c:200-247): 1 the
+// displacements, 2 the force increment, 3 the energy increment.
+inline const char *test_message(int err)
+{
+    return err == 1 ? "\n***ERROR*** Displacements are zero\n"
+                    : err == 2 ? "\n***ERROR*** Force increment is zero\n" : "\n***ERROR*** Energy increment is zero\n";
 }
 
 namespace drv {

@@ -65,6 +65,7 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
                "arc length) and 5 (nonlinear Newmark) are on the GPU path";
     }
     m.alg = alg;
+    m.echo.ana = ana;
     if (alg == 5) {
         (void)t.next();  // CHKPT
         int rflag = (int)t.next();
@@ -134,6 +135,7 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         if (k == 7) wrp[j - 1] = (int)t.next();
         m.jcode[(j - 1) * 7 + k - 1] = 0;
     }
+    m.echo.wrp = wrp;
     // DOFs no element type uses (model.c:267-285): truss joints keep 1-3,
     // shell joints 1-6, frame joints all 7
     for (long i = 0; i < NJ; ++i) {
@@ -221,11 +223,13 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
     for (long i = 0; i < NJ * 3; ++i) m.x0[i] = t.next();
     m.tr_e.resize(m.ne_tr);
     m.tr_a.resize(m.ne_tr);
+    m.echo.tr_dens.resize(m.ne_tr);
+    m.echo.tr_yield.resize(m.ne_tr);
     for (long i = 0; i < m.ne_tr; ++i) {
         m.tr_e[i] = t.next();
         m.tr_a[i] = t.next();
-        (void)t.next();  // density
-        (void)t.next();  // yield stress (ANAFLAG 3 only)
+        m.echo.tr_dens[i] = t.next();   // density
+        m.echo.tr_yield[i] = t.next();  // yield stress (ANAFLAG 3 only)
     }
     // frame properties (prop_fr, frame.c:43-224)
     m.fr_prop.resize(8 * F);
@@ -240,7 +244,8 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
             return "frame member end offsets are not supported";
         }
         for (long i = 0; i < F * 3; ++i) m.fr_aux[i] = t.next();
-        for (long i = 0; i < F * 3; ++i) (void)t.next();  // yield stress, plastic moduli (ANAFLAG 3)
+        m.echo.fr_yield.resize(3 * F);
+        for (long i = 0; i < F * 3; ++i) m.echo.fr_yield[i] = t.next();  // yield stress, plastic moduli
         j = (long)t.next();
         for (int k = 0; k < 4; ++k) (void)t.next();
         if (!t.ok) return "model_def ended inside the frame properties";
@@ -252,12 +257,14 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
     m.sh_e.resize(m.ne_sh);
     m.sh_nu.resize(m.ne_sh);
     m.sh_t.resize(m.ne_sh);
+    m.echo.sh_dens.resize(m.ne_sh);
+    m.echo.sh_yield.resize(m.ne_sh);
     for (long i = 0; i < m.ne_sh; ++i) {
         m.sh_e[i] = t.next();
         m.sh_nu[i] = t.next();
         m.sh_t[i] = t.next();
-        (void)t.next();
-        (void)t.next();
+        m.echo.sh_dens[i] = t.next();
+        m.echo.sh_yield[i] = t.next();
     }
     if (!t.ok) return "model_def ended inside the properties";
     m.q.assign(neq, 0.0);
@@ -339,6 +346,9 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         long k = m.jcode[(jt - 1) * 7 + dir - 1];
         if (k != 0) m.q[k - 1] = mag;
         any_load = true;
+        m.echo.load_jt.push_back(jt);
+        m.echo.load_dir.push_back((int)dir);
+        m.echo.load_mag.push_back(mag);
     }
     if (F > 0) {
         long fr = (long)t.next();
@@ -385,6 +395,8 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
     m.tolener = t.next();
     if (!t.ok) return "model_def ended inside the MSAL controls";
     if (jt < 1 || jt > NJ || dir < 1 || dir > 7) return "prescribed displacement joint out of range";
+    m.echo.dk_jt = jt;
+    m.echo.dk_dir = (int)dir;
     m.dkdof = m.jcode[(jt - 1) * 7 + dir - 1] - 1;
     if (m.dkdof < 0) return "initially prescribed displacement at fixed degree of freedom";
     status = CB_OK;

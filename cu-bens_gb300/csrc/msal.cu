@@ -520,14 +520,16 @@ void msal_begin(cb_model *m, cb_step *out)
         }
         m->tm.launches += 4;
         cb::MsalScalars &s = pull_scalars(m);
-        if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+        if (s.test_err) fail_run(m, CB_ERR_NUMERIC, "zero norm in the convergence test", test_message(s.test_err));
         log_iteration(m, s);
         lpf = s.lam_t;
         convchk = s.convchk;
         itecnt++;
         advance_iteration(m);
     } while (convchk != 0 && itecnt <= h.itemax);
-    if (convchk != 0) throw cb_status_error(CB_ERR_DIVERGED, "initially prescribed displacement too large");
+    if (convchk != 0)
+        fail_run(m, CB_ERR_DIVERGED, "initially prescribed displacement too large",
+                 "\n***ERROR*** Initially presecribed displacement too large\n");  // main.c:2520-2521
     // the first increment advances ip <- i after every iteration, converged or not
     // (main.c:2399-2428 run before the loop condition), so the newest state is in ip
     accept_state(m, true);
@@ -569,6 +571,7 @@ void msal_step(cb_model *m, cb_step *out)
     cudaStream_t st = m->st;
     out->done = 0;
     if (!(m->lpfc <= h.lpfmax && m->dkc <= h.dkimax)) {
+        ref_success(m, "\nSolution successful\n");  // main.c:3138-3140
         out->done = 1;
         out->lam = m->lpf;
         out->iterations = 0;
@@ -605,7 +608,9 @@ void msal_step(cb_model *m, cb_step *out)
             int *flags = m->hs->flags;
             d2h(flags, m->bf.flags, 2, st);
             CB_CUDA(cudaStreamSynchronize(st));
-            if (flags[1]) throw cb_status_error(CB_ERR_NUMERIC, "singular stiffness matrix (zero pivot)");
+            if (flags[1])
+                fail_run(m, CB_ERR_NUMERIC, "singular stiffness matrix (zero pivot)",
+                         "\n***ERROR*** Singular stiffness matrix\n");  // solve.c:566
             det = flags[0];
         }
         double a = m->psi >= h.psi_thresh ? m->qq + device_dot(m, m->ddq, nullptr) : device_dot(m, m->ddq, nullptr);
@@ -645,7 +650,7 @@ void msal_step(cb_model *m, cb_step *out)
             cb::MsalScalars &s = pull_scalars(m);
             int status = s.quad_status;
             if (status == 0) {
-                if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+                if (s.test_err) fail_run(m, CB_ERR_NUMERIC, "zero norm in the convergence test", test_message(s.test_err));
                 log_iteration(m, s);
                 convchk = s.convchk;
                 if (convchk == 0) {
@@ -675,7 +680,8 @@ void msal_step(cb_model *m, cb_step *out)
         } while (convchk != 0 && m->errchk2 == 0 && m->subcnt <= h.submax && m->imagcnt <= h.imagmax &&
                  m->negcnt <= h.negmax);
         if (m->subcnt > h.submax || m->imagcnt > h.imagmax || m->negcnt > h.negmax)
-            throw cb_status_error(CB_ERR_DIVERGED, "maximum allowable number of subdivisions exceeded");
+            fail_run(m, CB_ERR_DIVERGED, "maximum allowable number of subdivisions exceeded",
+                     "\n***ERROR*** Maximum allowable number of subdivisions exceeded\n");  // main.c:3041-3042
         if (m->errchk2 != 0) continue;
         // accept (main.c:3045-3133)
         cb::MsalScalars &s = *m->sc_h;

@@ -272,6 +272,7 @@ void newmark_step(cb_model *m, cb_step *out)
     cudaStream_t st = m->st;
     out->done = 0;
     if (m->nm_k >= h.nsteps) {
+        ref_success(m, "\nSolution successful!!\n");  // main.c:3956-3958
         out->done = 1;
         out->lam = (double)(h.nsteps - 1) * h.dt;
         out->iterations = 0;
@@ -312,7 +313,7 @@ void newmark_step(cb_model *m, cb_step *out)
             itecnt = 0;
             do {
                 cb::MsalScalars &s = newmark_iteration(m, p, k, sub_dt, lpf, itecnt, a0, a2, a3, a6, a7);
-                if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+                if (s.test_err) fail_run(m, CB_ERR_NUMERIC, "zero norm in the convergence test", test_message(s.test_err));
                 convchk = s.convchk;
                 res_num = s.dots[2];
                 res_den = s.dots[6];
@@ -320,14 +321,23 @@ void newmark_step(cb_model *m, cb_step *out)
                 itecnt++;
             } while (convchk != 0 && itecnt <= h.itemax);
             if (convchk != 0 && subcnt <= h.submax) {
-                if (lpf == lpfmax) break;            // main.c:3777-3782
-                else if (dlpfp == h.dlpfmin) break;  // main.c:3783-3787
+                if (lpf == lpfmax) {  // main.c:3777-3782
+                    ref_message(m, "\n***ERROR*** Maximum allowable load proportionality factor attempted without "
+                                   "convergence at current time step\n");
+                    break;
+                } else if (dlpfp == h.dlpfmin) {  // main.c:3783-3787
+                    ref_message(m, "\n***ERROR*** Minimum allowable increment of load proportionality factor "
+                                   "reached at current time step\n");
+                    break;
+                }
                 dlpf = dlpfp / 2;
                 if (dlpf < h.dlpfmin) dlpf = h.dlpfmin;
                 lpf = lpf - dlpfp + dlpf;
                 subcnt++;
                 solcnt = 0;
             } else if (subcnt > h.submax) {
+                ref_message(m, "\n***ERROR*** Maximum allowable number of subdivisions exceeded at current time "
+                               "step\n");  // main.c:3802-3805
                 break;
             } else {
                 solcnt++;
@@ -341,6 +351,7 @@ void newmark_step(cb_model *m, cb_step *out)
         } while (lpf <= lpfmax);
         if (convchk != 0) {
             // halve the time increment (main.c:3823-3843)
+            ref_message(m, "\nTime increment interval reduced\n");
             ddt = ddt / 2;
             dt_temp = ddt * dt;
             if (tsflag == 0) sub_dt = ddt;
@@ -368,7 +379,8 @@ void newmark_step(cb_model *m, cb_step *out)
         }
     } while (ddt >= 0.0001 && tsflag != 2);
     if (convchk != 0)
-        throw cb_status_error(CB_ERR_DIVERGED, "minimum time increment interval reached without convergence");
+        fail_run(m, CB_ERR_DIVERGED, "minimum time increment interval reached without convergence",
+                 "\n***ERROR*** Minimum time increment interval reached without convergence\n");  // main.c:3941
     CB_CUDA(cudaStreamSynchronize(st));
     m->nm_ddt = ddt;
     out->lam = (double)k * dt;

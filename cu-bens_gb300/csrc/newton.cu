@@ -70,6 +70,7 @@ void newton_step(cb_model *m, cb_step *out)
     out->done = 0;
     // the do { } while (lpf <= lpfmax) loop: its first pass always runs
     if (m->nr_incs > 0 && !(m->nr_lpf <= h.lpfmax)) {
+        ref_success(m, "\nSolution successful\n");  // main.c:2154-2156
         out->done = 1;
         out->lam = m->nr_lpf;
         out->iterations = out->attempts = 0;
@@ -108,7 +109,9 @@ void newton_step(cb_model *m, cb_step *out)
                 int fl[2] = {0, 0};
                 d2h(fl, m->bf.flags, 2, st);
                 CB_CUDA(cudaStreamSynchronize(st));
-                if (fl[1]) throw cb_status_error(CB_ERR_NUMERIC, "singular stiffness matrix (zero pivot)");
+                if (fl[1])
+                    fail_run(m, CB_ERR_NUMERIC, "singular stiffness matrix (zero pivot)",
+                             "\n***ERROR*** Singular stiffness matrix\n");  // solve.c:566
             }
             solve(m, m->r, m->dd);
             {
@@ -125,18 +128,18 @@ void newton_step(cb_model *m, cb_step *out)
                 m->tm.launches += 2;
             }
             cb::MsalScalars &s = pull_scalars(m);
-            if (s.test_err) throw cb_status_error(CB_ERR_NUMERIC, "zero norm in the convergence test");
+            if (s.test_err) fail_run(m, CB_ERR_NUMERIC, "zero norm in the convergence test", test_message(s.test_err));
             convchk = s.convchk;
             advance_iteration(m);
             ++itecnt;
         } while (convchk != 0 && itecnt <= h.itemax);
         if (convchk != 0 && m->nr_subcnt <= h.submax) {
             if (lpf == h.lpfmax)
-                throw cb_status_error(CB_ERR_DIVERGED, "maximum allowable load proportionality factor attempted "
-                                                       "without convergence");
+                fail_run(m, CB_ERR_DIVERGED, "maximum allowable load proportionality factor attempted without convergence",
+                         "\n***ERROR*** Maximum allowable load proportionality factor attempted without convergence\n");
             if (dlpfp == h.dlpfmin)
-                throw cb_status_error(CB_ERR_DIVERGED,
-                                      "minimum allowable increment of load proportionality factor reached");
+                fail_run(m, CB_ERR_DIVERGED, "minimum allowable increment of load proportionality factor reached",
+                         "\n***ERROR*** Minimum allowable increment of load proportionality factor reached\n");
             dlpf = dlpfp / 2;
             if (dlpf < h.dlpfmin) dlpf = h.dlpfmin;
             lpf = lpf - dlpfp + dlpf;
@@ -145,7 +148,8 @@ void newton_step(cb_model *m, cb_step *out)
             continue;
         }
         if (m->nr_subcnt > h.submax)
-            throw cb_status_error(CB_ERR_DIVERGED, "maximum allowable number of subdivisions exceeded");
+            fail_run(m, CB_ERR_DIVERGED, "maximum allowable number of subdivisions exceeded",
+                     "\n***ERROR*** Maximum allowable number of subdivisions exceeded\n");  // main.c:2065-2066
         // accept (main.c:2082-2147); the newest element state is in ip
         d2d(m->d, m->dt, N, st);
         d2d(m->f, m->fcur, N, st);

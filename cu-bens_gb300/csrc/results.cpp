@@ -1,7 +1,10 @@
 // results*.txt writers: the layout and records of the reference's output()
 // (misc.c:345-451) for the resident API, so that a run through cb_* leaves
 // the same results2.txt (displacements), results3.txt (truss forces),
-// results4.txt (frame forces) and results5.txt (shell forces) as main.c.
+// results4.txt (frame forces) and results5.txt (shell forces) as main.c,
+// and the same results1.txt: the input echo (echo.cpp) followed by the
+// run's messages (errors, subdivisions of a Newmark time step, the closing
+// "Solution successful" or "Solution failed"), appended as they occur.
 //
 // A record is the converged state on the device: d and the element forces
 // of the converged configuration, averaged over the element's nodes as
@@ -24,7 +27,17 @@ namespace {
 
 struct ResultFiles {
     FILE *f[4] = {nullptr, nullptr, nullptr, nullptr};  // results2..results5
+    FILE *r1 = nullptr;                                  // results1.txt
+    size_t r1_lines = 0;                                 // messages written so far
 };
+
+// Append the run's messages logged since the last call.
+void flush_messages(cb_model *m, ResultFiles &r)
+{
+    if (!r.r1) return;
+    for (; r.r1_lines < m->ofp0.size(); ++r.r1_lines) std::fputs(m->ofp0[r.r1_lines].c_str(), r.r1);
+    std::fflush(r.r1);
+}
 
 // "\t%e" for every value, formatted in chunks by up to `threads` threads
 void write_values(FILE *out, const std::vector<double> &v)
@@ -82,6 +95,16 @@ int cb_results_open(cb_model *m, const char *dir)
                 throw cb_status_error(CB_ERR_ARG, "cannot open " + path);
             }
         }
+        const std::string p1 = std::string(dir) + "/results1.txt";
+        r->r1 = std::fopen(p1.c_str(), "w");
+        if (!r->r1) {
+            for (FILE *f : r->f) std::fclose(f);
+            delete r;
+            throw cb_status_error(CB_ERR_ARG, "cannot open " + p1);
+        }
+        const std::string echo = cb::input_echo(m->h);
+        std::fwrite(echo.data(), 1, echo.size(), r->r1);
+        flush_messages(m, *r);
         const cb::HostModel &h = m->h;
         FILE *o1 = r->f[0], *o2 = r->f[1], *o3 = r->f[2], *o4 = r->f[3];
         // layout lines (output flag 0)
@@ -135,6 +158,7 @@ int cb_results_write(cb_model *m, double lam, int iterations)
         std::vector<double> ef = pull(F ? m->fr.ef_c : nullptr, 14 * F, st);
         std::vector<double> es = pull(E ? m->sh.ef_c : nullptr, 18 * E, st);
         CB_CUDA(cudaStreamSynchronize(st));
+        flush_messages(m, *m->results);
         FILE **o = m->results->f;
         std::fprintf(o[0], "\n\t%e\t%d\t", lam, iterations);
         write_values(o[0], d);
@@ -171,8 +195,10 @@ int cb_results_close(cb_model *m)
     if (!m) return CB_ERR_ARG;
     if (!m->results) return CB_OK;
     int rc = CB_OK;
+    flush_messages(m, *m->results);
     for (FILE *f : m->results->f)
         if (f && std::fclose(f) != 0) rc = CB_ERR_ARG;
+    if (m->results->r1 && std::fclose(m->results->r1) != 0) rc = CB_ERR_ARG;
     delete m->results;
     m->results = nullptr;
     return rc;

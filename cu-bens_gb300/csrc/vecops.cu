@@ -206,14 +206,14 @@ __global__ void test_kernel(const double *partial, MsalScalars *sc)
         if (d[3] != 0) {
             if (sqrt(d[2]) / sqrt(d[3]) > sc->tolforc) conv += 100;
         } else {
-            err = 1;
+            err = 2;
         }
     }
     if (!err && sc->tolener < 1) {
         if (sc->intener1 != 0) {
             if (fabs(d[4] / sc->intener1) > sc->tolener) conv += 1000;
         } else {
-            err = 1;
+            err = 3;
         }
     }
     sc->convchk = conv;
@@ -424,14 +424,14 @@ __global__ void nm_test_kernel(const double *partial, MsalScalars *sc, int first
         if (d[3] != 0) {
             if (sqrt(d[2]) / sqrt(d[3]) > sc->tolforc) conv += 100;
         } else {
-            err = 1;
+            err = 2;
         }
     }
     if (!err && sc->tolener < 1) {
         if (sc->intener1 != 0) {
             if (fabs(d[4] / sc->intener1) > sc->tolener) conv += 1000;
         } else {
-            err = 1;
+            err = 3;
         }
     }
     sc->convchk = conv;

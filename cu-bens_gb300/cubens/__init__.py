@@ -113,6 +113,7 @@ def load(path: Path | None = None):
     L.cb_results_open.argtypes = [vp, C.c_char_p]
     L.cb_results_write.argtypes = [vp, C.c_double, C.c_int]
     L.cb_results_close.argtypes = [vp]
+    L.cb_input_echo.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]
     L.cb_newton_begin.argtypes = [vp]
     L.cb_newton_step.argtypes = [vp, C.POINTER(Step)]
     L.cb_newmark_begin.argtypes = [vp]
@@ -139,6 +140,19 @@ def _d(a):
 
 def _c64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def input_echo(model_def: str) -> str:
+    """The input echo the reference writes to results1.txt for this
+    model_def (no GPU needed)."""
+    text = model_def.encode()
+    n = C.c_size_t()
+    rc = load().cb_input_echo(text, len(text), None, 0, C.byref(n))
+    if rc != 0:
+        raise CubensError(rc, "model_def rejected by the parser")
+    buf = C.create_string_buffer(n.value + 1)
+    load().cb_input_echo(text, len(text), buf, n.value + 1, C.byref(n))
+    return buf.raw[:n.value].decode()
 
 
 def batch_msal(models, steps: int, threads: int = 16):

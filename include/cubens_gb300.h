@@ -238,11 +238,18 @@ int cb_mpnn_eval(cb_model *m, const double *r, const double *p, const double *t,
  * reference's layout lines; cb_results_write appends the current converged
  * state as one record (lam: the load factor or time, iterations: itecnt),
  * element forces averaged over the element's nodes as output() does;
- * cb_results_close closes them (cb_model_destroy does too). results1.txt,
- * the reference's input echo and message log, is not written. */
+ * cb_results_close closes them (cb_model_destroy does too). It also writes
+ * dir/results1.txt: the reference's echo of the model_def and then the
+ * run's messages as they occur (errors, reduced Newmark time increments,
+ * the closing "Solution successful" or "Solution failed"). */
 int cb_results_open(cb_model *m, const char *dir);
 int cb_results_write(cb_model *m, double lam, int iterations);
 int cb_results_close(cb_model *m);
+/* The input echo of results1.txt for a model_def text, without a GPU: the
+ * text the reference writes while it reads the file. Writes at most cap - 1
+ * bytes and a terminating zero into buf (may be NULL) and the full length
+ * into *needed (may be NULL); returns the parser's status. */
+int cb_input_echo(const char *text, size_t len, char *buf, size_t cap, size_t *needed);
 
 /* Checkpoint and restart of the nonlinear Newmark driver (checkPoint and
  * restartStep, misc.c:494-716). cb_checkpoint_save writes the converged

@@ -147,6 +147,32 @@ def results_fixtures():
                         files=np.array(files), steps=np.array([results_cases()[n][1] for n in names]))
 
 
+def results1_cases():
+    """Models whose whole results1.txt (the input echo and the run's
+    messages) is pinned: the results2-5 cases, the frame with one warping DOF
+    per member end (MSAL and Newmark), and an arc-length run whose first
+    increment does not converge."""
+    c = dict(results_cases())
+    c["frame_msal_member"] = (frame_msal_model("member"), 3)
+    c["frame_newmark_member"] = (frame_newmark_model("member", 6), 5)
+    bad = models.MsalControls(joint=41, direction=3, dk=-50.0, toldisp=1e-5, tolforc=1.0, tolener=1.0, itemax=5)
+    c["panel8_too_large"] = (models.cylindrical_panel(8, controls=bad), 2)
+    return c
+
+
+def results1_fixtures():
+    """The reference's own results1.txt for the results1 cases."""
+    texts, files, names = [], [], list(results1_cases())
+    for name in names:
+        m, steps = results1_cases()[name]
+        r = refrun.run(m.text, steps, timeout=600)
+        texts.append(m.text)
+        files.append(r["results1"])
+        print("results1", name, r["returncode"], len(r["results1"]), repr(r["results1"][-80:]))
+    np.savez_compressed(OUT / "results1_files.npz", names=np.array(names), model_def=np.array(texts),
+                        results1=np.array(files), steps=np.array([results1_cases()[n][1] for n in names]))
+
+
 class RefElem:
     """The reference's element routines, called through the harness library."""
 
@@ -397,3 +423,4 @@ if __name__ == "__main__":
     whole_runs()
     newton_runs()
     results_fixtures()
+    results1_fixtures()

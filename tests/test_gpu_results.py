@@ -24,6 +24,13 @@ def _values(t: str) -> np.ndarray:
 def _run(name, text, steps, out_dir):
     m = cubens.Model(text, precision=cubens.FP64)
     m.results_open(out_dir)
+    try:
+        _steps(m, steps)
+    finally:
+        m.results_close()
+
+
+def _steps(m, steps):
     alg = m.info["algflag"]
     if alg == 3:
         r = m.begin()
@@ -43,7 +50,6 @@ def _run(name, text, steps, out_dir):
             if r.done:
                 break
             m.results_write(r.lam, r.iterations)
-    m.results_close()
 
 
 def test_results_files_match_the_reference(golden_dir, tmp_path):
@@ -61,3 +67,20 @@ def test_results_files_match_the_reference(golden_dir, tmp_path):
             if b.size:
                 scale = np.max(np.abs(b))
                 assert np.max(np.abs(a - b)) <= 2e-6 * scale + 1e-300, (name, k)
+
+
+def test_results1_matches_the_reference(golden_dir, tmp_path):
+    """results1.txt byte for byte: the input echo, then the run's messages
+    (the closing "Solution successful" of the Newton-Raphson run, the error
+    and "Solution failed" of an arc-length run whose first increment does not
+    converge; the capped runs end after the echo, as the reference's do)."""
+    z = np.load(golden_dir / "results1_files.npz")
+    for name, text, ref, steps in zip(z["names"], z["model_def"], z["results1"], z["steps"]):
+        d = tmp_path / str(name)
+        d.mkdir()
+        try:
+            _run(str(name), str(text), int(steps), d)
+        except cubens.CubensError:
+            assert str(name) == "panel8_too_large"
+        ours = (d / "results1.txt").read_text()
+        assert ours == str(ref), (name, ours[-200:], str(ref)[-200:])
