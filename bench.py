@@ -960,6 +960,11 @@ def main():
                     help="profiling: the FP32x2 band LDL^T of the same panel on an N x N mesh, or A axial by N "
                          "circumferential divisions (the band of the N x N panel with fewer equations): first "
                          "increment, then one factorisation alone; no JSON line")
+    ap.add_argument("--force-only", type=int, default=0, metavar="N",
+                    help="profiling: shell_forces_kernel on the same panel on an N x N mesh (first increment, "
+                         "then 20 launches alone); no JSON line")
+    ap.add_argument("--factor-kernel", type=int, default=0,
+                    help="--factor-only: 0 the tensor-core double-word factor, 1 the FP32-pipe one")
     ap.add_argument("--fp64-steps", type=int, default=2,
                     help="panel512: timed increments of the plain FP64 leg (about half a minute each)")
     ap.add_argument("--batch", type=int, default=48, help="instances of the batch workload")
@@ -970,11 +975,20 @@ def main():
         import cubens
         nf, _, na = args.factor_only.partition("x")
         m = cubens.Model(large_text(int(nf), n_axial=int(na) if na else None), precision=cubens.FP32X2,
-                         band_solve=1)
+                         band_solve=1, factor_kernel=args.factor_kernel)
         m.begin()
         ms, _, fl = m.profile_kernel(cubens.K_BAND_LDLT, reps=1)
         print(f"band LDL^T, NEQ {m.neq}, band {m.info['bandwidth']}: {ms:.1f} ms, "
               f"{fl / 2 / (ms * 1e-3) / 1e12:.3f} T double-word multiply-adds/s", flush=True)
+        return
+    if args.force_only:
+        import cubens
+        m = cubens.Model(large_text(args.force_only), precision=cubens.FP32X2, band_solve=1)
+        m.begin()
+        ms, nbytes, fl = m.profile_kernel(cubens.K_SHELL_FORCE, reps=20)
+        print(f"shell_forces_kernel, {m.info['ne_sh']} elements: {ms * 1e3:.1f} us, "
+              f"{nbytes / (ms * 1e-3) / 1e9:.0f} GB/s of {nbytes / m.info['ne_sh']:.0f} B per element, "
+              f"{fl / (ms * 1e-3) / 1e12:.3f} TFLOP/s FP64 (estimated flops)", flush=True)
         return
     world, rank, local, pg = dist_setup(args.gpus)
     if args.workload == "batch":

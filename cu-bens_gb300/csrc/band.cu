@@ -1814,10 +1814,11 @@ void band_alloc(BandFactor &f, long n, long bw, bool fp32, bool direct, bool use
     f.bytes = es * ((size_t)f.ld * npad + npad + blocks * (2 * f.s + 2 * f.w) + work);
 }
 
-void band_alloc_dw(BandFactor &f, long n, long bw)
+void band_alloc_dw(BandFactor &f, long n, long bw, bool simt)
 {
     band_alloc(f, n, bw, false, true, false, band_dw_block());
     f.dw = true;
+    f.dw_simt = simt;
     band_dw_alloc(f);
 }
 
@@ -1825,7 +1826,7 @@ void band_free(BandFactor &f)
 {
     if (f.factor_graph) cudaGraphExecDestroy(f.factor_graph);
     for (void *p : {f.band, f.dinv, f.linv, f.linvt, f.pmat, f.rmat, f.work, f.stage, f.look, (void *)f.ssd,
-                    (void *)f.flags, (void *)f.bar, (void *)f.fbar})
+                    (void *)f.flags, (void *)f.bar, (void *)f.fbar, f.slices, (void *)f.slice_exp})
         if (p) cudaFree(p);
     f = BandFactor{};
 }

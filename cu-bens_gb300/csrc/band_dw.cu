@@ -18,11 +18,15 @@
 //      and L into a k-major buffer;
 //   -- grid barrier --
 //   3. the trailing lower triangle of the band window in 64 x 64 tiles,
-//      A_ij -= sum_k W_ik L_jk, each thread a 4 x 4 block of accumulators;
-//      CTA 0 takes only tile (0,0), which is the next panel's diagonal
-//      block, and factors that block right after its update while the other
-//      CTAs work through the rest of the triangle;
+//      A_ij -= sum_k W_ik L_jk; CTA 0 takes only tile (0,0), which is the
+//      next panel's diagonal block, and factors that block right after its
+//      update while the other CTAs work through the rest of the triangle;
 //   -- grid barrier --
+// Two kernels differ in step 3. factor_dw_tc_kernel (the default) forms the
+// tile products on the tensor cores: step 2 splits every W and L row into
+// bfloat16 slices whose mma.sync products accumulate exactly in FP32 (the
+// comment above the kernel gives the bounds). factor_dw_kernel forms them
+// on the FP32 pipe, each thread a 4 x 4 block of double-word accumulators.
 // Then inv_block_kernel forms, for every 128-row block of the matrix, the
 // inverse X_i of its unit-lower diagonal block: its ten lower 32 x 32 tiles,
 // once row-major and once column-major.
@@ -35,6 +39,7 @@
 // the solution: each CTA copies the next block's inverse into shared memory
 // (cp.async) and each thread the next step's band values into registers
 // before the barrier that ends a step.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -82,6 +87,9 @@ struct DwFactorArgs {
     dw *look;       // the next panel's factored block (64 x 64) and 1/D (64)
     GridBarrier *bar;
     long long max_polls;
+    __nv_bfloat16 *wsl, *lsl;  // tensor-core factor: slices [NS][mrow][64] of W and of L
+    int *ew, *el;               // ... row exponents [mrow]
+    long mrow;                  // rows of a slice (bw + 1)
 };
 
 // shared memory of the factor: the diagonal block (and 1/D), W and L of a tile
@@ -103,24 +111,41 @@ __device__ __forceinline__ void cp_async_commit_f() { asm volatile("cp.async.com
 template <int N>
 __device__ __forceinline__ void cp_async_wait_f() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// Entry e of the lower triangle of a 64 x 64 block listed by columns
+// (column j starts at j (129 - j) / 2): its row i and column j.
+__device__ __forceinline__ void tri_entry(int e, int &i, int &j)
+{
+    constexpr int T2 = 2 * PW + 1;
+    int c = (int)((T2 - sqrtf((float)(T2 * T2 - 8 * e))) * 0.5f);
+    while (c > 0 && c * (T2 - c) / 2 > e) --c;
+    while ((c + 1) * (T2 - (c + 1)) / 2 <= e) ++c;
+    j = c;
+    i = e - c * (T2 - c) / 2 + c;
+}
+
 // LDL^T of the 64 x 64 block in A (lower triangle) by all threads of the CTA,
 // one CTA barrier per column: every thread forms 1/D_k itself from the final
-// pivot, the update uses the unscaled column (W = L D), and the columns are
-// scaled by 1/D at the end. On return L below the diagonal, D on it, di = 1/D.
+// pivot and the update uses the unscaled column (W = L D). The entries of
+// step k are the tail of the triangle's column list from column k + 1, dealt
+// out evenly to the threads. The columns are scaled by 1/D at the end. On
+// return L below the diagonal, D on it, di = 1/D.
 __device__ void ldlt_block_dw(dw (*A)[PW + 1], dw *di)
 {
     const int tid = threadIdx.x;
+    constexpr int total = PW * (PW + 1) / 2;
     for (int k = 0; k < PW; ++k) {
         const dw dk = dw_recip(A[k][k]);
-        for (int e = tid; e < PW * PW; e += kThreads) {
-            const int j = e / PW, i = e % PW;
-            if (j > k && i >= j) A[i][j] = dw_sub(A[i][j], dw_mul(dw_mul(A[i][k], dk), A[j][k]));
+        for (int e = (k + 1) * (2 * PW - k) / 2 + tid; e < total; e += kThreads) {
+            int i, j;
+            tri_entry(e, i, j);
+            A[i][j] = dw_sub(A[i][j], dw_mul(dw_mul(A[i][k], dk), A[j][k]));
         }
         if (tid == 0) di[k] = dk;
         __syncthreads();
     }
-    for (int e = tid; e < PW * PW; e += kThreads) {
-        const int j = e / PW, i = e % PW;
+    for (int e = tid; e < total; e += kThreads) {
+        int i, j;
+        tri_entry(e, i, j);
         if (i > j) A[i][j] = dw_mul(A[i][j], di[j]);
     }
     __syncthreads();
@@ -153,6 +178,74 @@ __device__ void load_block(const DwFactorArgs &a, long p, dw (*A)[PW + 1])
         A[i][j] = (i >= j && i - j <= a.bw) ? a.band[(p + j) * a.ld + (i - j)] : dw_zero();
     }
     __syncthreads();
+}
+
+// Row r of panel p (one warp; lane holds columns lane and lane + 32):
+// W_r by substitution against the factored diagonal block (W_r L_pp^T =
+// A_r), L_r = W_r D^-1 into the band. Returns W and L in w0, w1, l0, l1.
+__device__ __forceinline__ void panel_row(const DwFactorArgs &a, const dw (*A)[PW + 1], const dw *di, long p,
+                                          long r, int lane, dw &w0, dw &w1, dw &l0, dw &l1)
+{
+    const long ld = a.ld, bw = a.bw;
+    const long off0 = PW + r - lane, off1 = off0 - 32;
+    w0 = off0 <= bw ? a.band[(p + lane) * ld + off0] : dw_zero();
+    w1 = off1 <= bw ? a.band[(p + 32 + lane) * ld + off1] : dw_zero();
+    for (int k = 0; k < 32; ++k) {
+        const dw wk = shfl_dw(w0, k);
+        if (lane > k) w0 = dw_sub(w0, dw_mul(wk, A[lane][k]));
+        w1 = dw_sub(w1, dw_mul(wk, A[32 + lane][k]));
+    }
+    for (int k = 0; k < 31; ++k) {
+        const dw wk = shfl_dw(w1, k);
+        if (lane > k) w1 = dw_sub(w1, dw_mul(wk, A[32 + lane][32 + k]));
+    }
+    l0 = dw_mul(w0, di[lane]);
+    l1 = dw_mul(w1, di[32 + lane]);
+    if (off0 <= bw) a.band[(p + lane) * ld + off0] = l0;
+    if (off1 <= bw) a.band[(p + 32 + lane) * ld + off1] = l1;
+}
+
+// Two rows r and r2 of panel p at once (the second only when v2): the
+// same arithmetic as panel_row with two independent dependency chains.
+__device__ __forceinline__ void panel_row2(const DwFactorArgs &a, const dw (*A)[PW + 1], const dw *di, long p,
+                                           long r, long r2, bool v2, int lane, dw *w, dw *l)
+{
+    const long ld = a.ld, bw = a.bw;
+    const long o0 = PW + r - lane, o1 = o0 - 32, q0 = PW + r2 - lane, q1 = q0 - 32;
+    dw w0 = o0 <= bw ? a.band[(p + lane) * ld + o0] : dw_zero();
+    dw w1 = o1 <= bw ? a.band[(p + 32 + lane) * ld + o1] : dw_zero();
+    dw x0 = v2 && q0 <= bw ? a.band[(p + lane) * ld + q0] : dw_zero();
+    dw x1 = v2 && q1 <= bw ? a.band[(p + 32 + lane) * ld + q1] : dw_zero();
+    for (int k = 0; k < 32; ++k) {
+        const dw wk = shfl_dw(w0, k), xk = shfl_dw(x0, k);
+        const dw akl = A[lane][k], ak2 = A[32 + lane][k];
+        if (lane > k) {
+            w0 = dw_sub(w0, dw_mul(wk, akl));
+            x0 = dw_sub(x0, dw_mul(xk, akl));
+        }
+        w1 = dw_sub(w1, dw_mul(wk, ak2));
+        x1 = dw_sub(x1, dw_mul(xk, ak2));
+    }
+    for (int k = 0; k < 31; ++k) {
+        const dw wk = shfl_dw(w1, k), xk = shfl_dw(x1, k);
+        const dw ak = A[32 + lane][32 + k];
+        if (lane > k) {
+            w1 = dw_sub(w1, dw_mul(wk, ak));
+            x1 = dw_sub(x1, dw_mul(xk, ak));
+        }
+    }
+    w[0] = w0;
+    w[1] = w1;
+    w[2] = x0;
+    w[3] = x1;
+    l[0] = dw_mul(w0, di[lane]);
+    l[1] = dw_mul(w1, di[32 + lane]);
+    l[2] = dw_mul(x0, di[lane]);
+    l[3] = dw_mul(x1, di[32 + lane]);
+    if (o0 <= bw) a.band[(p + lane) * ld + o0] = l[0];
+    if (o1 <= bw) a.band[(p + 32 + lane) * ld + o1] = l[1];
+    if (v2 && q0 <= bw) a.band[(p + lane) * ld + q0] = l[2];
+    if (v2 && q1 <= bw) a.band[(p + 32 + lane) * ld + q1] = l[3];
 }
 
 __global__ void __launch_bounds__(kThreads, 1) factor_dw_kernel(DwFactorArgs a)
@@ -190,25 +283,12 @@ __global__ void __launch_bounds__(kThreads, 1) factor_dw_kernel(DwFactorArgs a)
             lbuf[tid * ms + m] = dw_zero();
         }
         for (long r = blockIdx.x * 8L + warp; r < m; r += G * 8L) {
-            const long off0 = PW + r - lane, off1 = off0 - 32;
-            dw w0 = off0 <= bw ? a.band[(p + lane) * ld + off0] : dw_zero();
-            dw w1 = off1 <= bw ? a.band[(p + 32 + lane) * ld + off1] : dw_zero();
-            for (int k = 0; k < 32; ++k) {
-                const dw wk = shfl_dw(w0, k);
-                if (lane > k) w0 = dw_sub(w0, dw_mul(wk, A[lane][k]));
-                w1 = dw_sub(w1, dw_mul(wk, A[32 + lane][k]));
-            }
-            for (int k = 0; k < 31; ++k) {
-                const dw wk = shfl_dw(w1, k);
-                if (lane > k) w1 = dw_sub(w1, dw_mul(wk, A[32 + lane][32 + k]));
-            }
-            const dw l0 = dw_mul(w0, di[lane]), l1 = dw_mul(w1, di[32 + lane]);
+            dw w0, w1, l0, l1;
+            panel_row(a, A, di, p, r, lane, w0, w1, l0, l1);
             wbuf[lane * ms + r] = w0;
             wbuf[(32 + lane) * ms + r] = w1;
             lbuf[lane * ms + r] = l0;
             lbuf[(32 + lane) * ms + r] = l1;
-            if (off0 <= bw) a.band[(p + lane) * ld + off0] = l0;
-            if (off1 <= bw) a.band[(p + 32 + lane) * ld + off1] = l1;
         }
         if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
         // ---- 3. trailing triangle; CTA 0: tile (0,0), then the next block ----
@@ -297,6 +377,263 @@ __global__ void __launch_bounds__(kThreads, 1) factor_dw_kernel(DwFactorArgs a)
             // tile (0,0) is the next panel's diagonal block (rows and columns
             // 0..63 of the window); band rows below the window, for a band
             // narrower than a panel, take no update from this panel
+            tiles(0, 1, ntiles > 0 ? 1 : 0);
+            if (p + PW < a.npad) {
+                const long pn = p + PW;
+                load_block(a, pn, A);
+                ldlt_block_dw(A, di);
+                record_block(a, pn, A, di);
+                for (int e = tid; e < PW * PW; e += kThreads) a.look[e] = A[e / PW][e % PW];
+                if (tid < PW) a.look[PW * PW + tid] = di[tid];
+            }
+            if (G == 1) tiles(1, 1, ntiles);
+        } else {
+            tiles(blockIdx.x, G - 1, ntiles);
+        }
+        if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same factor with the trailing update on the tensor cores.
+//
+// Every row of the panel's W (and of L) is split into NS bfloat16 slices of
+// 8 bits. With 2^e the row's bound (|v| < 2^e for its 64 values),
+// v = 2^(e-7) sum_s q_s 2^(-8s) with integers |q_s| <= 129; slice s holds
+// q_s 2^(-8s), exact in bfloat16. The product of slices a and b is
+// q_a q_b 2^(-8c), c = a + b, with |q_a q_b| < 2^15, so a 64-term sum of at
+// most six such products per diagonal c stays below 2^24 units of 2^(-8c):
+// mma.sync's FP32 accumulation of each of the diagonals 0, 1 and 2 is
+// exact. The diagonals 3 .. NS-1 share one accumulator, whose rounding is
+// below 2^-48 of the product of the two row bounds, and so are the
+// diagonals dropped (c >= NS): the resolution of the double-word format
+// itself. 21 slice products in all. Each output then adds its four
+// accumulators in double-word arithmetic, scales the sum by the two row
+// exponents and subtracts it from the band (the error-free splitting of
+// Ozaki, Ogita, Oishi and Rump, Numer. Algorithms 59 (2012) 95-118, on
+// 8-bit slices).
+constexpr int NS = 6;         // slices per value: 7 + 5 x 8 = 47 bits
+constexpr int NA = 4;         // accumulators: diagonals 0, 1, 2 and 3 .. NS-1
+constexpr int SST = KH + 8;   // shared row stride of a stage's slices (bf16): conflict-free fragments
+
+struct DwTcSmem {
+    dw A[PW][PW + 1];
+    dw di[PW];
+    __nv_bfloat16 Ws[2][NS][TW][SST];  // W slices of a tile's rows, one stage (KH columns of the panel)
+    __nv_bfloat16 Ls[2][NS][TW][SST];  // L slices of a tile's columns
+};
+
+__device__ __forceinline__ void mma16816(float *c, const unsigned *a, const unsigned *b)
+{
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Slices of one panel row (one warp; lane holds columns lane and lane + 32)
+// into out[s][r][0..63], its exponent e - 7 into ex[r].
+__device__ void slice_row(dw v0, dw v1, __nv_bfloat16 *out, int *ex, long r, long mrow, int lane)
+{
+    float mx = fmaxf(fabsf(v0.hi), fabsf(v1.hi));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if (mx > 0.0f) (void)frexpf(mx, &e);  // mx < 2^e, and so is every |v|
+    const int sh = 7 - e;
+    float h0 = ldexpf(v0.hi, sh), l0 = ldexpf(v0.lo, sh), h1 = ldexpf(v1.hi, sh), l1 = ldexpf(v1.lo, sh);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        const float q0 = rintf(h0), q1 = rintf(h1);
+        __nv_bfloat16 *row = out + ((long)s * mrow + r) * PW;
+        row[lane] = __float2bfloat16_rn(ldexpf(q0, -8 * s));
+        row[32 + lane] = __float2bfloat16_rn(ldexpf(q1, -8 * s));
+        // the remainder (h - q is exact: |h - q| <= 1/2 and q = rint(h)), times 2^8
+        two_sum(__fsub_rn(h0, q0), l0, h0, l0);
+        two_sum(__fsub_rn(h1, q1), l1, h1, l1);
+        h0 *= 256.0f;
+        l0 *= 256.0f;
+        h1 *= 256.0f;
+        l1 *= 256.0f;
+    }
+    if (lane == 0) ex[r] = e - 7;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) factor_dw_tc_kernel(DwFactorArgs a)
+{
+    extern __shared__ __align__(16) unsigned char dyn[];
+    DwTcSmem &sm = *reinterpret_cast<DwTcSmem *>(dyn);
+    auto &A = sm.A;
+    auto &di = sm.di;
+    unsigned ep = 0;  // grid barriers passed
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    const int g = lane >> 2, q = lane & 3;     // mma fragment coordinates
+    const int wr = warp >> 1, wc = warp & 1;   // the warp's 16 rows and 32 columns of a 64 x 64 tile
+    const long ld = a.ld, bw = a.bw, mrow = a.mrow;
+    const unsigned G = gridDim.x;
+    for (long p = 0; p < a.npad; p += PW) {
+        long m = a.npad - p - PW;
+        if (m > bw) m = bw;
+        if (m < 0) m = 0;
+        // ---- 1. the factored diagonal block ----
+        if (p == 0) {
+            load_block(a, 0, A);
+            ldlt_block_dw(A, di);
+            if (blockIdx.x == 0) record_block(a, 0, A, di);
+        } else {
+            for (int e = tid; e < PW * PW; e += kThreads) A[e / PW][e % PW] = a.look[e];
+            if (tid < PW) di[tid] = a.look[PW * PW + tid];
+        }
+        __syncthreads();
+        // ---- 2. panel rows by substitution, then their slices ----
+        // Column k of W is scaled by 2^-f_k and column k of L by 2^f_k, with
+        // 2^f_k near sqrt|D_k|: W L^T is unchanged and both rows take the
+        // magnitudes of the Cholesky-like factor L |D|^(1/2), whose row
+        // entries stay within the square root of the row's diagonal. Pivots
+        // that differ by orders of magnitude (the shells' drilling DOFs) then
+        // do not widen a row's range, which the row exponent of the slices
+        // would turn into lost bits.
+        int f0 = 0, f1 = 0;
+        {
+            int e0 = 0, e1 = 0;
+            const float d0 = fabsf(A[lane][lane].hi), d1 = fabsf(A[32 + lane][32 + lane].hi);
+            if (d0 > 0.0f) (void)frexpf(d0, &e0);
+            if (d1 > 0.0f) (void)frexpf(d1, &e1);
+            f0 = e0 / 2;
+            f1 = e1 / 2;
+        }
+        for (long r = blockIdx.x * 8L + warp; r < m; r += 2 * G * 8L) {
+            const long r2 = r + G * 8L;
+            const bool v2 = r2 < m;
+            dw w[4], l[4];
+            panel_row2(a, A, di, p, r, r2, v2, lane, w, l);
+            for (int h = 0; h < (v2 ? 2 : 1); ++h) {
+                const long rr = h ? r2 : r;
+                slice_row(dw{ldexpf(w[2 * h].hi, -f0), ldexpf(w[2 * h].lo, -f0)},
+                          dw{ldexpf(w[2 * h + 1].hi, -f1), ldexpf(w[2 * h + 1].lo, -f1)}, a.wsl, a.ew, rr, mrow, lane);
+                slice_row(dw{ldexpf(l[2 * h].hi, f0), ldexpf(l[2 * h].lo, f0)},
+                          dw{ldexpf(l[2 * h + 1].hi, f1), ldexpf(l[2 * h + 1].lo, f1)}, a.lsl, a.el, rr, mrow, lane);
+            }
+        }
+        if (!grid_barrier(a.bar, G, ep, a.max_polls)) return;
+        // ---- 3. trailing triangle on the tensor cores; CTA 0: tile (0,0), then the next block ----
+        const long nt = (m + TW - 1) / TW;
+        const long ntiles = nt * (nt + 1) / 2;
+        auto tiles = [&](long first, long stride, long last) {
+            if (first >= last) return;
+            const long nst = 2 * ((last - first + stride - 1) / stride);
+            auto coords = [&](long t, long &r0, long &j0) {
+                long ti = (long)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+                while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+                while (ti * (ti + 1) / 2 > t) --ti;
+                r0 = ti * TW;
+                j0 = (t - ti * (ti + 1) / 2) * TW;
+            };
+            // stage st: half h = st & 1 of the panel's columns of tile st / 2;
+            // 16-byte chunks of 8 slice values, rows past m zero-filled
+            auto fetch = [&](long st) {
+                long r0, j0;
+                coords(first + (st / 2) * stride, r0, j0);
+                const int h = (int)(st & 1), b = (int)(st & 1);
+                constexpr int CH = KH / 8;
+#pragma unroll 1
+                for (int e = tid; e < NS * TW * CH; e += kThreads) {
+                    const int sl = e / (TW * CH), rem = e % (TW * CH), row = rem / CH, c = rem % CH;
+                    const long kk = KH * h + 8 * c;
+                    const bool vw = r0 + row < m, vl = j0 + row < m;
+                    const long rw = vw ? r0 + row : 0, rl = vl ? j0 + row : 0;
+                    cp_async16_zfill(&sm.Ws[b][sl][row][8 * c], a.wsl + ((long)sl * mrow + rw) * PW + kk, vw);
+                    cp_async16_zfill(&sm.Ls[b][sl][row][8 * c], a.lsl + ((long)sl * mrow + rl) * PW + kk, vl);
+                }
+                cp_async_commit_f();
+            };
+            float acc[NA][4][4];  // [diagonal 0, 1, 2, the rest][n-tile][fragment]
+            long r0 = 0, j0 = 0;
+            fetch(0);
+            for (long st = 0; st < nst; ++st) {
+                const int b = (int)(st & 1);
+                if (st + 1 < nst) fetch(st + 1);
+                if ((st & 1) == 0) {
+                    coords(first + (st / 2) * stride, r0, j0);
+#pragma unroll
+                    for (int c = 0; c < NA; ++c)
+#pragma unroll
+                        for (int n = 0; n < 4; ++n)
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) acc[c][n][i] = 0.0f;
+                }
+                if (st + 1 < nst) cp_async_wait_f<1>();
+                else cp_async_wait_f<0>();
+                __syncthreads();
+#pragma unroll 1
+                for (int ks = 0; ks < KH; ks += 16) {
+                    // the warp's 16 rows: all slices' A fragments; then per
+                    // column block and L slice one B fragment
+                    unsigned af[NS][4];
+#pragma unroll
+                    for (int sa = 0; sa < NS; ++sa) {
+                        const __nv_bfloat16 *ap = &sm.Ws[b][sa][16 * wr + g][ks + 2 * q];
+                        af[sa][0] = *reinterpret_cast<const unsigned *>(ap);
+                        af[sa][1] = *reinterpret_cast<const unsigned *>(ap + 8 * SST);
+                        af[sa][2] = *reinterpret_cast<const unsigned *>(ap + 8);
+                        af[sa][3] = *reinterpret_cast<const unsigned *>(ap + 8 * SST + 8);
+                    }
+#pragma unroll
+                    for (int n = 0; n < 4; ++n)
+#pragma unroll
+                        for (int sb = 0; sb < NS; ++sb) {
+                            const __nv_bfloat16 *bp = &sm.Ls[b][sb][32 * wc + 8 * n + g][ks + 2 * q];
+                            const unsigned bfr[2] = {*reinterpret_cast<const unsigned *>(bp),
+                                                     *reinterpret_cast<const unsigned *>(bp + 8)};
+#pragma unroll
+                            for (int sa = 0; sa < NS - sb; ++sa)
+                                mma16816(acc[sa + sb < NA ? sa + sb : NA - 1][n], af[sa], bfr);
+                        }
+                }
+                __syncthreads();  // the buffer is refilled by the stage after next
+                if (st & 1) {
+                    // rows r0 + 16 wr + g (+8), columns j0 + 32 wc + 8 n + 2 q (+1):
+                    // the exponents and the band values first (one round trip),
+                    // then the updates
+                    const long rb = r0 + 16 * wr + g, cb = j0 + 32 * wc + 2 * q;
+                    int er[2], ec[8];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) er[h] = rb + 8 * h < m ? a.ew[rb + 8 * h] : 0;
+#pragma unroll
+                    for (int n = 0; n < 4; ++n)
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) ec[2 * n + h] = cb + 8 * n + h < m ? a.el[cb + 8 * n + h] : 0;
+#pragma unroll
+                    for (int n0 = 0; n0 < 4; n0 += 2) {  // two column blocks per round trip
+                        dw old[2][4];
+#pragma unroll
+                        for (int n = 0; n < 2; ++n)
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const long rr = rb + 8 * (i >> 1), jj = cb + 8 * (n0 + n) + (i & 1);
+                                old[n][i] = (rr < m && jj <= rr) ? a.band[(p + PW + jj) * ld + (rr - jj)] : dw_zero();
+                            }
+#pragma unroll
+                        for (int n = 0; n < 2; ++n)
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const long rr = rb + 8 * (i >> 1), jj = cb + 8 * (n0 + n) + (i & 1);
+                                if (rr < m && jj <= rr) {
+                                    dw v = dw{acc[NA - 1][n0 + n][i], 0.0f};
+#pragma unroll
+                                    for (int c = NA - 2; c >= 0; --c) v = dw_add(v, dw{acc[c][n0 + n][i], 0.0f});
+                                    const int sc = er[i >> 1] + ec[2 * (n0 + n) + (i & 1)];
+                                    v.hi = ldexpf(v.hi, sc);
+                                    v.lo = ldexpf(v.lo, sc);
+                                    a.band[(p + PW + jj) * ld + (rr - jj)] = dw_sub(old[n][i], v);
+                                }
+                            }
+                    }
+                }
+            }
+            __syncthreads();  // the tiles' band values are written before the caller reads them
+        };
+        if (blockIdx.x == 0) {
             tiles(0, 1, ntiles > 0 ? 1 : 0);
             if (p + PW < a.npad) {
                 const long pn = p + PW;
@@ -624,12 +961,28 @@ void band_dw_alloc(BandFactor &f)
     CB_CUDA_DW(cudaMalloc(&f.work, sizeof(dw) * wl));
     CB_CUDA_DW(cudaFree(f.look));
     CB_CUDA_DW(cudaMalloc(&f.look, sizeof(dw) * (PW * PW + PW)));
-    static const bool fsmem_ok = [] {
-        return cudaFuncSetAttribute(factor_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)sizeof(DwFactorSmem)) == cudaSuccess;
-    }();
-    if (!fsmem_ok) throw std::runtime_error("the double-word factor needs 97 KB of shared memory per CTA");
-    f.factor_grid = coop_grid(factor_dw_kernel, 1, sizeof(DwFactorSmem));
+    if (f.dw_simt) {
+        static const bool fsmem_ok = [] {
+            return cudaFuncSetAttribute(factor_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sizeof(DwFactorSmem)) == cudaSuccess;
+        }();
+        if (!fsmem_ok) throw std::runtime_error("the double-word factor needs 97 KB of shared memory per CTA");
+        f.factor_grid = coop_grid(factor_dw_kernel, 1, sizeof(DwFactorSmem));
+    } else {
+        static const bool tsmem_ok = [] {
+            return cudaFuncSetAttribute(factor_dw_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sizeof(DwTcSmem)) == cudaSuccess;
+        }();
+        if (!tsmem_ok) throw std::runtime_error("the tensor-core double-word factor needs 157 KB of shared memory");
+        f.factor_grid = coop_grid(factor_dw_tc_kernel, 1, sizeof(DwTcSmem));
+        // W and L slices of one panel ([NS][bw + 1][64] bfloat16 each) and their row exponents
+        const size_t mrow = (size_t)f.bw + 1;
+        CB_CUDA_DW(cudaMalloc(&f.slices, sizeof(__nv_bfloat16) * 2 * NS * mrow * PW));
+        CB_CUDA_DW(cudaMemset(f.slices, 0, sizeof(__nv_bfloat16) * 2 * NS * mrow * PW));
+        CB_CUDA_DW(cudaMalloc(&f.slice_exp, sizeof(int) * 2 * mrow));
+        CB_CUDA_DW(cudaMemset(f.slice_exp, 0, sizeof(int) * 2 * mrow));
+        f.bytes += sizeof(__nv_bfloat16) * 2 * NS * mrow * PW + sizeof(int) * 2 * mrow;
+    }
     static const bool smem_ok = [] {
         return cudaFuncSetAttribute(solve_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kSolveSmem) == cudaSuccess;
@@ -665,11 +1018,19 @@ void band_dw_factor(BandFactor &f, cudaStream_t st, long *launches)
     CB_CUDA_DW(cudaMemsetAsync(f.fbar, 0, sizeof(GridBarrier), st));
     const long tiles = ((f.bw + TW - 1) / TW) * ((f.bw + TW - 1) / TW + 1) / 2;
     const int grid = (int)std::max(1L, std::min<long>(f.factor_grid, std::max(tiles + 1, (f.bw + 7) / 8)));
-    DwFactorArgs a{band, f.ld, f.bw, npad, f.n, (dw *)f.dinv, f.ssd, f.flags, (dw *)f.work, (dw *)f.look, f.fbar,
-                   f.max_polls};
+    const long mrow = f.bw + 1;
+    __nv_bfloat16 *wsl = (__nv_bfloat16 *)f.slices;
+    DwFactorArgs a{band,        f.ld,    f.bw,  npad,   f.n,         (dw *)f.dinv,
+                   f.ssd,       f.flags, (dw *)f.work,  (dw *)f.look, f.fbar,    f.max_polls,
+                   wsl,         wsl ? wsl + (size_t)NS * mrow * PW : nullptr,
+                   f.slice_exp, f.slice_exp ? f.slice_exp + mrow : nullptr, mrow};
     void *args[] = {&a};
-    CB_CUDA_DW(cudaLaunchCooperativeKernel((const void *)factor_dw_kernel, dim3((unsigned)grid), dim3(kThreads),
-                                           args, sizeof(DwFactorSmem), st));
+    if (f.dw_simt)
+        CB_CUDA_DW(cudaLaunchCooperativeKernel((const void *)factor_dw_kernel, dim3((unsigned)grid),
+                                               dim3(kThreads), args, sizeof(DwFactorSmem), st));
+    else
+        CB_CUDA_DW(cudaLaunchCooperativeKernel((const void *)factor_dw_tc_kernel, dim3((unsigned)grid),
+                                               dim3(kThreads), args, sizeof(DwTcSmem), st));
     inv_block_kernel<<<(unsigned)(npad / SB), kThreads, 0, st>>>(band, f.ld, f.bw, (dw *)f.linv, (dw *)f.linvt);
     CB_CUDA_DW(cudaGetLastError());
     *launches += 2;

@@ -170,6 +170,10 @@ struct BandFactor {
     void *look = nullptr;        // 2 x (32x32 + 32): the next panel's factored block (L, D) and 1/D
     bool fp32 = false;
     bool dw = false;             // double-word band (pairs of floats, band_dw.cu); always direct
+    bool dw_simt = false;        // double-word factor: trailing update on the FP32 pipe instead of the
+                                 // tensor cores (bfloat16 slices, exact FP32 accumulation)
+    void *slices = nullptr;      // tensor-core factor: bfloat16 slices of the panel's W and L rows
+    int *slice_exp = nullptr;    // ... and their row exponents
     bool direct = false;         // no solve blocks: substitution with the band (one solve per factor)
     int solve_grid = 1;          // CTAs of the cooperative solve launch
     int solve_grid_full = 1;     // ... when the handle has the GPU to itself
@@ -194,7 +198,7 @@ void band_free(BandFactor &f);
 // significant bits), the factor and its solves run on the FP32 pipe.
 // band_alloc_dw allocates the band and the block inverses of the solve; the
 // tangent is gathered from FP64 element matrices by band_dw_gather.
-void band_alloc_dw(BandFactor &f, long n, long bw);
+void band_alloc_dw(BandFactor &f, long n, long bw, bool simt = false);
 void band_dw_alloc(BandFactor &f);
 size_t band_dw_extra_bytes(long n, long bw);
 long band_dw_block();  // rows of the solve's blocks (the band is padded to a multiple)

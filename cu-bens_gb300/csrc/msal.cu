@@ -191,7 +191,7 @@ void upload_model(cb_model *m)
     // Newmark and full Newton-Raphson refactor every iteration and solve once
     // per factorisation: direct substitution, no solve blocks
     if (dwp)
-        cb::band_alloc_dw(m->bf, N, h.bw);
+        cb::band_alloc_dw(m->bf, N, h.bw, m->opt.factor_kernel == 1);
     else
         cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5 || h.alg == 1 || m->opt.band_solve == 1,
                        m->opt.factor_kernel == 1);

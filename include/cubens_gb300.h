@@ -85,7 +85,9 @@ typedef struct {
     int factor_kernel;   /* band LDL^T in FP32: 0 the cooperative grid factor; 1 the
                             thread-block-cluster factor where the band's window fits a cluster's
                             distributed shared memory (measured slower on GB300: the grid factor
-                            stays the default) */
+                            stays the default). In CB_FP32X2: 0 the trailing update on the
+                            tensor cores (six bfloat16 slices per value, exact FP32
+                            accumulation); 1 on the FP32 pipe in double-word arithmetic */
     int band_solve;      /* band LDL^T solves: 0 (default) block-bidiagonal solve with the
                             factor's block inverses for arc-length and modified Newton-Raphson
                             models, direct substitution for the others; 1 direct substitution
