@@ -79,6 +79,16 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def bf16_peak():
+    """Sustained dense bf16 TFLOP/s (a kernel timed inside a long step)."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if "bf16_tflops_sustained" in d:
+            return d["bf16_tflops_sustained"], "measured"
+    return 1700.0, "fallback"
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -827,14 +837,16 @@ def run_large(args, world, rank, local, pg):
     timed = recs[1 + args.warmup:]
     n, bw = info["neq"], info["bandwidth"]
     fma = n * bw * bw / 2.0                        # band LDL^T multiply-adds per factorisation
-    fp32_ops = fma * 12.0                          # a double-word multiply-add: 12 FP32 instructions
-    fp32_peak = 152 * 128 * 2.07e9                 # FP32 lanes x clock (nominal), instructions/s
+    tc_flops = fma * 21 * 2.0                      # bfloat16 slice products executed on the tensor cores
+    tc_peak, tc_peak_kind = bf16_peak()
     achieved = bytes_ldlt / (ms_ldlt * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64 forces/residual/arc-length; f64 tangent; band LDL^T and solves in double-word f32 (~48-bit)",
+        "dtype": "f64 forces/residual/arc-length; f64 tangent; band LDL^T in double-word f32 (~48-bit) with its "
+                 "trailing update as bf16 slice products on the tensor cores (exact f32 accumulation); solves in "
+                 "double-word f32",
         "data": "synthetic",
         "config": {"workload": LARGE_WORKLOAD, "neq": n, "bandwidth": bw, "seed": LARGE_SEED,
                    "imperfection": f"{LARGE_IMP} t, modes (1,1),(1,2),(2,1),(2,2)", "controls": LARGE_CONTROLS,
@@ -860,21 +872,27 @@ def run_large(args, world, rank, local, pg):
                    "shell_force_GBps": bytes_force / (ms_force * 1e-3) / 1e9,
                    "fp32_band_ldlt": "diverges at this size (first increment: lambda 615 after the first solve "
                                      "against 81.45, no convergence in 100 iterations); not a leg"},
-        "roofline": {"kernel": "factor_dw_kernel (persistent band LDL^T, double-word FP32, two grid barriers per "
-                               "64-column panel)",
-                     "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "traffic": (TRAFFIC_DW_256 * (n * (bw + 5)) / (394752 * 1552)) if TRAFFIC_DW_256 else None,
-                     "traffic_source": "profiles/factor_dw_kernel_panel256.md (one launch on the 256 x 256 panel, "
-                                       "scaled by n ld)",
-                     "bytes_per_launch": bytes_ldlt, "ms_per_launch": ms_ldlt,
-                     "note": "compute-bound on the FP32 pipe: bytes = the band read and written once; the pipe "
-                             "figure is in roofline_compute"},
-        "roofline_compute": {"kernel": "factor_dw_kernel", "bound": "fp32 pipe",
-                             "achieved": fp32_ops / (ms_ldlt * 1e-3) / 1e12, "peak": fp32_peak / 1e12,
-                             "unit": "T FP32 instructions/s", "frac": fp32_ops / (ms_ldlt * 1e-3) / fp32_peak,
-                             "peak_kind": "nominal (152 SMs x 128 FP32 lanes x 2.07 GHz)",
-                             "work": f"n bw^2 / 2 = {fma:.3e} double-word multiply-adds x 12 FP32 instructions"},
+        "roofline": {"kernel": "factor_dw_tc_kernel (persistent band LDL^T in double-word FP32, trailing update "
+                               "on the tensor cores: 21 bfloat16 slice products per multiply-add, mma.sync)",
+                     "bound": "tensor", "achieved": tc_flops / (ms_ldlt * 1e-3) / 1e12, "peak": tc_peak,
+                     "unit": "TFLOP/s", "frac": tc_flops / (ms_ldlt * 1e-3) / 1e12 / tc_peak,
+                     "peak_kind": f"{tc_peak_kind} (cuBLAS bf16, sustained: the kernel runs inside a long step)",
+                     "traffic": (TRAFFIC_TC_512x32 * (n * (bw + 5)) / (101376 * 3088)) if TRAFFIC_TC_512x32 else None,
+                     "traffic_source": "profiles/factor_dw_tc_kernel_panel512.md (one launch on the 512 x 32 "
+                                       "panel, the same band, scaled by n ld)",
+                     "work": f"n bw^2 / 2 = {fma:.3e} double-word multiply-adds x 21 slice products x 2 flops",
+                     "ms_per_launch": ms_ldlt,
+                     "mma_sync_ceiling_tflops": MMA_SYNC_TFLOPS,
+                     "frac_of_mma_sync_ceiling": tc_flops / (ms_ldlt * 1e-3) / 1e12 / MMA_SYNC_TFLOPS,
+                     "note": "mma.sync (bf16, m16n8k16) peaks near 600 TFLOP/s on GB300, below the tcgen05 rate "
+                             "that cuBLAS reaches; the band's bytes (read and written once) are in roofline_hbm"},
+        "roofline_hbm": {"kernel": "factor_dw_tc_kernel", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                         "bytes_per_launch": bytes_ldlt},
+        "fp64_equivalent": {"kernel": "factor_dw_tc_kernel", "achieved": 2 * fma / (ms_ldlt * 1e-3) / 1e12,
+                            "unit": "TFLOP/s of ~48-bit multiply-adds (2 per)",
+                            "fp64_band_factor_tflops": 2 * fma / (tm64["ms_factor"] * 1e-3) / 1e12,
+                            "note": "the same factorisation in native FP64 on GB300's FP64 pipe (the plain leg)"},
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
         "e2e": e2e, "clocks": clk, "gpu_launches": launches,
     }
@@ -940,9 +958,11 @@ def run_reference_large(args, world, rank, pg):
     print(json.dumps(line), flush=True)
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one factor_dw_kernel launch on the 256 x 256
-# panel (NEQ 394,752, ld 1,552), from profiles/factor_dw_kernel_panel256.md
-TRAFFIC_DW_256 = 4.972161e9 + 4.856823e9
+# dram__bytes_read.sum + dram__bytes_write.sum of one factor_dw_tc_kernel launch on the 512 x 32
+# panel (NEQ 101,376, ld 3,088), from profiles/factor_dw_tc_kernel_panel512.md
+TRAFFIC_TC_512x32 = 2503401728 + 6141808128
+# bf16 mma.sync m16n8k16 throughput measured on GB300 (all SMs, independent accumulators)
+MMA_SYNC_TFLOPS = 600.0
 
 
 def main():
