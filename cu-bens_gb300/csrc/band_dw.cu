@@ -578,17 +578,23 @@ __global__ void __launch_bounds__(kThreads, 1) factor_dw_tc_kernel(DwFactorArgs 
                         af[sa][2] = *reinterpret_cast<const unsigned *>(ap + 8);
                         af[sa][3] = *reinterpret_cast<const unsigned *>(ap + 8 * SST + 8);
                     }
+                    // consecutive products go to the four column blocks' independent
+                    // accumulators (the shared one of diagonals 3 .. 5 takes 15 of the
+                    // 21 products of a block)
 #pragma unroll
-                    for (int n = 0; n < 4; ++n)
+                    for (int sb = 0; sb < NS; ++sb) {
+                        unsigned bfr[4][2];
 #pragma unroll
-                        for (int sb = 0; sb < NS; ++sb) {
+                        for (int n = 0; n < 4; ++n) {
                             const __nv_bfloat16 *bp = &sm.Ls[b][sb][32 * wc + 8 * n + g][ks + 2 * q];
-                            const unsigned bfr[2] = {*reinterpret_cast<const unsigned *>(bp),
-                                                     *reinterpret_cast<const unsigned *>(bp + 8)};
-#pragma unroll
-                            for (int sa = 0; sa < NS - sb; ++sa)
-                                mma16816(acc[sa + sb < NA ? sa + sb : NA - 1][n], af[sa], bfr);
+                            bfr[n][0] = *reinterpret_cast<const unsigned *>(bp);
+                            bfr[n][1] = *reinterpret_cast<const unsigned *>(bp + 8);
                         }
+#pragma unroll
+                        for (int sa = 0; sa < NS - sb; ++sa)
+#pragma unroll
+                            for (int n = 0; n < 4; ++n) mma16816(acc[sa + sb < NA ? sa + sb : NA - 1][n], af[sa], bfr[n]);
+                    }
                 }
                 __syncthreads();  // the buffer is refilled by the stage after next
                 if (st & 1) {
