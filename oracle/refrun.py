@@ -79,4 +79,4 @@ def run(model_text: str, cap_steps: int, timeout: float = 600.0,
         files = {k: (wd / f"results{k}.txt").read_text() for k in range(2, 6) if (wd / f"results{k}.txt").exists()}
         return dict(neq=neq, steps=steps, iterations=its, lam=lam, d=d, seconds=secs,
                     step_times=np.array(times), testlog=log, returncode=proc.returncode,
-                    stdout=proc.stdout, results1=errors, results=files)
+                    stdout=proc.stdout, stderr=proc.stderr, results1=errors, results=files)
