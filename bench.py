@@ -202,7 +202,9 @@ def cpu_baseline(text: str, target_s: float = 20.0):
     nstep = len(r["t"]) - 1
     secs = r["t"][-1] - r["t"][0]
     return {"value": nstep / secs, "unit": "steps/s", "cores": 1, "kind": "port",
-            "sample": f"oracle port (C restatement, gcc -O2, 1 thread): first increment untimed, "
+            "sample": f"oracle port (C restatement, gcc -O2, 1 thread; bit-identical to the reference's own build "
+                      f"on the reference's fixtures, which the Arm box cannot build: no reference sources there): "
+                      f"first increment untimed, "
                       f"{nstep} arc-length steps timed ({secs:.1f} s), same model",
             "iterations": [int(x) for x in r["its"][1:]], "total_s": time.perf_counter() - t0}
 
@@ -742,7 +744,9 @@ def large_cpu_sample(n_sample: int = 128, steps: int = 2):
     scale = (nf * bf ** 2) / (ns * bs ** 2)
     per_step = secs / steps * scale
     return {"value": 1.0 / per_step, "unit": "steps/s", "cores": 1, "kind": "port",
-            "sample": f"oracle port (C restatement of the reference, gcc -O2, 1 thread): the same panel on a "
+            "sample": f"oracle port (C restatement of the reference, gcc -O2, 1 thread; bit-identical to the "
+                      f"reference's own build on its fixtures; the Arm box has no reference sources): the same "
+                      f"panel on a "
                       f"{n_sample}x{n_sample} mesh (NEQ {ns}), first increment untimed, {steps} arc-length steps "
                       f"in {secs:.1f} s ({[int(x) for x in r['its'][1:]]} iterations), scaled by n bw^2 to NEQ "
                       f"{nf} (x{scale:.0f}): extrapolated, {per_step / 3600:.2f} h per step",
