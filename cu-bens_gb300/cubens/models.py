@@ -305,7 +305,8 @@ def frame_building(bays_x: int = 20, bays_y: int = 20, storeys: int = 30,
                    bay: float = 6.0, storey: float = 3.5, warping: str = "fixed",
                    steps: int = 2000, dt: float = 0.005, rms: float = 5e3, seed: int = 4,
                    loaded_face: bool = True, newmark: NewmarkControls | None = None,
-                   msal: MsalControls | None = None, msal_load: float = 1e3) -> ModelSpec:
+                   msal: MsalControls | None = None, msal_load: float = 1e3, linear: bool = False,
+                   initial: list | None = None) -> ModelSpec:
     """Rigid-jointed 3D frame building of co-rotational 14-DOF frame members.
 
     Joint (i, j, s) at (bay*i, bay*j, storey*s) is number
@@ -323,7 +324,12 @@ def frame_building(bays_x: int = 20, bays_y: int = 20, storeys: int = 30,
     global x at each joint of the floor's x = 0 face (one history per floor,
     ``steps`` + 1 time points of ``dt``). With ``msal`` given the model is an
     MSAL model instead: ``msal_load`` in x at every joint of the roof's x = 0
-    face is the reference load.
+    face is the reference load. With ``linear`` the dynamic model is the
+    reference's linear one (ANAFLAG 1, ALGFLAG 4: one factorisation of the
+    initial effective stiffness, main.c:3143-3302): its controls are
+    ``newmark``'s numopt and spectrds and then lpfmax alone (main.c:3184,
+    3192), and ``initial`` lists (joint, direction, d, v, a) initial
+    conditions.
     """
     bx, by, ns = bays_x, bays_y, storeys
     nper = (bx + 1) * (by + 1)
@@ -364,7 +370,9 @@ def frame_building(bays_x: int = 20, bays_y: int = 20, storeys: int = 30,
         aux.append(",".join(_fmt(x0[k] + off[k]) for k in range(3)))
     face = lambda s: [jid(0, j, s) for j in range(by + 1)]  # noqa: E731
     dynamic = msal is None
-    out = ["2", "5" if dynamic else _alg(msal)]
+    if linear and not dynamic:
+        raise ValueError("a linear (ALGFLAG 4) model is dynamic: give no msal controls")
+    out = ["1" if linear else "2", ("4" if linear else "5") if dynamic else _alg(msal)]
     if dynamic:
         out.append("0,0")                     # CHKPT, RFLAG
     out += ["0", "1", str(len(nodes)), f"0,{len(members)},0,0,0"]
@@ -389,14 +397,20 @@ def frame_building(bays_x: int = 20, bays_y: int = 20, storeys: int = 30,
             joints = face(s) if loaded_face else [jid(0, 0, s)]
             for jt in joints:
                 out += [f"{jt},1,{_fmt(v)}" for v in hist]
-        out += ["0,0,0", "0,0,0", "0,0,0,0,0"]
-        out += (newmark or NewmarkControls()).lines()
+        out += ["0,0,0", "0,0,0"]
+        out += [f"{jt},{dr},{_fmt(d)},{_fmt(v)},{_fmt(a)}" for jt, dr, d, v, a in (initial or [])]
+        out.append("0,0,0,0,0")
+        nm = newmark or NewmarkControls()
+        if linear:
+            out += [f"{nm.numopt},{nm.spectrds!r}", f"{nm.lpfmax!r}"]
+        else:
+            out += nm.lines()
         params.update(steps=steps, dt=dt, rms=rms)
     else:
         out += [f"{jt},1,{_fmt(msal_load)}" for jt in face(ns)] + ["0,0,0"]
         out.append("0,0,0")                   # no distributed loads
         out += msal.lines()
-    name = f"frame{bx}x{by}x{ns}" + ("" if dynamic else "_msal")
+    name = f"frame{bx}x{by}x{ns}" + ("" if dynamic else "_msal") + ("_linear" if linear else "")
     params["members"] = members               # 1-based joint pairs, in input order
     return ModelSpec(name, "\n".join(out) + "\n", nj=len(nodes), ne_fr=len(members),
                      seed=seed if dynamic else None, params=params)

@@ -64,6 +64,8 @@ struct orc_model {
     double dt, ttot, numopt, spectrds, lpf0, dlpf0, dlpfmax, dlpfmin;
     int solmin;
     double *pinpt;   /* NEQ*ntin per-step joint forces */
+    double *um0, *vm0, *am0; /* linear Newmark (ALGFLAG 4): NEQ initial displacements, velocities,
+                                accelerations (load, model.c:1583-1604) */
 };
 
 /* ---- token reader: the model_def layout is positional numbers ---- */
@@ -318,6 +320,9 @@ void orc_free(orc_model *m)
     free(m->fr_c0);
     free(m->fr_mc);
     free(m->pinpt);
+    free(m->um0);
+    free(m->vm0);
+    free(m->am0);
     free(m);
 }
 
@@ -353,8 +358,9 @@ orc_model *orc_load(const char *text, char *err, int errlen)
     orc_model *m = calloc(1, sizeof *m);
     int ana = (int)tok_num(&t);
     int alg = (int)tok_num(&t);
-    if (ana != 2 || (alg != 3 && alg != 5))
-        return load_fail(m, err, errlen, "oracle supports ANAFLAG 2 with ALGFLAG 3 (MSAL) or 5 (Newmark)");
+    if (!((ana == 2 && (alg == 3 || alg == 5)) || (ana == 1 && alg == 4)))
+        return load_fail(m, err, errlen, "oracle supports ANAFLAG 2 with ALGFLAG 3 (MSAL) or 5 (Newmark), "
+                                         "and ANAFLAG 1 with ALGFLAG 4 (linear Newmark)");
     m->alg = alg;
     if (alg > 3) {
         int chkpt = (int)tok_num(&t), rflag = (int)tok_num(&t);
@@ -370,7 +376,7 @@ orc_model *orc_load(const char *text, char *err, int errlen)
     m->ne_sh = (long)tok_num(&t);
     long nsbr = (long)tok_num(&t), nfbr = (long)tok_num(&t);
     if (nsbr || nfbr || !t.ok) return load_fail(m, err, errlen, "brick elements are not supported");
-    if (alg == 5 && (m->ne_tr || m->ne_sh))
+    if (alg >= 4 && (m->ne_tr || m->ne_sh))
         return load_fail(m, err, errlen, "the Newmark oracle supports frame-only models");
     long NJ = m->nj;
     m->tr_conn = calloc((size_t)(2 * m->ne_tr + 1), sizeof(long));
@@ -604,7 +610,7 @@ orc_model *orc_load(const char *text, char *err, int errlen)
             long dir = (long)tok_num(&t);
             double mag = tok_num(&t);
             if (!t.ok || jt == 0) break;
-            if (mag == 0) mag = 1e-30;
+            if (alg == 5 && mag == 0) mag = 1e-30;
             long ks = m->jcode[(jt - 1) * 7 + dir - 1];
             if (ks != kps) i = 0;
             if (ks != 0 && i < m->ntin) m->pinpt[(ks - 1) * m->ntin + i] = mag;
@@ -616,10 +622,33 @@ orc_model *orc_load(const char *text, char *err, int errlen)
         (void)tok_num(&t);
         (void)tok_num(&t);
         if (jt != 0) return load_fail(m, err, errlen, "prescribed displacements are not supported");
+        /* initial conditions: kept by the linear driver only, since the
+         * nonlinear one zeroes its motion before the first step */
+        m->um0 = calloc((size_t)neq + 1, sizeof(double));
+        m->vm0 = calloc((size_t)neq + 1, sizeof(double));
+        m->am0 = calloc((size_t)neq + 1, sizeof(double));
         for (;;) {
             jt = (long)tok_num(&t);
-            for (int k = 0; k < 4; ++k) (void)tok_num(&t);
+            long dir = (long)tok_num(&t);
+            double d0 = tok_num(&t), v0 = tok_num(&t), a0 = tok_num(&t);
             if (!t.ok || jt == 0) break;
+            if (jt < 1 || jt > NJ || dir < 1 || dir > 7) return load_fail(m, err, errlen, "bad initial condition");
+            long k = m->jcode[(jt - 1) * 7 + dir - 1];
+            if (k != 0) {
+                if (d0 != 0) m->um0[k - 1] = d0;
+                if (v0 != 0) m->vm0[k - 1] = v0;
+                if (a0 != 0) m->am0[k - 1] = a0;
+            }
+        }
+        if (alg == 4) {
+            /* linear Newmark controls (main.c:3184, 3192) */
+            m->numopt = tok_num(&t);
+            m->spectrds = tok_num(&t);
+            m->lpfmax = tok_num(&t);
+            if (!t.ok) return load_fail(m, err, errlen, "model_def ended early");
+            if (m->numopt == 0 && m->spectrds != 1)
+                return load_fail(m, err, errlen, "invalid spectral radius for Newmark without dissipation");
+            return m;
         }
         /* Newmark controls (main.c:3320-3326) */
         m->numopt = tok_num(&t);
@@ -1746,6 +1775,124 @@ done:
  * accepted pass, d[k*NEQ ...] (may be NULL), res[k] = |dyn - f| / |dyn| with
  * dyn = qtot - M a (the dynamic equilibrium the convergence test judges).
  * Returns the number of steps recorded, or -(error code) with err set. */
+/* y = K x for the symmetric skyline K (skymult, solve.c:700-757): column n
+ * holds K(n, n) at maxa[n-1] and the entries above it after; the upper
+ * triangle's columns are applied from the last one, then the diagonal, then
+ * the lower triangle row by row. */
+static void sky_mult(long neq, const long *maxa, const double *ss, const double *x, double *y)
+{
+    for (long i = 0; i < neq; ++i) y[i] = 0;
+    for (long n = neq; n >= 2; --n) {
+        long k = n;
+        for (long kk = maxa[n - 1] + 1; kk <= maxa[n] - 1; ++kk) {
+            --k;
+            y[k - 1] += ss[kk - 1] * x[n - 1];
+        }
+    }
+    for (long n = 0; n < neq; ++n) y[n] += x[n] * ss[maxa[n] - 1];
+    for (long n = neq; n >= 1; --n) {
+        if (maxa[n] - 1 < maxa[n - 1] + 1) continue;
+        long k = n;
+        double c = 0;
+        for (long kk = maxa[n - 1] + 1; kk <= maxa[n] - 1; ++kk) {
+            --k;
+            c += ss[kk - 1] * x[k - 1];
+        }
+        y[n - 1] += c;
+    }
+}
+
+/* Linear Newmark (ANAFLAG 1, ALGFLAG 4; main.c:3143-3302 with the effective
+ * stiffness of solve.c:139-222 and the time loop of solve.c:246-467, SLVFLAG
+ * 0, no prescribed motion, no restart): the stiffness of the initial state
+ * and the lumped mass are formed once, K_eff = K + a0 (1 - am) / (1 - af) M
+ * is factored once, and every time step k solves
+ *   K_eff u = p_k [+ af / (1 - af) p_(k-1)] + M_eff(u_m, v_m, a_m)
+ *             [- af / (1 - af) K u_m]
+ * followed by the Newmark kinematics. Writes per step the time k dt and u. */
+int orc_linear_newmark(orc_model *m, long max_steps, double *time_out, double *dout, char *err, int errlen)
+{
+    if (m->alg != 4) {
+        set_err(err, errlen, "model is not a linear Newmark model (ALGFLAG 4)");
+        return -1;
+    }
+    long N = m->neq, F = m->ne_fr, NT = m->nsteps;
+    if (NT != m->ntin) {
+        set_err(err, errlen, "ttot/dt + 1 differs from the number of input time points");
+        return -1;
+    }
+    size_t nb = sizeof(double) * (size_t)(N + 1);
+    double *ss = malloc(sizeof(double) * (size_t)m->lss), *keff = malloc(sizeof(double) * (size_t)m->lss),
+           *sm = calloc(1, nb), *ssd = calloc(1, nb), *um = calloc(1, nb), *vm = calloc(1, nb),
+           *am = calloc(1, nb), *uc = calloc(1, nb), *vc = calloc(1, nb), *ac = calloc(1, nb),
+           *reff = calloc(1, nb), *ku = calloc(1, nb), *ef0 = calloc((size_t)(14 * F + 1), sizeof(double));
+    double alpham = 0, alphaf = 0;
+    if (m->numopt == 1) {
+        alpham = (2 * m->spectrds - 1) / (m->spectrds + 1);
+        alphaf = m->spectrds / (m->spectrds + 1);
+    } else if (m->numopt == 2) {
+        alphaf = (1 - m->spectrds) / (1 + m->spectrds);
+    } else if (m->numopt == 3) {
+        alpham = (m->spectrds - 1) / (m->spectrds + 1);
+    }
+    const double alpha = pow(1 - alpham + alphaf, 2) / 4, delta = 0.5 - alpham + alphaf;
+    const double dt = m->dt, dt_temp = 1 * dt;
+    const double a0 = 1 / (alpha * pow(dt_temp, 2)), a2 = 1 / (alpha * dt_temp), a3 = 1 / (2 * alpha) - 1;
+    const double a6 = (dt_temp) * (1 - delta), a7 = delta * (dt_temp);
+    /* stiffness of the initial state (the element forces are zero, so the
+     * geometric terms vanish: stiffe alone, as ANAFLAG 1 forms it) and mass */
+    tangent_all(m, m->x0, NULL, NULL, NULL, NULL, NULL, m->fr_c0, ef0, m->fr_len0, m->fr_len0, ss);
+    orc_frame_mass(m, m->x0, sm);
+    memcpy(keff, ss, sizeof(double) * (size_t)m->lss);
+    for (long i = 0; i < N; ++i) keff[m->maxa[i] - 1] += a0 * (1 - alpham) * sm[i] / (1 - alphaf);
+    int det = 0;
+    sky_factor(N, m->maxa, keff, ssd, &det, 1);
+    memcpy(um, m->um0, nb - sizeof(double));
+    memcpy(vm, m->vm0, nb - sizeof(double));
+    memcpy(am, m->am0, nb - sizeof(double));
+    const double *pq = m->pinpt;
+    long k = 0;
+    for (; k < NT && k < max_steps; ++k) {
+        for (long i = 0; i < N; ++i) {
+            const double meff = sm[i] * ((1 - alpham) * (um[i] * a0 + vm[i] * a2 + am[i] * a3) - alpham * am[i]) /
+                                (1 - alphaf);
+            reff[i] = k == 0 ? pq[i * NT + k] + meff
+                             : pq[i * NT + k] + alphaf / (1 - alphaf) * pq[i * NT + k - 1] + meff;
+        }
+        if (alphaf != 0) {
+            sky_mult(N, m->maxa, ss, um, ku);
+            for (long i = 0; i < N; ++i) reff[i] -= alphaf / (1 - alphaf) * ku[i];
+        }
+        sky_solve(N, m->maxa, keff, reff);
+        for (long i = 0; i < N; ++i) {
+            uc[i] = reff[i];
+            ac[i] = a0 * (uc[i] - um[i]) - a2 * vm[i] - a3 * am[i];
+            vc[i] = vm[i] + a6 * am[i] + a7 * ac[i];
+        }
+        time_out[k] = k * dt;
+        if (dout) memcpy(dout + (size_t)k * N, uc, sizeof(double) * (size_t)N);
+        for (long i = 0; i < N; ++i) {
+            um[i] = uc[i];
+            vm[i] = vc[i];
+            am[i] = ac[i];
+        }
+    }
+    free(ss);
+    free(keff);
+    free(sm);
+    free(ssd);
+    free(um);
+    free(vm);
+    free(am);
+    free(uc);
+    free(vc);
+    free(ac);
+    free(reff);
+    free(ku);
+    free(ef0);
+    return (int)k;
+}
+
 int orc_newmark(orc_model *m, long max_steps, double *time_out, int *its_out, double *dout,
                 double *res_out, char *err, int errlen)
 {

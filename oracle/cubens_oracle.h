@@ -47,6 +47,8 @@ int orc_msal_timed(orc_model *m, int max_steps, double *lam, int *its, double *d
 /* Nonlinear Newmark time loop (main.c:3305-3960). Per recorded time step k:
  * time[k], its[k], d[k*NEQ ...] (d may be NULL), res[k] = |dyn - f| / |dyn|.
  * Returns the number of steps recorded, or -(error code) with err set. */
+/* linear Newmark (ANAFLAG 1, ALGFLAG 4): per step the time and the displacements */
+int orc_linear_newmark(orc_model *m, long max_steps, double *time, double *d, char *err, int errlen);
 int orc_newmark(orc_model *m, long max_steps, double *time, int *its, double *d, double *res,
                 char *err, int errlen);
 

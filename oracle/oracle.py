@@ -47,6 +47,8 @@ def lib():
         L.orc_skyline_solve.argtypes = [P, dp, dp, dp, ip, C.c_int]
         L.orc_shell_initial.argtypes = [P, dp, dp]
         L.orc_dyn_sizes.argtypes = [P, lp, dp]
+        L.orc_linear_newmark.restype = C.c_int
+        L.orc_linear_newmark.argtypes = [P, C.c_long, dp, dp, C.c_char_p, C.c_int]
         L.orc_newmark.restype = C.c_int
         L.orc_newmark.argtypes = [P, C.c_long, dp, ip, dp, dp, C.c_char_p, C.c_int]
         L.orc_frame_initial.argtypes = [P, dp, dp]
@@ -136,6 +138,16 @@ class OracleModel:
         k = max(n, 0)
         return dict(rc=n, error=err.value.decode(), time=t[:k], its=its[:k], res=res[:k],
                     d=d[:k] if keep_d else None)
+
+    def linear_newmark(self, steps: int):
+        """Linear Newmark run (ALGFLAG 4): per time step the time and d."""
+        t = np.zeros(steps)
+        d = np.zeros((steps, self.neq))
+        err = C.create_string_buffer(256)
+        n = lib().orc_linear_newmark(self.h, steps, _d(t), _d(d), err, 256)
+        if n < 0:
+            raise ValueError(err.value.decode())
+        return dict(rc=n, time=t[:n], d=d[:n])
 
     def frame_initial(self):
         c = np.zeros(self.ne_fr * 9)

@@ -147,6 +147,30 @@ def results_fixtures():
                         files=np.array(files), steps=np.array([results_cases()[n][1] for n in names]))
 
 
+def linear_cases():
+    """Linear Newmark frames (ANAFLAG 1, ALGFLAG 4) with initial conditions:
+    numopt 1 (HHT-type dissipation, so the K u_m term of the effective load
+    is active), warping fixed and one warping DOF per member end."""
+    nm = models.NewmarkControls(numopt=1, spectrds=0.8)
+    init = [(20, 1, 0.001, 0.01, 0.0), (30, 2, 0.0, -0.02, 0.5)]
+    return {w: models.frame_building(2, 2, 3, warping=w, steps=40, dt=0.005, seed=3, linear=True, newmark=nm,
+                                     initial=init)
+            for w in ("fixed", "member")}
+
+
+def linear_runs():
+    """The reference's own linear Newmark runs: per time step the time and d
+    (output() records; the reference's closing record, lpfmax with zero d, is
+    dropped)."""
+    for w, m in linear_cases().items():
+        r = refrun.run(m.text, 1000, timeout=600)
+        assert r["returncode"] == 0, r["results1"][-400:]
+        n = len(r["lam"]) - 1
+        np.savez_compressed(OUT / f"run_frame_linear_{w}.npz", model_def=np.array(m.text), time=r["lam"][:n],
+                            d=r["d"][:n], neq=r["neq"], results_tail=np.array(r["results1"][-200:]))
+        print("linear", w, "neq", r["neq"], "steps", n)
+
+
 def results1_cases():
     """Models whose whole results1.txt (the input echo and the run's
     messages) is pinned: the results2-5 cases, the frame with one warping DOF
@@ -424,3 +448,4 @@ if __name__ == "__main__":
     newton_runs()
     results_fixtures()
     results1_fixtures()
+    linear_runs()

@@ -98,3 +98,16 @@ def test_frame_forces_tangent_mass_match_reference(golden_dir):
     np.testing.assert_allclose(ss, z["ss"], rtol=0, atol=1e-12 * np.abs(z["ss"]).max())
     sm = o.frame_mass(z["x_after"])
     np.testing.assert_array_equal(sm, z["sm"])
+
+
+@pytest.mark.parametrize("warping", ["fixed", "member"])
+def test_linear_newmark_path_matches_reference(golden_dir, warping):
+    """Linear Newmark (ANAFLAG 1, ALGFLAG 4) with HHT-type dissipation and
+    initial conditions: the oracle's displacements per time step equal the
+    reference's bit for bit."""
+    z = np.load(golden_dir / f"run_frame_linear_{warping}.npz")
+    steps = len(z["time"])
+    o = oracle.OracleModel(str(z["model_def"])).linear_newmark(steps)
+    assert o["rc"] == steps
+    np.testing.assert_array_equal(o["time"], z["time"])
+    np.testing.assert_array_equal(o["d"], z["d"])
