@@ -55,6 +55,8 @@ std::string input_echo(const HostModel &m)
     if (alg < 4) {
         if (ana == 2) put(s, "Analysis Type:\n\t2nd Order Elastic\n");
         else if (ana == 3) put(s, "Analysis Type:\n\t2nd Order Inelastic\n");
+    } else if (ana == 1 && alg == 4) {
+        put(s, "Analysis Type:\n\t1st Order Elastic Dynamic\n");
     } else if (ana == 2 && alg == 5) {
         put(s, "Analysis Type:\n\t2nd Order Elastic Dynamic\n");
     } else if (ana == 3 && alg == 5) {

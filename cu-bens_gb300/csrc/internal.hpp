@@ -45,13 +45,14 @@ struct HostModel {
     std::vector<double> fr_prop;  // NE_FR*8, per member: E, G, rho, A, I strong, I weak, J, I warping
     std::vector<double> fr_aux;   // NE_FR*3 auxiliary points
     std::vector<long> fr_mc;      // NE_FR*14 1-based equation numbers (0 = fixed), warping per member
-    int alg = 3;                  // ALGFLAG: 1 NR, 2 modified NR, 3 MSAL, 5 nonlinear Newmark
+    int alg = 3;                  // ALGFLAG: 1 NR, 2 modified NR, 3 MSAL, 4 linear Newmark, 5 nonlinear Newmark
     // nonlinear Newmark input (main.c:1600-1607, 3320-3326; load, model.c:1492-1609)
     long ntin = 0;                // input time points
     long nsteps = 0;              // NTSTPS = (long)(ttot/dt + 1)
     double dt = 0, ttot = 0, numopt = 0, spectrds = 1, lpf0 = 1, dlpf0 = 1, dlpfmax = 1, dlpfmin = 1;
     int solmin = 1;
     std::vector<double> pin;      // ntin*NEQ joint forces, time-major: pin[k*NEQ + i]
+    std::vector<double> um0, vm0, am0;  // NEQ initial displacements, velocities, accelerations (ALGFLAG 4)
     // MSAL controls (arc.c:48, main.c:2240-2245)
     long dkdof = -1;
     double dk = 0, alpha = 1, psi_thresh = 0.1, lpfmax = 0, dkimax = 0;
@@ -457,6 +458,15 @@ void launch_nm_keff(T *band, long ld, const double *sm, double c0, double den, l
 void launch_nm_update(double *dd, int neg, double *d_temp, const double *um, const double *vm, const double *am,
                       double *uc_i, double *vc_i, double *ac_i, double a0, double a2, double a3, double a6,
                       double a7, const int *eq_x, double *x_t, long n, cudaStream_t st);
+// Linear Newmark (solve.c:246-467): the effective load of time step k,
+// reff = p_k [+ c p_(k-1)] + M_eff(um, vm, am) [- c K um] with c = af / (1 - af)
+// (nku = -K um, or null when af = 0), and after the solve u = uc the
+// kinematics ac, vc, then (um, vm, am) <- (uc, vc, ac) and d = uc
+void launch_lin_reff(int first, double alpham, double alphaf, double a0, double a2, double a3,
+                     const double *pin_km1, const double *pin_k, const double *sm, const double *um,
+                     const double *vm, const double *am, const double *nku, double *reff, long n, cudaStream_t st);
+void launch_lin_update(const double *uc, double *um, double *vm, double *am, double *vc, double *ac, double *d,
+                       double a0, double a2, double a3, double a6, double a7, long n, cudaStream_t st);
 // dyn = qtot - sm ac_i, the test sums -> sc->dots[0..6], intener1 on the first
 // iteration, convchk / test_err
 void launch_nm_test(const double *dd, const double *dt, const double *f, const double *fp, const double *fip,

@@ -55,18 +55,23 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
     }
     int alg = (int)t.next();
     if (!t.ok) return "empty model_def";
-    if (ana != 2) {
+    if (!(ana == 2 || (ana == 1 && alg == 4))) {
         status = CB_ERR_UNSUPPORTED;
-        return "only ANAFLAG 2 (second-order elastic) is on the GPU path";
+        return "the GPU path takes ANAFLAG 2 (second-order elastic), and ANAFLAG 1 (first-order elastic) with "
+               "ALGFLAG 4 (linear Newmark)";
     }
-    if (alg != 1 && alg != 2 && alg != 3 && alg != 5) {
+    if (alg == 4 && ana != 1) {
+        status = CB_ERR_UNSUPPORTED;
+        return "ALGFLAG 4 (linear Newmark) is a first-order elastic analysis: ANAFLAG 1 (main.c:393)";
+    }
+    if (alg != 1 && alg != 2 && alg != 3 && alg != 4 && alg != 5) {
         status = CB_ERR_UNSUPPORTED;
         return "only ALGFLAG 1 and 2 (static Newton-Raphson, modified Newton-Raphson), 3 (modified spherical "
-               "arc length) and 5 (nonlinear Newmark) are on the GPU path";
+               "arc length), 4 (linear Newmark) and 5 (nonlinear Newmark) are on the GPU path";
     }
     m.alg = alg;
     m.echo.ana = ana;
-    if (alg == 5) {
+    if (alg >= 4) {
         (void)t.next();  // CHKPT
         int rflag = (int)t.next();
         if (rflag != 0) {
@@ -94,7 +99,7 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         status = CB_ERR_UNSUPPORTED;
         return "brick elements are not on the GPU path";
     }
-    if (alg == 5 && (m.ne_tr || m.ne_sh)) {
+    if (alg >= 4 && (m.ne_tr || m.ne_sh)) {
         status = CB_ERR_UNSUPPORTED;
         return "the GPU Newmark path takes frame-only models (mass_fr indexes its properties without "
                "the truss offset, frame.c:1357-1363)";
@@ -179,7 +184,7 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
                 }
             }
     }
-    if (alg == 5) {
+    if (alg >= 4) {
         // prescribed support motion list (skylin, model.c:1156-1201)
         long j = (long)t.next();
         (void)t.next();
@@ -268,10 +273,10 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
     }
     if (!t.ok) return "model_def ended inside the properties";
     m.q.assign(neq, 0.0);
-    if (alg == 5) {
+    if (alg >= 4) {
         // time points (main.c:1600-1607) and per-step joint forces (load,
         // model.c:1516-1549): the lines of one DOF are consecutive time
-        // points; a zero force is stored as 1e-30
+        // points; in a nonlinear Newmark model a zero force is stored as 1e-30
         long ntsteps = (long)t.next();
         m.ttot = t.next();
         if (!t.ok || ntsteps <= 0) return "bad time-step line";
@@ -291,7 +296,7 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
             if (!t.ok) return "joint load list not terminated";
             if (jt == 0) break;
             if (jt < 0 || jt > NJ || dir < 1 || dir > 7) return "joint load out of range";
-            if (mag == 0) mag = 1e-30;
+            if (alg == 5 && mag == 0) mag = 1e-30;
             long ks = m.jcode[(jt - 1) * 7 + dir - 1];
             if (ks != kps) i = 0;
             if (ks != 0) {
@@ -309,13 +314,35 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
             status = CB_ERR_UNSUPPORTED;
             return "prescribed displacements are not supported";
         }
-        // initial conditions: read and dropped, since the reference zeroes
-        // uc, vc and ac before the first step (main.c:3440-3443)
+        // initial conditions (load, model.c:1583-1604): the linear driver
+        // starts from them; the nonlinear one zeroes its motion before the
+        // first step (main.c:3440-3443)
+        m.um0.assign(neq, 0.0);
+        m.vm0.assign(neq, 0.0);
+        m.am0.assign(neq, 0.0);
         for (;;) {
             jt = (long)t.next();
-            for (int k = 0; k < 4; ++k) (void)t.next();
+            const long dir = (long)t.next();
+            const double d0 = t.next(), v0 = t.next(), a0 = t.next();
             if (!t.ok) return "initial condition list not terminated";
             if (jt == 0) break;
+            if (jt < 0 || jt > NJ || dir < 1 || dir > 7) return "initial condition out of range";
+            const long k = m.jcode[(jt - 1) * 7 + dir - 1];
+            if (k != 0) {
+                if (d0 != 0) m.um0[k - 1] = d0;
+                if (v0 != 0) m.vm0[k - 1] = v0;
+                if (a0 != 0) m.am0[k - 1] = a0;
+            }
+        }
+        if (alg == 4) {
+            // linear Newmark controls (main.c:3184, 3192)
+            m.numopt = t.next();
+            m.spectrds = t.next();
+            m.lpfmax = t.next();
+            if (!t.ok) return "model_def ended inside the linear Newmark controls";
+            if (m.numopt == 0 && m.spectrds != 1) return "invalid spectral radius for Newmark without dissipation";
+            status = CB_OK;
+            return "";
         }
         m.numopt = t.next();
         m.spectrds = t.next();

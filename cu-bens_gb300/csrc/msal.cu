@@ -148,7 +148,7 @@ void upload_model(cb_model *m)
         d2d(fr.len_c, fr.len0, F, st);
         d2d(m->fr_lref, fr.len0, F, st);
     }
-    if (h.alg == 5) {
+    if (h.alg >= 4) {
         for (double **v : {&m->uc, &m->vc, &m->ac, &m->uc_i, &m->vc_i, &m->ac_i, &m->um, &m->vm, &m->am, &m->sm,
                            &m->qtot, &m->dyn, &m->fp})
             *v = m->alloc<double>(N);
@@ -193,7 +193,7 @@ void upload_model(cb_model *m)
     if (dwp)
         cb::band_alloc_dw(m->bf, N, h.bw, m->opt.factor_kernel == 1);
     else
-        cb::band_alloc(m->bf, N, h.bw, fp32, h.alg == 5 || h.alg == 1 || m->opt.band_solve == 1,
+        cb::band_alloc(m->bf, N, h.bw, fp32, h.alg >= 4 || h.alg == 1 || m->opt.band_solve == 1,
                        m->opt.factor_kernel == 1);
     m->bytes += m->bf.bytes;
     cb::build_tangent_map(h, m->bf.ld, tm);
@@ -209,6 +209,12 @@ void upload_model(cb_model *m)
     if (fp32 && h.alg == 5) {
         m->band64 = m->alloc<double>((size_t)m->bf.ld * m->bf.nblk * m->bf.s);
         m->kel64 = m->alloc<double>(105 * F);
+        for (double **v : {&m->ref_r, &m->ref_x, &m->ref_w}) *v = m->alloc<double>(N);
+    }
+    if (h.alg == 4) {
+        // linear Newmark: the stiffness kept beside the factored K_eff (K u_m
+        // of the effective load), and work vectors of the band product
+        m->band64 = m->alloc<double>((size_t)m->bf.ld * m->bf.nblk * m->bf.s);
         for (double **v : {&m->ref_r, &m->ref_x, &m->ref_w}) *v = m->alloc<double>(N);
     }
     m->sc = m->alloc<cb::MsalScalars>(1);
@@ -748,6 +754,11 @@ int cb_model_create(const char *model_def, size_t len, const cb_options *opt, cb
         m->err = "unknown solver";
         *out = m;
         return CB_ERR_ARG;
+    }
+    if (m->h.alg == 4 && (m->opt.solver != CB_SOLVER_BAND || m->opt.precision != CB_FP64)) {
+        m->err = "the linear Newmark driver (ALGFLAG 4) factors its effective stiffness once with the FP64 band";
+        *out = m;
+        return CB_ERR_UNSUPPORTED;
     }
     if (m->opt.solver == CB_SOLVER_FGMRES && m->h.alg != 5 && m->h.alg != 3) {
         m->err = "the FGMRES solver serves the nonlinear Newmark and arc-length drivers; static "

@@ -393,6 +393,104 @@ void newmark_step(cb_model *m, cb_step *out)
     if (m->nm_k >= h.nsteps) m->nm_phase = 2;
 }
 
+// ---- linear Newmark (ANAFLAG 1, ALGFLAG 4): main.c:3143-3302 with the
+// effective stiffness of solve.c:139-222 and the time loop of solve.c:246-467
+// (SLVFLAG 0, no prescribed motion, no restart) ----
+
+struct LinearCoeffs {
+    double a0, a2, a3, a6, a7;
+};
+
+LinearCoeffs linear_coeffs(const NewmarkParams &p, double dt)
+{
+    const double dt_temp = 1 * dt;  // the solve's ddt is 1 (main.c:3268)
+    return LinearCoeffs{1 / (p.alpha * std::pow(dt_temp, 2)), 1 / (p.alpha * dt_temp), 1 / (2 * p.alpha) - 1,
+                        (dt_temp) * (1 - p.delta), p.delta * (dt_temp)};
+}
+
+// The stiffness of the initial state (the element forces are zero, so the
+// frame tangent is stiffe alone, as ANAFLAG 1 forms it), kept for K u_m; the
+// lumped mass; K_eff = K + a0 (1 - am) / (1 - af) M factored once; the
+// motion from the initial conditions.
+void linear_begin(cb_model *m)
+{
+    newmark_begin(m);
+    const cb::HostModel &h = m->h;
+    const long N = h.neq, F = h.ne_fr;
+    cudaStream_t st = m->st;
+    const NewmarkParams p = newmark_params(h);
+    const LinearCoeffs c = linear_coeffs(p, h.dt);
+    assemble_tangent(m, TangentState::converged);
+    d2d(m->band64, (const double *)m->bf.band, (size_t)m->bf.ld * m->bf.nblk * m->bf.s, st);
+    {
+        PhaseTimer t(m, &m->tm.ms_tangent);
+        cb::launch_frame_mass(m->fr, m->x_c, m->fr_lref, m->me, F, st);
+        cb::launch_gather_f64(m->fmap_ptr, m->fmap_src, m->me, m->sm, N, st);
+        cb::launch_nm_keff<double>((double *)m->bf.band, m->bf.ld, m->sm, c.a0 * (1 - p.alpham), 1 - p.alphaf, N,
+                                   st);
+        m->tm.launches += 3;
+    }
+    factor(m);
+    h2d(m->um, h.um0.data(), N, st);
+    h2d(m->vm, h.vm0.data(), N, st);
+    h2d(m->am, h.am0.data(), N, st);
+    (void)pull_scalars(m);  // a timed-out factorisation barrier is reported here
+}
+
+// time step k: K_eff uc = p_k [+ af/(1-af) p_(k-1)] + M_eff [- af/(1-af) K u_m],
+// then the kinematics
+void linear_step(cb_model *m, cb_step *out)
+{
+    const cb::HostModel &h = m->h;
+    const long N = h.neq;
+    cudaStream_t st = m->st;
+    out->done = 0;
+    if (m->nm_k >= h.nsteps) {
+        ref_success(m, "\nSolution successful!!\n");  // main.c:3300-3302
+        out->done = 1;
+        out->lam = (double)(h.nsteps - 1) * h.dt;
+        out->iterations = 0;
+        out->attempts = 0;
+        out->residual = 0;
+        out->dk = 0;
+        return;
+    }
+    const long k = m->nm_k;
+    const NewmarkParams p = newmark_params(h);
+    const LinearCoeffs c = linear_coeffs(p, h.dt);
+    const double *pin_k = m->pin + (size_t)k * N;
+    const double *pin_km1 = k > 0 ? m->pin + (size_t)(k - 1) * N : pin_k;
+    {
+        PhaseTimer t(m, &m->tm.ms_vector);
+        const double *nku = nullptr;
+        if (p.alphaf != 0) {
+            // -K u_m from the kept stiffness (the band product r = b - K x with b = 0)
+            CB_CUDA(cudaMemsetAsync(m->ref_x, 0, N * sizeof(double), st));
+            cb::band_residual64(m->band64, m->bf.ld, m->bf.bw, N, m->ref_x, m->um, m->ref_r, m->ref_w, st);
+            nku = m->ref_r;
+            m->tm.launches += 2;
+        }
+        cb::launch_lin_reff(k == 0, p.alpham, p.alphaf, c.a0, c.a2, c.a3, pin_km1, pin_k, m->sm, m->um, m->vm, m->am,
+                            nku, m->r, N, st);
+        m->tm.launches += 1;
+    }
+    solve(m, m->r, m->uc);
+    {
+        PhaseTimer t(m, &m->tm.ms_vector);
+        cb::launch_lin_update(m->uc, m->um, m->vm, m->am, m->vc, m->ac, m->d, c.a0, c.a2, c.a3, c.a6, c.a7, N, st);
+        m->tm.launches += 1;
+    }
+    (void)pull_scalars(m);  // one synchronisation; a timed-out solve barrier is reported
+    out->lam = (double)k * h.dt;
+    out->iterations = 0;
+    out->attempts = 1;
+    out->residual = 0;
+    out->dk = 0;
+    m->itecnt = 0;
+    m->nm_k = k + 1;
+    if (m->nm_k >= h.nsteps) m->nm_phase = 2;
+}
+
 }  // namespace
 
 extern "C" {
@@ -400,11 +498,14 @@ extern "C" {
 int cb_newmark_begin(cb_model *m)
 {
     if (!m || !m->st) return CB_ERR_ARG;
-    if (m->h.alg != 5) {
-        m->err = "cb_newmark_begin needs an ALGFLAG 5 (nonlinear Newmark) model";
+    if (m->h.alg != 5 && m->h.alg != 4) {
+        m->err = "cb_newmark_begin needs an ALGFLAG 5 (nonlinear Newmark) or ALGFLAG 4 (linear Newmark) model";
         return CB_ERR_STATE;
     }
-    return guarded(m, [&] { newmark_begin(m); });
+    return guarded(m, [&] {
+        if (m->h.alg == 4) linear_begin(m);
+        else newmark_begin(m);
+    });
 }
 
 int cb_newmark_step(cb_model *m, cb_step *out)
@@ -414,7 +515,10 @@ int cb_newmark_step(cb_model *m, cb_step *out)
         m->err = "cb_newmark_begin has not completed";
         return CB_ERR_STATE;
     }
-    return guarded(m, [&] { newmark_step(m, out); });
+    return guarded(m, [&] {
+        if (m->h.alg == 4) linear_step(m, out);
+        else newmark_step(m, out);
+    });
 }
 
 int cb_set_krylov_tolerance(cb_model *m, double rtol)
@@ -511,7 +615,7 @@ int cb_mpnn_eval(cb_model *m, const double *r, const double *p, const double *t,
 
 int cb_newmark_state(const cb_model *m, double *u, double *v, double *a)
 {
-    if (!m || m->h.alg != 5) return CB_ERR_ARG;
+    if (!m || (m->h.alg != 5 && m->h.alg != 4)) return CB_ERR_ARG;
     cb_model *mm = const_cast<cb_model *>(m);
     return guarded(mm, [&] {
         const long N = m->h.neq;

@@ -346,6 +346,46 @@ __global__ void nm_keff_kernel(T *__restrict__ band, long ld, const double *__re
     band[i * ld] = (T)((double)band[i * ld] + add);
 }
 
+// Linear Newmark effective load (solve.c:349-385; i-th equation):
+// M_eff = sm ((1 - am)(um a0 + vm a2 + am a3) - am am) / (1 - af),
+// reff = p_k + M_eff on the first step, p_k + af/(1-af) p_(k-1) + M_eff after,
+// then reff -= af/(1-af) (K um) when af != 0 (nku holds -K um).
+__global__ void lin_reff_kernel(int first, double alpham, double alphaf, double a0, double a2, double a3,
+                                const double *__restrict__ pin_km1, const double *__restrict__ pin_k,
+                                const double *__restrict__ sm, const double *__restrict__ um,
+                                const double *__restrict__ vm, const double *__restrict__ am,
+                                const double *__restrict__ nku, double *__restrict__ reff, long n)
+{
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double meff = sm[i] * ((1 - alpham) * (um[i] * a0 + vm[i] * a2 + am[i] * a3) - alpham * am[i]) /
+                        (1 - alphaf);
+    const double c = alphaf / (1 - alphaf);
+    double r = first ? pin_k[i] + meff : pin_k[i] + c * pin_km1[i] + meff;
+    if (nku) r -= c * (-nku[i]);
+    reff[i] = r;
+}
+
+// Linear Newmark kinematics (solve.c:434-452): ac, vc from the solution uc,
+// then the step's motion becomes the previous one; d mirrors uc.
+__global__ void lin_update_kernel(const double *__restrict__ uc, double *__restrict__ um, double *__restrict__ vm,
+                                  double *__restrict__ am, double *__restrict__ vc, double *__restrict__ ac,
+                                  double *__restrict__ d, double a0, double a2, double a3, double a6, double a7,
+                                  long n)
+{
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double u = uc[i], uo = um[i], vo = vm[i], ao = am[i];
+    const double a = a0 * (u - uo) - a2 * vo - a3 * ao;
+    const double v = vo + a6 * ao + a7 * a;
+    ac[i] = a;
+    vc[i] = v;
+    um[i] = u;
+    vm[i] = v;
+    am[i] = a;
+    d[i] = u;
+}
+
 // dd sign (correctors solve for -dd, main.c:3625-3631), d_temp += dd, the
 // Newmark kinematics of main.c:3634-3639 and x_temp += dd (updatc).
 __global__ void nm_update_kernel(double *__restrict__ dd, int neg, double *__restrict__ d_temp,
@@ -500,6 +540,18 @@ void launch_nm_reff(int mode, double sub_dt, double lpf, double alpham, double a
 {
     nm_reff_kernel<<<nb(n), kT, 0, st>>>(mode, sub_dt, lpf, alpham, alphaf, a2, a3, pin_km1, pin_k, f_temp, sm,
                                          vc_i, ac_i, qtot, reff, n);
+}
+void launch_lin_reff(int first, double alpham, double alphaf, double a0, double a2, double a3,
+                     const double *pin_km1, const double *pin_k, const double *sm, const double *um,
+                     const double *vm, const double *am, const double *nku, double *reff, long n, cudaStream_t st)
+{
+    lin_reff_kernel<<<nb(n), kT, 0, st>>>(first, alpham, alphaf, a0, a2, a3, pin_km1, pin_k, sm, um, vm, am, nku,
+                                           reff, n);
+}
+void launch_lin_update(const double *uc, double *um, double *vm, double *am, double *vc, double *ac, double *d,
+                       double a0, double a2, double a3, double a6, double a7, long n, cudaStream_t st)
+{
+    lin_update_kernel<<<nb(n), kT, 0, st>>>(uc, um, vm, am, vc, ac, d, a0, a2, a3, a6, a7, n);
 }
 template <typename T>
 void launch_nm_keff(T *band, long ld, const double *sm, double c0, double den, long n, cudaStream_t st)

@@ -135,3 +135,32 @@ def test_newton_raphson_models_parse_and_fgmres_is_refused_for_them(lib):
         rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
         lib.cb_model_destroy(h)
         assert rc == 4
+
+
+def test_linear_newmark_models_take_the_fp64_band_only(lib):
+    """ALGFLAG 4 (ANAFLAG 1) parses; it factors its effective stiffness once
+    with the FP64 band, so FGMRES and the other precisions are refused before
+    any upload."""
+    from cubens import models
+    text = models.frame_building(2, 2, 3, steps=10, dt=0.005, seed=3, linear=True).text.encode()
+    opt = cubens.Options()
+    lib.cb_default_options(C.byref(opt))
+    h = C.c_void_p()
+    rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
+    msg = lib.cb_last_error(h).decode()
+    lib.cb_model_destroy(h)
+    assert rc in (0, 3), (rc, msg)  # 3: no CUDA device here
+    for solver, precision in ((cubens.SOLVER_FGMRES, cubens.FP64), (cubens.SOLVER_BAND, cubens.MIXED)):
+        opt.solver, opt.precision = solver, precision
+        h = C.c_void_p()
+        rc = lib.cb_model_create(text, len(text), C.byref(opt), C.byref(h))
+        msg = lib.cb_last_error(h).decode()
+        lib.cb_model_destroy(h)
+        assert rc == 4 and "linear Newmark" in msg, (rc, msg)
+    # ALGFLAG 4 with ANAFLAG 2 is not an analysis the reference runs (main.c:393)
+    bad = b"2" + text[1:]
+    h = C.c_void_p()
+    opt.solver, opt.precision = cubens.SOLVER_BAND, cubens.FP64
+    rc = lib.cb_model_create(bad, len(bad), C.byref(opt), C.byref(h))
+    lib.cb_model_destroy(h)
+    assert rc == 4
