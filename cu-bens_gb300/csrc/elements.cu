@@ -21,6 +21,33 @@ inline unsigned blocks_for(long n, int t = kThreads) { return (unsigned)((n + t 
 
 // Initial shell geometry, local coordinates and element stiffnesses
 // (prop_sh shell.c:61-95, stiffe_m_sh, stiffe_b_sh), once per model.
+// Lumped shell mass (mass_sh, shell.c:1505-1592), one thread per element:
+// Mtot = rho A t with the face area from the coordinates x, Mtot/3 at each
+// vertex's translations and Mtot/3 t^2/12 at its rotations, in the element
+// force buffer's layout [k * E + e] (gathered into the equations like forces).
+__global__ void shell_mass_kernel(DevShell s, const double *__restrict__ x, const double *__restrict__ dens,
+                                  double *__restrict__ me, long E)
+{
+    long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double p[3][3];
+    for (int a = 0; a < 3; ++a) {
+        int n = s.conn[a * E + e];
+        for (int m = 0; m < 3; ++m) p[a][m] = x[n * 3 + m];
+    }
+    double el12[3], el31[3];
+    for (int m = 0; m < 3; ++m) {
+        el31[m] = p[2][m] - p[0][m];
+        el12[m] = p[1][m] - p[0][m];
+    }
+    const double n0 = el12[1] * el31[2] - el12[2] * el31[1], n1 = el12[2] * el31[0] - el12[0] * el31[2],
+                 n2 = el12[0] * el31[1] - el12[1] * el31[0];
+    const double area = 0.5 * sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    const double t = s.prop[2 * E + e], mtot = dens[e] * area * t;
+    const double mt = mtot / 3, mr = mtot / 3 * (t * t) / 12;
+    for (int k = 0; k < 18; ++k) me[k * E + e] = (k % 6) < 3 ? mt : mr;
+}
+
 __global__ void shell_setup_kernel(DevShell s, const double *__restrict__ x0, long E)
 {
     long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -295,6 +322,11 @@ __global__ void update_coords_kernel(const int *__restrict__ eq_x, const double 
 
 }  // namespace
 
+void launch_shell_mass(const DevShell &s, const double *x, const double *dens, double *me, long ne,
+                       cudaStream_t st)
+{
+    if (ne > 0) shell_mass_kernel<<<blocks_for(ne), kThreads, 0, st>>>(s, x, dens, me, ne);
+}
 void launch_shell_setup(const DevShell &s, const double *x0, long ne, cudaStream_t st)
 {
     if (ne > 0) shell_setup_kernel<<<blocks_for(ne, 64), 64, 0, st>>>(s, x0, ne);

@@ -361,6 +361,9 @@ double mpnn_train(Mpnn &mp, const KrylovSolver &ks, int steps, cudaStream_t st);
 // Kernel entry points (host wrappers)
 // ---------------------------------------------------------------------------
 void launch_shell_setup(const DevShell &s, const double *x0, long ne, cudaStream_t st);
+// lumped shell mass (mass_sh) into the element buffer layout me[k * E + e]
+void launch_shell_mass(const DevShell &s, const double *x, const double *dens, double *me, long ne,
+                       cudaStream_t st);
 void launch_shell_forces(const DevShell &s, const double *x_t, const double *dd, double *fe,
                          long ne, cudaStream_t st);
 void launch_truss_forces(const DevTruss &t, const double *x_t, double *fe, long nt,

@@ -116,6 +116,7 @@ struct cb_model {
     // arc-length with FGMRES: pivots of the LDL^T of each joint's diagonal
     // block (psi), and the converged increments so far (learning schedule)
     double *bpiv = nullptr;
+    double *sh_dens = nullptr;  // linear Newmark with shells: densities (mass_sh)
     long msal_incs = 0;
 
     // timing

@@ -99,10 +99,11 @@ std::string parse_model_def(const char *text, size_t len, HostModel &m, int &sta
         status = CB_ERR_UNSUPPORTED;
         return "brick elements are not on the GPU path";
     }
-    if (alg >= 4 && (m.ne_tr || m.ne_sh)) {
+    if ((alg == 5 && (m.ne_tr || m.ne_sh)) || (alg == 4 && (m.ne_tr || (m.ne_sh && m.ne_fr)))) {
         status = CB_ERR_UNSUPPORTED;
-        return "the GPU Newmark path takes frame-only models (mass_fr indexes its properties without "
-               "the truss offset, frame.c:1357-1363)";
+        return "the GPU Newmark path takes frame-only models, and the linear one also shell-only models "
+               "(the mass routines index the shared density array without the element-type offsets, "
+               "frame.c:1357-1363, shell.c:1558)";
     }
     const long NJ = m.nj, F = m.ne_fr;
     std::vector<char> has_tr(NJ, 0), has_sh(NJ, 0);

@@ -152,7 +152,11 @@ void upload_model(cb_model *m)
         for (double **v : {&m->uc, &m->vc, &m->ac, &m->uc_i, &m->vc_i, &m->ac_i, &m->um, &m->vm, &m->am, &m->sm,
                            &m->qtot, &m->dyn, &m->fp})
             *v = m->alloc<double>(N);
-        m->me = m->alloc<double>(14 * F);
+        m->me = m->alloc<double>(18 * E + 6 * T + 14 * F);  // element masses in the force buffer's layout
+        if (E) {
+            m->sh_dens = m->alloc<double>(E);
+            h2d(m->sh_dens, h.echo.sh_dens.data(), E, st);
+        }
         m->pin = m->alloc<double>(h.pin.size());
         h2d(m->pin, h.pin.data(), h.pin.size(), st);
     }

@@ -409,9 +409,9 @@ LinearCoeffs linear_coeffs(const NewmarkParams &p, double dt)
 }
 
 // The stiffness of the initial state (the element forces are zero, so the
-// frame tangent is stiffe alone, as ANAFLAG 1 forms it), kept for K u_m; the
-// lumped mass; K_eff = K + a0 (1 - am) / (1 - af) M factored once; the
-// motion from the initial conditions.
+// frame and shell tangents are stiffe alone, as ANAFLAG 1 forms them), kept
+// for K u_m; the lumped mass (mass_fr or mass_sh); K_eff = K + a0 (1 - am) /
+// (1 - af) M factored once; the motion from the initial conditions.
 void linear_begin(cb_model *m)
 {
     newmark_begin(m);
@@ -424,7 +424,9 @@ void linear_begin(cb_model *m)
     d2d(m->band64, (const double *)m->bf.band, (size_t)m->bf.ld * m->bf.nblk * m->bf.s, st);
     {
         PhaseTimer t(m, &m->tm.ms_tangent);
-        cb::launch_frame_mass(m->fr, m->x_c, m->fr_lref, m->me, F, st);
+        const long E = h.ne_sh, T = h.ne_tr;
+        if (E) cb::launch_shell_mass(m->sh, m->x_c, m->sh_dens, m->me, E, st);
+        if (F) cb::launch_frame_mass(m->fr, m->x_c, m->fr_lref, m->me + 18 * E + 6 * T, F, st);
         cb::launch_gather_f64(m->fmap_ptr, m->fmap_src, m->me, m->sm, N, st);
         cb::launch_nm_keff<double>((double *)m->bf.band, m->bf.ld, m->sm, c.a0 * (1 - p.alpham), 1 - p.alphaf, N,
                                    st);

@@ -243,6 +243,34 @@ def cylindrical_panel(n: int = 64, seed: int | None = None, imperfection: float 
                                         "imperfection_amplitudes": amps.tolist()})
 
 
+def shell_panel_linear(n: int = 8, steps: int = 40, dt: float = 0.01, peak: float = -1.0,
+                       numopt: int = 1, spectrds: float = 0.8, dens: float = 1.0) -> ModelSpec:
+    """The hinged cylindrical panel of ``cylindrical_panel`` as a linear
+    dynamic model (ANAFLAG 1, ALGFLAG 4, main.c:3143-3302): density ``dens``,
+    a half-sine pulse of ``peak`` in direction 3 at the centre joint over the
+    first quarter of the ``steps`` time steps of ``dt``, then free vibration;
+    Newmark controls numopt and spectrds (main.c:3184) and lpfmax 1."""
+    base = cylindrical_panel(n).text.splitlines()
+    ne = 2 * n * n
+    nj = (n + 1) * (n + 1)
+    centre = n // 2 * (n + 1) + n // 2 + 1
+    # the MSAL text: flags, incidences, constraints ... "0,0", coordinates,
+    # properties, then the loads and controls, which are replaced
+    i_cons_end = base.index("0,0")
+    head = base[4:i_cons_end + 1]                     # NJ, counts, incidences, constraints, "0,0"
+    coords = base[i_cons_end + 1:i_cons_end + 1 + nj]
+    props = [f"{_fmt(PANEL_E)},{_fmt(PANEL_NU)},{_fmt(PANEL_T)},{_fmt(dens)},1e30"] * ne
+    out = ["1", "4", "0,0", "0", "1"] + head + ["0,0"] + coords + props
+    out.append(f"{steps},{_fmt(steps * dt)}")
+    npulse = max(2, steps // 4)
+    for k in range(steps + 1):
+        v = peak * math.sin(math.pi * k / npulse) if k <= npulse else 0.0
+        out.append(f"{centre},3,{_fmt(v)}")
+    out += ["0,0,0", "0,0,0", "0,0,0,0,0", f"{numopt},{spectrds!r}", "1.0"]
+    return ModelSpec(f"panel{n}_linear", "\n".join(out) + "\n", nj=nj, ne_sh=ne,
+                     params={"n": n, "centre": centre, "steps": steps, "dt": dt})
+
+
 def batch_sizes(count: int = 512, seed: int = 2024,
                 choices: tuple[int, ...] = tuple(range(16, 97, 8))) -> list[int]:
     """Mesh sizes drawn uniformly from {16, 24, ..., 96}, seeded."""

@@ -189,7 +189,8 @@ int cb_newton_step(cb_model *m, cb_step *out);
  * halving included) and returns CB_OK with out->done = 1 once all NTSTPS
  * steps are taken. cb_get_displacements then returns d; cb_newmark_state
  * the displacement, velocity and acceleration (NEQ each; any may be NULL).
- * Linear Newmark models (ANAFLAG 1 with ALGFLAG 4, frames, FP64 band) use the
+ * Linear Newmark models (ANAFLAG 1 with ALGFLAG 4, frame-only or shell-only,
+ * FP64 band) use the
  * same calls: cb_newmark_begin forms the stiffness of the initial state and
  * the lumped mass and factors the effective stiffness once (main.c:3143-3302,
  * solve.c:139-222); each cb_newmark_step solves one time step k of

@@ -39,7 +39,7 @@ struct orc_model {
     double *tr_e, *tr_a, *tr_len0, *tr_dir0; /* dir0: NE_TR*3 */
     /* shell */
     long *sh_conn;   /* NE_SH*3 (0-based joints) */
-    double *sh_e, *sh_nu, *sh_t;
+    double *sh_e, *sh_nu, *sh_t, *sh_dens;
     double *sh_xl;   /* NE_SH*3 local x2, x3, y3 of the initial geometry */
     double *sh_area0;
     double *sh_slen0; /* NE_SH*3 initial side lengths l12, l23, l31 */
@@ -302,6 +302,7 @@ void orc_free(orc_model *m)
     free(m->sh_t);
     free(m->sh_xl);
     free(m->sh_area0);
+    free(m->sh_dens);
     free(m->sh_slen0);
     free(m->sh_c0);
     free(m->sh_kem);
@@ -376,8 +377,10 @@ orc_model *orc_load(const char *text, char *err, int errlen)
     m->ne_sh = (long)tok_num(&t);
     long nsbr = (long)tok_num(&t), nfbr = (long)tok_num(&t);
     if (nsbr || nfbr || !t.ok) return load_fail(m, err, errlen, "brick elements are not supported");
-    if (alg >= 4 && (m->ne_tr || m->ne_sh))
-        return load_fail(m, err, errlen, "the Newmark oracle supports frame-only models");
+    if (alg == 5 && (m->ne_tr || m->ne_sh))
+        return load_fail(m, err, errlen, "the nonlinear Newmark oracle supports frame-only models");
+    if (alg == 4 && (m->ne_tr || (m->ne_sh && m->ne_fr)))
+        return load_fail(m, err, errlen, "the linear Newmark oracle supports frame-only or shell-only models");
     long NJ = m->nj;
     m->tr_conn = calloc((size_t)(2 * m->ne_tr + 1), sizeof(long));
     m->fr_conn = calloc((size_t)(2 * m->ne_fr + 1), sizeof(long));
@@ -537,6 +540,7 @@ orc_model *orc_load(const char *text, char *err, int errlen)
     m->sh_e = calloc((size_t)E + 1, sizeof(double));
     m->sh_nu = calloc((size_t)E + 1, sizeof(double));
     m->sh_t = calloc((size_t)E + 1, sizeof(double));
+    m->sh_dens = calloc((size_t)E + 1, sizeof(double));
     m->sh_xl = calloc((size_t)E * 3 + 1, sizeof(double));
     m->sh_area0 = calloc((size_t)E + 1, sizeof(double));
     m->sh_slen0 = calloc((size_t)E * 3 + 1, sizeof(double));
@@ -547,8 +551,8 @@ orc_model *orc_load(const char *text, char *err, int errlen)
         m->sh_e[i] = tok_num(&t);
         m->sh_nu[i] = tok_num(&t);
         m->sh_t[i] = tok_num(&t);
-        (void)tok_num(&t); /* density */
-        (void)tok_num(&t); /* yield */
+        m->sh_dens[i] = tok_num(&t); /* density (mass_sh) */
+        (void)tok_num(&t);            /* yield */
         const double *p1 = m->x0 + m->sh_conn[i * 3] * 3, *p2 = m->x0 + m->sh_conn[i * 3 + 1] * 3,
                      *p3 = m->x0 + m->sh_conn[i * 3 + 2] * 3;
         shell_geometry(p1, p2, p3, m->sh_c0 + i * 9, m->sh_area0 + i, m->sh_slen0 + i * 3);
@@ -1775,6 +1779,30 @@ done:
  * accepted pass, d[k*NEQ ...] (may be NULL), res[k] = |dyn - f| / |dyn| with
  * dyn = qtot - M a (the dynamic equilibrium the convergence test judges).
  * Returns the number of steps recorded, or -(error code) with err set. */
+/* Lumped shell mass (mass_sh, shell.c:1505-1592): Mtot = rho A t with the
+ * face area from the coordinates x, Mtot/3 at each vertex's translations and
+ * Mtot/3 t^2/12 at its rotations, added to sm[eq] element by element. */
+static void shell_mass(const orc_model *m, const double *x, double *sm)
+{
+    for (long s = 0; s < m->ne_sh; ++s) {
+        const double *p0 = x + m->sh_conn[s * 3] * 3, *p1 = x + m->sh_conn[s * 3 + 1] * 3,
+                     *p2 = x + m->sh_conn[s * 3 + 2] * 3;
+        double el12[3], el31[3], nrm[3];
+        for (int k = 0; k < 3; ++k) {
+            el31[k] = p2[k] - p0[k];
+            el12[k] = p1[k] - p0[k];
+        }
+        cross3(el12, el31, nrm, 0);
+        const double area = 0.5 * sqrt(dot3(nrm, nrm));
+        const double t = m->sh_t[s], mtot = m->sh_dens[s] * area * t;
+        const double mt = mtot / 3, mr = mtot / 3 * pow(t, 2) / 12;
+        long mc[18];
+        shell_mcode(m, s, mc);
+        for (int i = 0; i < 18; ++i)
+            if (mc[i]) sm[mc[i] - 1] += (i % 6) < 3 ? mt : mr;
+    }
+}
+
 /* y = K x for the symmetric skyline K (skymult, solve.c:700-757): column n
  * holds K(n, n) at maxa[n-1] and the entries above it after; the upper
  * triangle's columns are applied from the last one, then the diagonal, then
@@ -1840,9 +1868,11 @@ int orc_linear_newmark(orc_model *m, long max_steps, double *time_out, double *d
     const double a0 = 1 / (alpha * pow(dt_temp, 2)), a2 = 1 / (alpha * dt_temp), a3 = 1 / (2 * alpha) - 1;
     const double a6 = (dt_temp) * (1 - delta), a7 = delta * (dt_temp);
     /* stiffness of the initial state (the element forces are zero, so the
-     * geometric terms vanish: stiffe alone, as ANAFLAG 1 forms it) and mass */
-    tangent_all(m, m->x0, NULL, NULL, NULL, NULL, NULL, m->fr_c0, ef0, m->fr_len0, m->fr_len0, ss);
-    orc_frame_mass(m, m->x0, sm);
+     * geometric terms vanish: stiffe alone, as ANAFLAG 1 forms it) and the
+     * lumped mass (mass_fr or mass_sh) */
+    tangent_all(m, m->x0, m->sh_c0, m->sh_area0, NULL, NULL, NULL, m->fr_c0, ef0, m->fr_len0, m->fr_len0, ss);
+    if (m->ne_fr) orc_frame_mass(m, m->x0, sm);
+    if (m->ne_sh) shell_mass(m, m->x0, sm);
     memcpy(keff, ss, sizeof(double) * (size_t)m->lss);
     for (long i = 0; i < N; ++i) keff[m->maxa[i] - 1] += a0 * (1 - alpham) * sm[i] / (1 - alphaf);
     int det = 0;

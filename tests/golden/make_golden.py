@@ -161,14 +161,17 @@ def linear_cases():
 def linear_runs():
     """The reference's own linear Newmark runs: per time step the time and d
     (output() records; the reference's closing record, lpfmax with zero d, is
-    dropped)."""
-    for w, m in linear_cases().items():
+    dropped). Frames (warping fixed and per member) and the DKT panel with
+    its lumped shell mass (mass_sh)."""
+    cases = {f"frame_linear_{w}": m for w, m in linear_cases().items()}
+    cases["panel8_linear"] = models.shell_panel_linear(8, steps=40, dt=0.01)
+    for name, m in cases.items():
         r = refrun.run(m.text, 1000, timeout=600)
         assert r["returncode"] == 0, r["results1"][-400:]
         n = len(r["lam"]) - 1
-        np.savez_compressed(OUT / f"run_frame_linear_{w}.npz", model_def=np.array(m.text), time=r["lam"][:n],
+        np.savez_compressed(OUT / f"run_{name}.npz", model_def=np.array(m.text), time=r["lam"][:n],
                             d=r["d"][:n], neq=r["neq"], results_tail=np.array(r["results1"][-200:]))
-        print("linear", w, "neq", r["neq"], "steps", n)
+        print("linear", name, "neq", r["neq"], "steps", n)
 
 
 def results1_cases():

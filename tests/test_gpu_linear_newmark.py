@@ -3,8 +3,9 @@ own runs: the stiffness of the initial state and the lumped mass, the
 effective stiffness factored once in FP64, then per time step one solve and
 the kinematics (main.c:3143-3302, solve.c:139-222 and 246-467). The runs use
 numopt 1 (HHT-type dissipation, so the K u_m term of the effective load is
-active) and initial conditions; warping fixed and one warping DOF per member
-end. The path is linear and FP64, so the displacement history agrees to
+active): frames with initial conditions, warping fixed and one warping DOF
+per member end, and the DKT panel with its lumped shell mass (mass_sh,
+shell.c:1505-1592) under a pulse at its centre. The path is linear and FP64, so the displacement history agrees to
 1e-10 relative (the band LDL^T and the reference's skyline LDL^T sum in
 different orders)."""
 import numpy as np
@@ -15,9 +16,9 @@ import cubens
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("warping", ["fixed", "member"])
-def test_linear_newmark_matches_reference(golden_dir, warping, tmp_path):
-    z = np.load(golden_dir / f"run_frame_linear_{warping}.npz")
+@pytest.mark.parametrize("name", ["frame_linear_fixed", "frame_linear_member", "panel8_linear"])
+def test_linear_newmark_matches_reference(golden_dir, name, tmp_path):
+    z = np.load(golden_dir / f"run_{name}.npz")
     steps = len(z["time"])
     m = cubens.Model(str(z["model_def"]))
     assert m.info["algflag"] == 4 and m.info["nsteps"] == steps

@@ -157,6 +157,14 @@ def test_linear_newmark_models_take_the_fp64_band_only(lib):
         msg = lib.cb_last_error(h).decode()
         lib.cb_model_destroy(h)
         assert rc == 4 and "linear Newmark" in msg, (rc, msg)
+    # the DKT panel with its lumped shell mass parses too
+    panel = models.shell_panel_linear(8, steps=10).text.encode()
+    opt.solver, opt.precision = cubens.SOLVER_BAND, cubens.FP64
+    h = C.c_void_p()
+    rc = lib.cb_model_create(panel, len(panel), C.byref(opt), C.byref(h))
+    msg = lib.cb_last_error(h).decode()
+    lib.cb_model_destroy(h)
+    assert rc in (0, 3), (rc, msg)
     # ALGFLAG 4 with ANAFLAG 2 is not an analysis the reference runs (main.c:393)
     bad = b"2" + text[1:]
     h = C.c_void_p()

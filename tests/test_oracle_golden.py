@@ -100,12 +100,12 @@ def test_frame_forces_tangent_mass_match_reference(golden_dir):
     np.testing.assert_array_equal(sm, z["sm"])
 
 
-@pytest.mark.parametrize("warping", ["fixed", "member"])
-def test_linear_newmark_path_matches_reference(golden_dir, warping):
-    """Linear Newmark (ANAFLAG 1, ALGFLAG 4) with HHT-type dissipation and
-    initial conditions: the oracle's displacements per time step equal the
-    reference's bit for bit."""
-    z = np.load(golden_dir / f"run_frame_linear_{warping}.npz")
+@pytest.mark.parametrize("name", ["frame_linear_fixed", "frame_linear_member", "panel8_linear"])
+def test_linear_newmark_path_matches_reference(golden_dir, name):
+    """Linear Newmark (ANAFLAG 1, ALGFLAG 4) with HHT-type dissipation: frames
+    with initial conditions, and the DKT panel with its lumped shell mass. The
+    oracle's displacements per time step equal the reference's bit for bit."""
+    z = np.load(golden_dir / f"run_{name}.npz")
     steps = len(z["time"])
     o = oracle.OracleModel(str(z["model_def"])).linear_newmark(steps)
     assert o["rc"] == steps
